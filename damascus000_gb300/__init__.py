@@ -1,0 +1,534 @@
+"""GB300 (sm_103a) Damascus Fold prover/verifier -- Python binding of the C ABI.
+
+The compute path is ``libdamascus_gb300.so`` (hand-written CUDA for sm_103a plus
+the C++ host runtime) built in-tree by :mod:`damascus000_gb300.build` and
+loaded here through ctypes.  The classes mirror the reference crate's public API
+(``DamascusProver``, ``DamascusVerifier``, ``ModuleSisCommitter``,
+``negacyclic_multiply``), with field elements as Python ints and serialized
+objects as bincode bytes identical to the reference's.
+
+There is no CPU fallback: creating a :class:`Context` without a GB300 raises
+:class:`DamascusError`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+from typing import Iterable, List, Optional, Sequence, Tuple
+
+from . import build as _build
+
+Q = (1 << 112) - 75
+MODULE_RANK = 8
+MIN_FOLD_DEPTH = 6
+BYTES_PER_COEFF = 13
+CRT_PRIMES = (3892314113, 2281701377, 2013265921, 2885681153,
+              2483027969, 1811939329, 469762049, 4194304001)
+DEFAULT_GENERATOR_SEED = bytes([7]) * 32
+DEFAULT_EPOCH_SEED = bytes([11]) * 32
+DEFAULT_MEMORY_LIMIT_BYTES = 512 * 1024 * 1024
+
+OK = 0
+EINVAL, ENOMEM_BUDGET, ECUDA, ETIMEOUT, EVERIFY, EINVARIANT, ESTATE, ESIZE, EDESERIALIZE, EUNSUPPORTED = \
+    -1, -2, -3, -4, -5, -6, -7, -8, -9, -10
+_CODE_NAMES = {EINVAL: "EINVAL", ENOMEM_BUDGET: "ENOMEM_BUDGET", ECUDA: "ECUDA", ETIMEOUT: "ETIMEOUT",
+               EVERIFY: "EVERIFY", EINVARIANT: "EINVARIANT", ESTATE: "ESTATE", ESIZE: "ESIZE",
+               EDESERIALIZE: "EDESERIALIZE", EUNSUPPORTED: "EUNSUPPORTED"}
+
+#: every symbol include/damascus.h declares
+EXPORTED_SYMBOLS = (
+    "damascus_ctx_create", "damascus_ctx_destroy", "damascus_last_error", "damascus_create_error",
+    "damascus_ctx_budget", "damascus_ctx_reserved",
+    "damascus_fp_add", "damascus_fp_sub", "damascus_fp_mul", "damascus_fp_inv",
+    "damascus_fp_from_le_bytes_mod_order", "damascus_blake3", "damascus_blake3_keyed",
+    "damascus_transcript_challenge", "damascus_coeff_count_for_byte_len", "damascus_layout_for_byte_len",
+    "damascus_proof_size", "damascus_record_size", "damascus_statement_size", "damascus_prover_footprint",
+    "damascus_file_id", "damascus_derive_generators", "damascus_commit_with_generators", "damascus_commit",
+    "damascus_ring_mul_batch", "damascus_ring_mul_batch_device",
+    "damascus_prover_new", "damascus_prover_free", "damascus_prover_rounds_total",
+    "damascus_prover_current_round", "damascus_prover_dimensions", "damascus_prover_statement",
+    "damascus_prover_current_commitment", "damascus_prover_fold_round", "damascus_prover_final_opening",
+    "damascus_prove", "damascus_prove_device", "damascus_prove_device_timed", "damascus_ctx_flush_l2",
+    "damascus_verifier_new", "damascus_verifier_free", "damascus_verifier_update_commitment",
+    "damascus_verifier_verify_final_opening", "damascus_verifier_round", "damascus_verifier_dimensions",
+    "damascus_verify", "damascus_cuda_fold_batch", "damascus_cuda_ntt_batch",
+    "damascus_ctx_set_profiling", "damascus_ctx_reset_stats", "damascus_ctx_kernel_stat",
+    "damascus_ctx_synchronize",
+)
+
+
+class DamascusError(RuntimeError):
+    def __init__(self, code: int, message: str = ""):
+        self.code = code
+        super().__init__(f"{_CODE_NAMES.get(code, code)}: {message}")
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def library_path() -> Path:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads libdamascus_gb300.so (building it in-tree when missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    path = library_path()
+    if not path.exists():
+        raise DamascusError(ECUDA, f"{path} is missing; run damascus000_gb300.build.build()")
+    L = ctypes.CDLL(str(path))
+    _declare(L)
+    _lib = L
+    return L
+
+
+def _declare(L: ctypes.CDLL) -> None:
+    vp, sz, u64, u32, i32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int
+    cp = ctypes.c_char_p
+    P = ctypes.POINTER
+
+    def sig(name, res, *args):
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = list(args)
+
+    sig("damascus_ctx_create", i32, i32, u64, P(vp))
+    sig("damascus_ctx_destroy", None, vp)
+    sig("damascus_last_error", cp, vp)
+    sig("damascus_create_error", cp)
+    sig("damascus_ctx_budget", u64, vp)
+    sig("damascus_ctx_reserved", u64, vp)
+    for n in ("damascus_fp_add", "damascus_fp_sub", "damascus_fp_mul"):
+        sig(n, None, cp, cp, vp)
+    sig("damascus_fp_inv", None, cp, vp)
+    sig("damascus_fp_from_le_bytes_mod_order", None, cp, sz, vp)
+    sig("damascus_blake3", None, cp, sz, vp)
+    sig("damascus_blake3_keyed", None, cp, cp, sz, vp)
+    sig("damascus_transcript_challenge", i32, cp, cp, cp, u64, cp, u64, cp, u64, cp, u64, vp)
+    sig("damascus_coeff_count_for_byte_len", u64, u64)
+    sig("damascus_layout_for_byte_len", i32, u64, P(u32), P(u64))
+    sig("damascus_proof_size", sz, u64)
+    sig("damascus_record_size", sz, u64, u64)
+    sig("damascus_statement_size", sz, u64)
+    sig("damascus_prover_footprint", u64, u64)
+    sig("damascus_file_id", i32, vp, cp, sz, vp)
+    sig("damascus_derive_generators", i32, vp, cp, u64, u64, vp)
+    sig("damascus_commit_with_generators", i32, vp, cp, cp, u64, u64, vp)
+    sig("damascus_commit", i32, vp, cp, sz, cp, vp, sz, P(sz))
+    sig("damascus_ring_mul_batch", i32, vp, cp, cp, vp, u64, u64)
+    sig("damascus_ring_mul_batch_device", i32, vp, vp, vp, vp, u64, u64, i32)
+    sig("damascus_prover_new", i32, vp, cp, sz, cp, cp, u64, P(vp))
+    sig("damascus_prover_free", None, vp)
+    sig("damascus_prover_rounds_total", u32, vp)
+    sig("damascus_prover_current_round", u64, vp)
+    sig("damascus_prover_dimensions", None, vp, P(u64), P(u64))
+    sig("damascus_prover_statement", i32, vp, vp, sz, P(sz))
+    sig("damascus_prover_current_commitment", i32, vp, vp, sz, P(sz))
+    sig("damascus_prover_fold_round", i32, vp, u64, vp, sz, P(sz))
+    sig("damascus_prover_final_opening", i32, vp, vp)
+    sig("damascus_prove", i32, vp, cp, sz, cp, cp, vp, sz, P(sz))
+    sig("damascus_prove_device", i32, vp, vp, sz, cp, cp, vp, sz, P(sz))
+    sig("damascus_prove_device_timed", i32, vp, vp, sz, cp, cp, vp, sz, P(sz), P(ctypes.c_double))
+    sig("damascus_ctx_flush_l2", i32, vp)
+    sig("damascus_verifier_new", i32, vp, cp, sz, cp, P(vp))
+    sig("damascus_verifier_free", None, vp)
+    sig("damascus_verifier_update_commitment", i32, vp, cp, sz)
+    sig("damascus_verifier_verify_final_opening", i32, vp, cp)
+    sig("damascus_verifier_round", u64, vp)
+    sig("damascus_verifier_dimensions", None, vp, P(u64), P(u64))
+    sig("damascus_verify", i32, vp, cp, sz, cp)
+    sig("damascus_cuda_fold_batch", i32, vp, vp, vp, vp, vp, vp, sz, u64, u64)
+    sig("damascus_cuda_ntt_batch", i32, vp, vp, vp, sz, vp, vp, vp, vp)
+    sig("damascus_ctx_set_profiling", i32, vp, i32)
+    sig("damascus_ctx_reset_stats", None, vp)
+    sig("damascus_ctx_kernel_stat", i32, vp, cp, P(u64), P(ctypes.c_double), P(ctypes.c_double),
+        P(ctypes.c_double))
+    sig("damascus_ctx_synchronize", i32, vp)
+
+
+# ------------------------------------------------------------------ encoding helpers
+def fe(v: int) -> bytes:
+    return int(v).to_bytes(16, "little")
+
+
+def fe_vec(vals: Iterable[int]) -> bytes:
+    return b"".join(int(v).to_bytes(16, "little") for v in vals)
+
+
+def unfe_vec(b: bytes) -> List[int]:
+    return [int.from_bytes(b[i:i + 16], "little") for i in range(0, len(b), 16)]
+
+
+# ------------------------------------------------------------------ host-side API (no GPU needed)
+def fp_mul(a: int, b: int) -> int:
+    out = ctypes.create_string_buffer(16)
+    load().damascus_fp_mul(fe(a), fe(b), out)
+    return int.from_bytes(out.raw, "little")
+
+
+def fp_add(a: int, b: int) -> int:
+    out = ctypes.create_string_buffer(16)
+    load().damascus_fp_add(fe(a), fe(b), out)
+    return int.from_bytes(out.raw, "little")
+
+
+def fp_sub(a: int, b: int) -> int:
+    out = ctypes.create_string_buffer(16)
+    load().damascus_fp_sub(fe(a), fe(b), out)
+    return int.from_bytes(out.raw, "little")
+
+
+def fp_inv(a: int) -> int:
+    out = ctypes.create_string_buffer(16)
+    load().damascus_fp_inv(fe(a), out)
+    return int.from_bytes(out.raw, "little")
+
+
+def fp_from_le_bytes_mod_order(b: bytes) -> int:
+    out = ctypes.create_string_buffer(16)
+    load().damascus_fp_from_le_bytes_mod_order(b, len(b), out)
+    return int.from_bytes(out.raw, "little")
+
+
+def blake3(data: bytes) -> bytes:
+    out = ctypes.create_string_buffer(32)
+    load().damascus_blake3(data, len(data), out)
+    return out.raw
+
+
+def blake3_keyed(key: bytes, data: bytes) -> bytes:
+    out = ctypes.create_string_buffer(32)
+    load().damascus_blake3_keyed(key, data, len(data), out)
+    return out.raw
+
+
+def transcript_challenge(epoch_seed: bytes, file_id: bytes, label: str, rnd: int,
+                         c: bytes, n_c: int, l: bytes, n_l: int, r: bytes, n_r: int) -> int:
+    out = ctypes.create_string_buffer(16)
+    rc = load().damascus_transcript_challenge(epoch_seed, file_id, label.encode(), rnd, c, n_c, l, n_l, r, n_r,
+                                              out)
+    if rc:
+        raise DamascusError(rc, "transcript challenge")
+    return int.from_bytes(out.raw, "little")
+
+
+def coeff_count_for_byte_len(n: int) -> int:
+    return load().damascus_coeff_count_for_byte_len(n)
+
+
+def layout_for_byte_len(n: int) -> Tuple[int, int]:
+    d, dim = ctypes.c_uint32(), ctypes.c_uint64()
+    rc = load().damascus_layout_for_byte_len(n, ctypes.byref(d), ctypes.byref(dim))
+    if rc:
+        raise DamascusError(rc, "layout")
+    return d.value, dim.value
+
+
+def proof_size(file_len: int) -> int:
+    return load().damascus_proof_size(file_len)
+
+
+def record_size(ring_len_vec: int, ring_len_poly: int) -> int:
+    return load().damascus_record_size(ring_len_vec, ring_len_poly)
+
+
+def statement_size(ring_len: int) -> int:
+    return load().damascus_statement_size(ring_len)
+
+
+def prover_footprint(file_len: int) -> int:
+    return load().damascus_prover_footprint(file_len)
+
+
+def depth_j(d: int, j: int) -> Tuple[int, int]:
+    """(N_j, n_j) after j rounds (src/protocol/prover.rs:316-320)."""
+    assert j <= d, "round index exceeds fold depth"
+    dim = 1 << (d - j)
+    return dim, dim
+
+
+# ------------------------------------------------------------------ device API
+class Context:
+    """A GPU context: device, stream, twiddle/CRT tables and an HBM budget."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        L = load()
+        h = ctypes.c_void_p()
+        rc = L.damascus_ctx_create(device, hbm_budget_bytes, ctypes.byref(h))
+        if rc:
+            raise DamascusError(rc, L.damascus_create_error().decode())
+        self._h = h
+        self._lib = L
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.damascus_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def last_error(self) -> str:
+        return self._lib.damascus_last_error(self._h).decode()
+
+    def check(self, rc: int, what: str = "") -> None:
+        if rc:
+            raise DamascusError(rc, f"{what}: {self.last_error()}")
+
+    @property
+    def budget(self) -> int:
+        return self._lib.damascus_ctx_budget(self._h)
+
+    @property
+    def reserved(self) -> int:
+        return self._lib.damascus_ctx_reserved(self._h)
+
+    # -- profiling
+    def set_profiling(self, on: bool) -> None:
+        self.check(self._lib.damascus_ctx_set_profiling(self._h, int(on)), "set_profiling")
+
+    def reset_stats(self) -> None:
+        self._lib.damascus_ctx_reset_stats(self._h)
+
+    def kernel_stat(self, name: str):
+        """(launches, total_ms, algorithmic_bytes, algorithmic_ops) or None."""
+        n, ms, b, o = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        rc = self._lib.damascus_ctx_kernel_stat(self._h, name.encode(), ctypes.byref(n), ctypes.byref(ms),
+                                                ctypes.byref(b), ctypes.byref(o))
+        if rc:
+            return None
+        return n.value, ms.value, b.value, o.value
+
+    def synchronize(self) -> None:
+        self.check(self._lib.damascus_ctx_synchronize(self._h), "synchronize")
+
+    # -- commitment layer
+    def file_id(self, data: bytes) -> bytes:
+        out = ctypes.create_string_buffer(32)
+        self.check(self._lib.damascus_file_id(self._h, data, len(data), out), "file_id")
+        return out.raw
+
+    def derive_generators(self, g_seed: bytes, vector_len: int, ring_len: int) -> bytes:
+        out = ctypes.create_string_buffer(vector_len * MODULE_RANK * ring_len * 16)
+        self.check(self._lib.damascus_derive_generators(self._h, g_seed, vector_len, ring_len, out),
+                   "derive_generators")
+        return out.raw
+
+    def commit_with_generators(self, witness: bytes, generators: bytes, vector_len: int, ring_len: int) -> bytes:
+        out = ctypes.create_string_buffer(MODULE_RANK * ring_len * 16)
+        self.check(self._lib.damascus_commit_with_generators(self._h, witness, generators, vector_len, ring_len,
+                                                             out), "commit_with_generators")
+        return out.raw
+
+    def commit(self, data: bytes, seed_generators: bytes = DEFAULT_GENERATOR_SEED) -> bytes:
+        d, dim = layout_for_byte_len(len(data))
+        cap = statement_size(dim)
+        out = ctypes.create_string_buffer(cap)
+        n = ctypes.c_size_t()
+        self.check(self._lib.damascus_commit(self._h, data, len(data), seed_generators, out, cap, ctypes.byref(n)),
+                   "commit")
+        return out.raw[:n.value]
+
+    def ring_mul_batch(self, a: bytes, b: bytes, n: int, count: int) -> bytes:
+        out = ctypes.create_string_buffer(count * n * 16)
+        self.check(self._lib.damascus_ring_mul_batch(self._h, a, b, out, n, count), "ring_mul_batch")
+        return out.raw
+
+    def ring_mul_batch_device(self, d_a: int, d_b: int, d_out: int, n: int, count: int, sync: bool = True) -> None:
+        self.check(self._lib.damascus_ring_mul_batch_device(self._h, ctypes.c_void_p(d_a), ctypes.c_void_p(d_b),
+                                                            ctypes.c_void_p(d_out), n, count, int(sync)),
+                   "ring_mul_batch_device")
+
+    # -- protocol
+    def prove(self, data: bytes, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
+              epoch_seed: bytes = DEFAULT_EPOCH_SEED) -> bytes:
+        cap = proof_size(len(data))
+        out = ctypes.create_string_buffer(cap)
+        n = ctypes.c_size_t()
+        self.check(self._lib.damascus_prove(self._h, data, len(data), seed_generators, epoch_seed, out, cap,
+                                            ctypes.byref(n)), "prove")
+        return out.raw[:n.value]
+
+    def prove_device(self, d_file: int, length: int, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
+                     epoch_seed: bytes = DEFAULT_EPOCH_SEED, out=None) -> bytes:
+        cap = proof_size(length)
+        if out is None:
+            out = ctypes.create_string_buffer(cap)
+        n = ctypes.c_size_t()
+        self.check(self._lib.damascus_prove_device(self._h, ctypes.c_void_p(d_file), length, seed_generators,
+                                                   epoch_seed, out, cap, ctypes.byref(n)), "prove_device")
+        return out.raw[:n.value]
+
+    def prove_device_timed(self, d_file: int, length: int, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
+                           epoch_seed: bytes = DEFAULT_EPOCH_SEED, out=None):
+        """(proof bytes, device milliseconds) for a file already in device memory."""
+        cap = proof_size(length)
+        if out is None:
+            out = ctypes.create_string_buffer(cap)
+        n = ctypes.c_size_t()
+        ms = ctypes.c_double()
+        self.check(self._lib.damascus_prove_device_timed(self._h, ctypes.c_void_p(d_file), length, seed_generators,
+                                                         epoch_seed, out, cap, ctypes.byref(n), ctypes.byref(ms)),
+                   "prove_device_timed")
+        return out.raw[:n.value], ms.value
+
+    def flush_l2(self) -> None:
+        self.check(self._lib.damascus_ctx_flush_l2(self._h), "flush_l2")
+
+    def verify(self, proof: bytes, epoch_seed: bytes = DEFAULT_EPOCH_SEED) -> bool:
+        rc = self._lib.damascus_verify(self._h, proof, len(proof), epoch_seed)
+        if rc == EVERIFY or rc == EDESERIALIZE:
+            return False
+        self.check(rc, "verify")
+        return True
+
+
+class DamascusProver:
+    """Mirror of DamascusProver (src/protocol/prover.rs:56-313) on the GPU."""
+
+    def __init__(self, ctx: Context, data: bytes, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
+                 epoch_seed: bytes = DEFAULT_EPOCH_SEED, max_preprocess_bytes: int = DEFAULT_MEMORY_LIMIT_BYTES):
+        self._ctx = ctx
+        self._lib = ctx._lib
+        h = ctypes.c_void_p()
+        ctx.check(self._lib.damascus_prover_new(ctx.handle, data, len(data), seed_generators, epoch_seed,
+                                                max_preprocess_bytes, ctypes.byref(h)), "initialize")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.damascus_prover_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rounds_total(self) -> int:
+        return self._lib.damascus_prover_rounds_total(self._h)
+
+    def current_round(self) -> int:
+        return self._lib.damascus_prover_current_round(self._h)
+
+    def current_dimensions(self) -> Tuple[int, int]:
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._lib.damascus_prover_dimensions(self._h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def statement(self) -> bytes:
+        n = ctypes.c_size_t()
+        self._lib.damascus_prover_statement(self._h, None, 0, ctypes.byref(n))
+        buf = ctypes.create_string_buffer(n.value)
+        self._ctx.check(self._lib.damascus_prover_statement(self._h, buf, n.value, ctypes.byref(n)), "statement")
+        return buf.raw
+
+    def current_commitment(self) -> bytes:
+        n = ctypes.c_size_t()
+        self._lib.damascus_prover_current_commitment(self._h, None, 0, ctypes.byref(n))
+        buf = ctypes.create_string_buffer(n.value)
+        self._ctx.check(self._lib.damascus_prover_current_commitment(self._h, buf, n.value, ctypes.byref(n)),
+                        "current_commitment")
+        return buf.raw
+
+    def fold_round(self, rnd: int) -> bytes:
+        N, n = self.current_dimensions()
+        cap = record_size(N, max(n // 2, 1))
+        buf = ctypes.create_string_buffer(cap)
+        ln = ctypes.c_size_t()
+        self._ctx.check(self._lib.damascus_prover_fold_round(self._h, rnd, buf, cap, ctypes.byref(ln)),
+                        f"fold_round({rnd})")
+        return buf.raw[:ln.value]
+
+    def final_opening(self) -> Optional[bytes]:
+        out = ctypes.create_string_buffer(16)
+        if self._lib.damascus_prover_final_opening(self._h, out):
+            return None
+        return out.raw
+
+
+class DamascusVerifier:
+    """Mirror of DamascusVerifier (src/protocol/verifier.rs:11-134) on the GPU."""
+
+    def __init__(self, ctx: Context, statement: bytes, epoch_seed: bytes = DEFAULT_EPOCH_SEED):
+        self._ctx = ctx
+        self._lib = ctx._lib
+        h = ctypes.c_void_p()
+        ctx.check(self._lib.damascus_verifier_new(ctx.handle, statement, len(statement), epoch_seed,
+                                                  ctypes.byref(h)), "verifier new")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.damascus_verifier_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def update_commitment(self, record: bytes) -> int:
+        """0 when the round replays; a negative DAMASCUS_E* code when rejected."""
+        return self._lib.damascus_verifier_update_commitment(self._h, record, len(record))
+
+    def verify_final_opening(self, opening: bytes) -> int:
+        return self._lib.damascus_verifier_verify_final_opening(self._h, opening)
+
+    def round(self) -> int:
+        return self._lib.damascus_verifier_round(self._h)
+
+    def current_dimensions(self) -> Tuple[int, int]:
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._lib.damascus_verifier_dimensions(self._h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+
+# ------------------------------------------------------------------ reference FFI drop-ins
+def cuda_fold_batch(left: Sequence[int], right: Sequence[int], challenge: int) -> List[int]:
+    """damascus_cuda_fold_batch with the reference's split lo/hi layout (src/utils/gpu.rs:95-138)."""
+    n = len(left)
+    A = ctypes.c_uint64 * n
+    ll, lh = A(*[v & (2**64 - 1) for v in left]), A(*[v >> 64 for v in left])
+    rl, rh = A(*[v & (2**64 - 1) for v in right]), A(*[v >> 64 for v in right])
+    ol, oh = A(), A()
+    rc = load().damascus_cuda_fold_batch(ll, lh, rl, rh, ol, oh, n, challenge & (2**64 - 1), challenge >> 64)
+    if rc:
+        raise DamascusError(rc, "cuda_fold_batch")
+    return [ol[i] | (oh[i] << 64) for i in range(n)]
+
+
+def cuda_ntt_batch(a: Sequence[Sequence[int]], b: Sequence[Sequence[int]], n: int) -> List[List[int]]:
+    """damascus_cuda_ntt_batch (src/utils/gpu.rs:140-207): per-prime cyclic convolution of length n."""
+    A = ctypes.c_uint64 * (8 * n)
+    ha = A(*[v for row in a for v in row])
+    hb = A(*[v for row in b for v in row])
+    out = A()
+    primes = (ctypes.c_uint64 * 8)(*CRT_PRIMES)
+    log_n = n.bit_length() - 1
+    roots = (ctypes.c_uint64 * max(1, 8 * log_n))()
+    inv_sizes = (ctypes.c_uint64 * 8)()
+    rc = load().damascus_cuda_ntt_batch(ha, hb, out, n, primes, roots, roots, inv_sizes)
+    if rc:
+        raise DamascusError(rc, "cuda_ntt_batch")
+    return [[out[p * n + i] for i in range(n)] for p in range(8)]

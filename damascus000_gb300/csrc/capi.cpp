@@ -1,0 +1,568 @@
+// extern "C" entry points declared in include/damascus.h.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/damascus.h"
+#include "dm_tables.h"
+#include "engine.h"
+#include "host_blake3.h"
+
+using namespace dm;
+
+struct damascus_ctx {
+    Context* ctx;
+    std::string err_copy;
+};
+struct damascus_prover {
+    damascus_ctx* owner;
+    GpuProver* p;
+};
+struct damascus_verifier {
+    damascus_ctx* owner;
+    GpuVerifier* v;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// Reference default of RuntimeConfig.max_preprocess_bytes (src/utils/config.rs:21, 69-87).
+constexpr uint64_t kDefaultMaxPreprocess = 512ull * 1024 * 1024;
+
+int set_err(damascus_ctx* c, int code, const std::string& msg) {
+    if (c) c->ctx->set_error(msg);
+    return code;
+}
+
+// Scoped device buffer for the synchronous helpers (charged to the budget).
+struct Scratch {
+    DevMem m;
+    int alloc(Context* c, size_t b) { return m.alloc(c, b); }
+};
+
+fq fq_arg(const uint8_t* p) { return fq_from_u128_words(fq_from_bytes(p)); }
+
+bool pow2(uint64_t v) { return v && !(v & (v - 1)); }
+uint32_t log2u(uint64_t v) {
+    uint32_t l = 0;
+    while ((1ull << l) < v) ++l;
+    return l;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ context
+int damascus_ctx_create(int device, uint64_t hbm_budget_bytes, damascus_ctx** out) {
+    if (!out) return DAMASCUS_EINVAL;
+    Context* c = nullptr;
+    std::string err;
+    int rc = Context::create(device, hbm_budget_bytes, &c, &err);
+    if (rc != kOk) {
+        g_create_error = err;
+        *out = nullptr;
+        return rc;
+    }
+    *out = new damascus_ctx{c, {}};
+    return DAMASCUS_OK;
+}
+
+void damascus_ctx_destroy(damascus_ctx* ctx) {
+    if (!ctx) return;
+    delete ctx->ctx;
+    delete ctx;
+}
+
+const char* damascus_last_error(damascus_ctx* ctx) {
+    if (!ctx) return "null context";
+    ctx->err_copy = ctx->ctx->last_error();
+    return ctx->err_copy.c_str();
+}
+
+const char* damascus_create_error(void) { return g_create_error.c_str(); }
+uint64_t damascus_ctx_budget(damascus_ctx* ctx) { return ctx ? ctx->ctx->budget() : 0; }
+uint64_t damascus_ctx_reserved(damascus_ctx* ctx) { return ctx ? ctx->ctx->reserved() : 0; }
+
+// ------------------------------------------------------------------ field
+void damascus_fp_add(const uint8_t a[16], const uint8_t b[16], uint8_t out[16]) {
+    fq_to_bytes(fq_add(fq_arg(a), fq_arg(b)), out);
+}
+void damascus_fp_sub(const uint8_t a[16], const uint8_t b[16], uint8_t out[16]) {
+    fq_to_bytes(fq_sub(fq_arg(a), fq_arg(b)), out);
+}
+void damascus_fp_mul(const uint8_t a[16], const uint8_t b[16], uint8_t out[16]) {
+    fq_to_bytes(fq_mul(fq_arg(a), fq_arg(b)), out);
+}
+void damascus_fp_inv(const uint8_t a[16], uint8_t out[16]) { fq_to_bytes(fq_inv(fq_arg(a)), out); }
+void damascus_fp_from_le_bytes_mod_order(const uint8_t* bytes, size_t len, uint8_t out[16]) {
+    // Horner over 16-byte words from the most significant end: acc = acc * 2^128 + w.
+    fq acc = fq_zero();
+    fq two128;  // 2^128 mod q = 2^16 * 75
+    {
+        uint32_t r[8] = {0, 0, 0, 0, 1, 0, 0, 0};
+        two128 = fq_reduce8(r);
+    }
+    size_t nwords = (len + 15) / 16;
+    for (size_t w = nwords; w-- > 0;) {
+        uint8_t buf[16] = {0};
+        const size_t off = w * 16, n = len - off < 16 ? len - off : 16;
+        std::memcpy(buf, bytes + off, n);
+        acc = fq_add(fq_mul(acc, two128), fq_from_u128_words(fq_from_bytes(buf)));
+    }
+    fq_to_bytes(acc, out);
+}
+
+// ------------------------------------------------------------------ hashing
+void damascus_blake3(const uint8_t* data, size_t len, uint8_t out[32]) { blake3_hash(data, len, out); }
+void damascus_blake3_keyed(const uint8_t key[32], const uint8_t* data, size_t len, uint8_t out[32]) {
+    blake3_keyed_hash(key, data, len, out);
+}
+
+int damascus_transcript_challenge(const uint8_t epoch_seed[32], const uint8_t file_id[32], const char* label,
+                                  uint64_t round, const uint8_t* c, uint64_t n_c, const uint8_t* l, uint64_t n_l,
+                                  const uint8_t* r, uint64_t n_r, uint8_t out[16]) {
+    auto load = [](const uint8_t* p, uint64_t n) {
+        Module m = Module::zero((uint32_t)n);
+        for (size_t i = 0; i < m.c.size(); ++i) m.c[i] = fq_arg(p + 16 * i);
+        return m;
+    };
+    Transcript t(epoch_seed, file_id);
+    const Module mc = load(c, n_c), ml = load(l, n_l), mr = load(r, n_r);
+    fq v;
+    if (std::strcmp(label, "vec") == 0)
+        v = t.challenge_vec(round, mc, ml, mr);
+    else if (std::strcmp(label, "poly") == 0)
+        v = t.challenge_poly(round, mc, ml, mr);
+    else
+        return DAMASCUS_EINVAL;
+    fq_to_bytes(v, out);
+    return DAMASCUS_OK;
+}
+
+// ------------------------------------------------------------------ layout
+uint64_t damascus_coeff_count_for_byte_len(uint64_t byte_len) { return coeff_count_for_byte_len(byte_len); }
+int damascus_layout_for_byte_len(uint64_t byte_len, uint32_t* depth, uint64_t* dimension) {
+    return square_layout_for_byte_len(byte_len, depth, dimension) ? DAMASCUS_OK : DAMASCUS_EINVAL;
+}
+size_t damascus_proof_size(uint64_t file_len) {
+    uint32_t d;
+    uint64_t dim;
+    if (!square_layout_for_byte_len(file_len, &d, &dim)) return 0;
+    return proof_encoded_size(d);
+}
+size_t damascus_record_size(uint64_t nv, uint64_t np) { return record_encoded_size((uint32_t)nv, (uint32_t)np); }
+size_t damascus_statement_size(uint64_t n) { return statement_encoded_size((uint32_t)n); }
+uint64_t damascus_prover_footprint(uint64_t file_len) { return GpuProver::footprint(file_len); }
+
+// ------------------------------------------------------------------ commitment
+int damascus_file_id(damascus_ctx* ctx, const uint8_t* file, size_t len, uint8_t out[32]) {
+    if (!ctx || (!file && len)) return DAMASCUS_EINVAL;
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    Scratch f, sc, o;
+    if (f.alloc(C, len + 16) || sc.alloc(C, file_hash_scratch_words(len) * 4) || o.alloc(C, 32))
+        return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+    cudaStream_t s = C->stream();
+    cudaError_t e = len ? cudaMemcpyAsync(f.m.as<uint8_t>(), file, len, cudaMemcpyHostToDevice, s) : cudaSuccess;
+    if (e == cudaSuccess) e = launch_file_hash(f.m.as<uint8_t>(), len, sc.m.as<uint32_t>(), o.m.as<uint32_t>(), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, o.m.as<uint8_t>(), 32, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("file_id: ") + cudaGetErrorString(e));
+    return DAMASCUS_OK;
+}
+
+int damascus_derive_generators(damascus_ctx* ctx, const uint8_t g_seed[32], uint64_t N, uint64_t n, uint8_t* out) {
+    if (!ctx || !out || !pow2(n) || n > (1u << kLogMaxProverRing) || N == 0) return set_err(ctx, DAMASCUS_EINVAL, "bad generator shape");
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    const size_t bytes = N * kRank * n * 16;
+    Scratch gb;
+    if (gb.alloc(C, bytes)) return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+    cudaStream_t s = C->stream();
+    cudaError_t e = launch_gen_generators(g_seed, N, log2u(n), gb.m.as<uint4>(), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, gb.m.as<uint8_t>(), bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("derive_generators: ") + cudaGetErrorString(e));
+    return DAMASCUS_OK;
+}
+
+int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, const uint8_t* generators, uint64_t N,
+                                    uint64_t n, uint8_t* com_out) {
+    if (!ctx || !witness || !generators || !com_out || N == 0 || !pow2(n) || n > (1u << kLogMaxProverRing))
+        return set_err(ctx, DAMASCUS_EINVAL, "bad commitment shape");
+    // CRT headroom of the single NTT-domain sum: N * n * q^2 < P / 2.
+    if (N * n > (1ull << 22)) return set_err(ctx, DAMASCUS_EUNSUPPORTED, "N * n above 2^22 exceeds the CRT range");
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    const DeviceTables& T = C->tables();
+    const uint32_t L = log2u(n);
+    Scratch m, gg, mh, gh, part, out;
+    const uint32_t parts = 1;
+    if (m.alloc(C, N * n * 16) || gg.alloc(C, N * kRank * n * 16) || mh.alloc(C, N * n * 32) ||
+        gh.alloc(C, N * kRank * n * 32) || part.alloc(C, (size_t)parts * 64 * n * 4) || out.alloc(C, kRank * n * 16))
+        return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+    cudaStream_t s = C->stream();
+    MacJob job{0, 0, (uint32_t)N};
+    FinishJob fj{part.m.as<uint32_t>(), parts, L, kFinishPlain, out.m.as<uint4>()};
+    cudaError_t e = cudaMemcpyAsync(m.m.as<uint8_t>(), witness, N * n * 16, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(gg.m.as<uint8_t>(), generators, N * kRank * n * 16, cudaMemcpyHostToDevice, s);
+    // inputs may be any 128-bit words: reduce them mod q first
+    if (e == cudaSuccess) e = launch_canon(m.m.as<uint4>(), N * n, s);
+    if (e == cudaSuccess) e = launch_canon(gg.m.as<uint4>(), N * kRank * n, s);
+    if (e == cudaSuccess) e = launch_ntt_fwd(T, m.m.as<uint4>(), mh.m.as<uint32_t>(), N, L, s);
+    if (e == cudaSuccess) e = launch_ntt_fwd(T, gg.m.as<uint4>(), gh.m.as<uint32_t>(), N * kRank, L, s);
+    if (e == cudaSuccess) e = launch_mac(T, gh.m.as<uint32_t>(), mh.m.as<uint32_t>(), L, &job, 1, parts, part.m.as<uint32_t>(), s);
+    if (e == cudaSuccess) e = launch_finish(T, &fj, 1, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(com_out, out.m.as<uint8_t>(), kRank * n * 16, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("commit_with_generators: ") + cudaGetErrorString(e));
+    return DAMASCUS_OK;
+}
+
+int damascus_commit(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                    uint8_t* statement_out, size_t cap, size_t* statement_len) {
+    if (!ctx || (!file && len) || !seed_generators) return DAMASCUS_EINVAL;
+    static const uint8_t kZeroEpoch[32] = {0};
+    GpuProver p(ctx->ctx);
+    int rc = p.init(file, len, false, seed_generators, kZeroEpoch, std::numeric_limits<uint64_t>::max());
+    if (rc != kOk) return rc;
+    std::vector<uint8_t> buf;
+    encode_statement(buf, p.statement());
+    if (statement_len) *statement_len = buf.size();
+    if (!statement_out || cap < buf.size()) return set_err(ctx, DAMASCUS_ESIZE, "statement buffer too small");
+    std::memcpy(statement_out, buf.data(), buf.size());
+    return DAMASCUS_OK;
+}
+
+int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const void* d_b, void* d_out, uint64_t n,
+                                   uint64_t count, int sync);
+
+int damascus_ring_mul_batch(damascus_ctx* ctx, const uint8_t* a, const uint8_t* b, uint8_t* out, uint64_t n,
+                            uint64_t count) {
+    if (!ctx || !a || !b || !out || !pow2(n) || n > (1u << kLogMaxProverRing)) return set_err(ctx, DAMASCUS_EINVAL, "bad ring shape");
+    if (count == 0) return DAMASCUS_OK;
+    Context* C = ctx->ctx;
+    Scratch da, db, dout;
+    const size_t bytes = count * n * 16;
+    {
+        std::lock_guard<std::mutex> g(C->mutex());
+        cudaSetDevice(C->device());
+        if (da.alloc(C, bytes) || db.alloc(C, bytes) || dout.alloc(C, bytes))
+            return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+        cudaError_t e = cudaMemcpyAsync(da.m.as<uint8_t>(), a, bytes, cudaMemcpyHostToDevice, C->stream());
+        if (e == cudaSuccess) e = cudaMemcpyAsync(db.m.as<uint8_t>(), b, bytes, cudaMemcpyHostToDevice, C->stream());
+        if (e == cudaSuccess) e = launch_canon(da.m.as<uint4>(), count * n, C->stream());
+        if (e == cudaSuccess) e = launch_canon(db.m.as<uint4>(), count * n, C->stream());
+        if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("H2D: ") + cudaGetErrorString(e));
+    }
+    int rc = damascus_ring_mul_batch_device(ctx, da.m.as<void>(), db.m.as<void>(), dout.m.as<void>(), n, count, 0);
+    if (rc != DAMASCUS_OK) return rc;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaError_t e = cudaMemcpyAsync(out, dout.m.as<uint8_t>(), bytes, cudaMemcpyDeviceToHost, C->stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(C->stream());
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("D2H: ") + cudaGetErrorString(e));
+    return DAMASCUS_OK;
+}
+
+int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const void* d_b, void* d_out, uint64_t n,
+                                   uint64_t count, int sync) {
+    if (!ctx || !pow2(n) || n > (1u << kLogMaxProverRing)) return set_err(ctx, DAMASCUS_EINVAL, "bad ring shape");
+    if (count == 0) return DAMASCUS_OK;
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    const DeviceTables& T = C->tables();
+    const uint32_t L = log2u(n);
+    Scratch ra, rb;
+    if (ra.alloc(C, count * n * 32) || rb.alloc(C, count * n * 32))
+        return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+    cudaStream_t s = C->stream();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (C->profiling()) {
+        e0 = C->take_event();
+        cudaEventRecord(e0, s);
+    }
+    cudaError_t e = launch_ntt_fwd(T, static_cast<const uint4*>(d_a), ra.m.as<uint32_t>(), count, L, s);
+    if (e == cudaSuccess) e = launch_ntt_fwd(T, static_cast<const uint4*>(d_b), rb.m.as<uint32_t>(), count, L, s);
+    if (e0) {
+        e1 = C->take_event();
+        cudaEventRecord(e1, s);
+        C->record("ntt_fwd", e0, e1, (double)count * n * 96, (double)2 * count * 8 * (n / 2) * L);
+        e0 = C->take_event();
+        cudaEventRecord(e0, s);
+    }
+    if (e == cudaSuccess) e = launch_ring_mul(T, ra.m.as<uint32_t>(), rb.m.as<uint32_t>(), static_cast<uint4*>(d_out), count, L, s);
+    if (e0) {
+        e1 = C->take_event();
+        cudaEventRecord(e1, s);
+        C->record("ring_mul", e0, e1, (double)count * n * (64 + 16), (double)count * 8 * (n / 2) * L);
+    }
+    // Scratch is released when this returns: wait for the kernels that read it.
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    (void)sync;
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("ring_mul: ") + cudaGetErrorString(e));
+    return DAMASCUS_OK;
+}
+
+// ------------------------------------------------------------------ prover
+int damascus_prover_new(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                        const uint8_t epoch_seed[32], uint64_t max_preprocess_bytes, damascus_prover** out) {
+    if (!ctx || !out || (!file && len) || !seed_generators || !epoch_seed) return DAMASCUS_EINVAL;
+    GpuProver* p = new GpuProver(ctx->ctx);
+    int rc = p->init(file, len, false, seed_generators, epoch_seed,
+                     max_preprocess_bytes ? max_preprocess_bytes : kDefaultMaxPreprocess);
+    if (rc != kOk) {
+        delete p;
+        *out = nullptr;
+        return rc;
+    }
+    *out = new damascus_prover{ctx, p};
+    return DAMASCUS_OK;
+}
+
+void damascus_prover_free(damascus_prover* p) {
+    if (!p) return;
+    delete p->p;
+    delete p;
+}
+uint32_t damascus_prover_rounds_total(const damascus_prover* p) { return p ? p->p->rounds_total() : 0; }
+uint64_t damascus_prover_current_round(const damascus_prover* p) { return p ? p->p->current_round() : 0; }
+void damascus_prover_dimensions(const damascus_prover* p, uint64_t* N, uint64_t* n) {
+    if (N) *N = p ? p->p->vector_len() : 0;
+    if (n) *n = p ? p->p->ring_len() : 0;
+}
+
+int damascus_prover_statement(const damascus_prover* p, uint8_t* buf, size_t cap, size_t* len) {
+    if (!p) return DAMASCUS_EINVAL;
+    std::vector<uint8_t> v;
+    encode_statement(v, p->p->statement());
+    if (len) *len = v.size();
+    if (!buf || cap < v.size()) return DAMASCUS_ESIZE;
+    std::memcpy(buf, v.data(), v.size());
+    return DAMASCUS_OK;
+}
+
+int damascus_prover_current_commitment(const damascus_prover* p, uint8_t* buf, size_t cap, size_t* len) {
+    if (!p) return DAMASCUS_EINVAL;
+    const Module& m = p->p->current_commitment();
+    const size_t need = m.c.size() * 16;
+    if (len) *len = need;
+    if (!buf || cap < need) return DAMASCUS_ESIZE;
+    for (size_t i = 0; i < m.c.size(); ++i) fq_to_bytes(m.c[i], buf + 16 * i);
+    return DAMASCUS_OK;
+}
+
+int damascus_prover_fold_round(damascus_prover* p, uint64_t round, uint8_t* record_out, size_t cap,
+                               size_t* record_len) {
+    if (!p) return DAMASCUS_EINVAL;
+    RoundRecord rec;
+    int rc = p->p->fold_round(round, &rec);
+    if (rc != kOk) return rc;
+    std::vector<uint8_t> v;
+    encode_record(v, rec);
+    if (record_len) *record_len = v.size();
+    if (!record_out || cap < v.size()) return set_err(p->owner, DAMASCUS_ESIZE, "record buffer too small");
+    std::memcpy(record_out, v.data(), v.size());
+    return DAMASCUS_OK;
+}
+
+int damascus_prover_final_opening(const damascus_prover* p, uint8_t out[16]) {
+    if (!p || !out) return DAMASCUS_EINVAL;
+    fq o;
+    if (!p->p->final_opening(&o)) return DAMASCUS_ESTATE;
+    fq_to_bytes(o, out);
+    return DAMASCUS_OK;
+}
+
+static int prove_common(damascus_ctx* ctx, const uint8_t* file, size_t len, bool on_device, const uint8_t* seed,
+                        const uint8_t* epoch, uint8_t* proof_out, size_t cap, size_t* proof_len,
+                        double* device_ms = nullptr) {
+    if (!ctx || (!file && len) || !seed || !epoch) return DAMASCUS_EINVAL;
+    std::vector<uint8_t> proof;
+    int rc = prove_all(ctx->ctx, file, len, on_device, seed, epoch, &proof, device_ms);
+    if (rc != kOk) return rc;
+    if (proof_len) *proof_len = proof.size();
+    if (!proof_out || cap < proof.size()) return set_err(ctx, DAMASCUS_ESIZE, "proof buffer too small");
+    std::memcpy(proof_out, proof.data(), proof.size());
+    return DAMASCUS_OK;
+}
+
+int damascus_prove(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                   const uint8_t epoch_seed[32], uint8_t* proof_out, size_t cap, size_t* proof_len) {
+    return prove_common(ctx, file, len, false, seed_generators, epoch_seed, proof_out, cap, proof_len);
+}
+
+int damascus_prove_device(damascus_ctx* ctx, const void* d_file, size_t len, const uint8_t seed_generators[32],
+                          const uint8_t epoch_seed[32], uint8_t* proof_out, size_t cap, size_t* proof_len) {
+    return prove_common(ctx, static_cast<const uint8_t*>(d_file), len, true, seed_generators, epoch_seed, proof_out,
+                        cap, proof_len);
+}
+
+int damascus_prove_device_timed(damascus_ctx* ctx, const void* d_file, size_t len, const uint8_t seed_generators[32],
+                                const uint8_t epoch_seed[32], uint8_t* proof_out, size_t cap, size_t* proof_len,
+                                double* device_ms) {
+    return prove_common(ctx, static_cast<const uint8_t*>(d_file), len, true, seed_generators, epoch_seed, proof_out,
+                        cap, proof_len, device_ms);
+}
+
+int damascus_ctx_flush_l2(damascus_ctx* ctx) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    return ctx->ctx->flush_l2();
+}
+
+// ------------------------------------------------------------------ verifier
+int damascus_verifier_new(damascus_ctx* ctx, const uint8_t* statement, size_t len, const uint8_t epoch_seed[32],
+                          damascus_verifier** out) {
+    if (!ctx || !statement || !epoch_seed || !out) return DAMASCUS_EINVAL;
+    GpuVerifier* v = new GpuVerifier(ctx->ctx);
+    int rc = v->init(statement, len, epoch_seed);
+    if (rc != kOk) {
+        delete v;
+        *out = nullptr;
+        return rc;
+    }
+    *out = new damascus_verifier{ctx, v};
+    return DAMASCUS_OK;
+}
+
+void damascus_verifier_free(damascus_verifier* v) {
+    if (!v) return;
+    delete v->v;
+    delete v;
+}
+
+int damascus_verifier_update_commitment(damascus_verifier* v, const uint8_t* record, size_t len) {
+    if (!v || !record) return DAMASCUS_EINVAL;
+    const uint8_t* p = record;
+    RoundRecord rec;
+    if (!decode_record(p, record + len, rec)) return set_err(v->owner, DAMASCUS_EDESERIALIZE, "round record deserialization failed");
+    return v->v->update_commitment(rec);
+}
+
+int damascus_verifier_verify_final_opening(damascus_verifier* v, const uint8_t opening[16]) {
+    if (!v || !opening) return DAMASCUS_EINVAL;
+    return v->v->verify_final_opening(fq_from_bytes(opening));
+}
+
+uint64_t damascus_verifier_round(const damascus_verifier* v) { return v ? v->v->round() : 0; }
+void damascus_verifier_dimensions(const damascus_verifier* v, uint64_t* N, uint64_t* n) {
+    if (N) *N = v ? v->v->vector_len() : 0;
+    if (n) *n = v ? v->v->ring_len() : 0;
+}
+
+int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const uint8_t epoch_seed[32]) {
+    if (!ctx || !proof || !epoch_seed) return DAMASCUS_EINVAL;
+    return verify_proof(ctx->ctx, proof, len, epoch_seed);
+}
+
+// ------------------------------------------------------------------ reference FFI
+namespace {
+damascus_ctx* default_ctx() {
+    static damascus_ctx* c = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (damascus_ctx_create(0, 0, &c) != DAMASCUS_OK) c = nullptr;
+    });
+    return c;
+}
+}  // namespace
+
+int damascus_cuda_fold_batch(const uint64_t* left_lo, const uint64_t* left_hi, const uint64_t* right_lo,
+                             const uint64_t* right_hi, uint64_t* out_lo, uint64_t* out_hi, size_t len,
+                             uint64_t challenge_lo, uint64_t challenge_hi) {
+    if (!left_lo || !left_hi || !right_lo || !right_hi || !out_lo || !out_hi || len == 0) return 1;
+    damascus_ctx* ctx = default_ctx();
+    if (!ctx) return 2;
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    Scratch b;
+    const size_t w = len * 8;
+    if (b.alloc(C, 6 * w)) return 3;
+    uint64_t* base = b.m.as<uint64_t>();
+    uint64_t *ll = base, *lh = base + len, *rl = base + 2 * len, *rh = base + 3 * len, *ol = base + 4 * len,
+             *oh = base + 5 * len;
+    cudaStream_t s = C->stream();
+    const uint64_t cw[2] = {challenge_lo, challenge_hi};
+    uint32_t c8[8] = {(uint32_t)cw[0], (uint32_t)(cw[0] >> 32), (uint32_t)cw[1], (uint32_t)(cw[1] >> 32), 0, 0, 0, 0};
+    const fq c = fq_reduce8(c8);
+    if (cudaMemcpyAsync(ll, left_lo, w, cudaMemcpyHostToDevice, s) != cudaSuccess) return 4;
+    if (cudaMemcpyAsync(lh, left_hi, w, cudaMemcpyHostToDevice, s) != cudaSuccess) return 5;
+    if (cudaMemcpyAsync(rl, right_lo, w, cudaMemcpyHostToDevice, s) != cudaSuccess) return 6;
+    if (cudaMemcpyAsync(rh, right_hi, w, cudaMemcpyHostToDevice, s) != cudaSuccess) return 7;
+    if (launch_fold_split(ll, lh, rl, rh, ol, oh, len, c, s) != cudaSuccess) return 8;
+    if (cudaMemcpyAsync(out_lo, ol, w, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 9;
+    if (cudaMemcpyAsync(out_hi, oh, w, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 10;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return 11;
+    return 0;
+}
+
+int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint64_t* host_out, size_t n,
+                            const uint64_t* primes, const uint64_t* stage_roots, const uint64_t* inv_roots,
+                            const uint64_t* inv_sizes) {
+    if (!host_a || !host_b || !host_out || !primes || !stage_roots || !inv_roots || !inv_sizes || !pow2(n)) return 1;
+    if (n > (1u << kLogMaxProverRing)) return 12;
+    for (int i = 0; i < kPrimes; ++i)
+        if (primes[i] != host_tables().pc.p[i]) return 13;  // the kernels are specialised to the reference's primes
+    damascus_ctx* ctx = default_ctx();
+    if (!ctx) return 2;
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    Scratch b;
+    const size_t words = (size_t)kPrimes * n;
+    if (b.alloc(C, 3 * words * 4)) return 3;
+    std::vector<uint32_t> ha(words), hb(words), ho(words);
+    for (size_t i = 0; i < words; ++i) {
+        const uint64_t p = primes[i / n];
+        ha[i] = (uint32_t)(host_a[i] % p);
+        hb[i] = (uint32_t)(host_b[i] % p);
+    }
+    uint32_t* da = b.m.as<uint32_t>();
+    uint32_t *db = da + words, *dout = da + 2 * words;
+    cudaStream_t s = C->stream();
+    if (cudaMemcpyAsync(da, ha.data(), words * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 6;
+    if (cudaMemcpyAsync(db, hb.data(), words * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 7;
+    if (launch_cyclic_conv(C->tables(), da, db, dout, log2u(n), s) != cudaSuccess) return 8;
+    if (cudaMemcpyAsync(ho.data(), dout, words * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 15;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return 16;
+    for (size_t i = 0; i < words; ++i) host_out[i] = ho[i];
+    return 0;
+}
+
+// ------------------------------------------------------------------ measurement
+int damascus_ctx_set_profiling(damascus_ctx* ctx, int on) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    ctx->ctx->set_profiling(on != 0);
+    return DAMASCUS_OK;
+}
+void damascus_ctx_reset_stats(damascus_ctx* ctx) {
+    if (ctx) ctx->ctx->reset_stats();
+}
+int damascus_ctx_kernel_stat(damascus_ctx* ctx, const char* name, uint64_t* launches, double* total_ms,
+                             double* algo_bytes, double* algo_ops) {
+    if (!ctx || !name) return DAMASCUS_EINVAL;
+    KernelStat s;
+    if (!ctx->ctx->stat(name, &s)) return DAMASCUS_EINVAL;
+    if (launches) *launches = s.launches;
+    if (total_ms) *total_ms = s.total_ms;
+    if (algo_bytes) *algo_bytes = s.bytes;
+    if (algo_ops) *algo_ops = s.ops;
+    return DAMASCUS_OK;
+}
+int damascus_ctx_synchronize(damascus_ctx* ctx) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    cudaSetDevice(ctx->ctx->device());
+    return cudaDeviceSynchronize() == cudaSuccess ? DAMASCUS_OK : DAMASCUS_ECUDA;
+}
+
+}  // extern "C"

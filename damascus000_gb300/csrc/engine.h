@@ -1,0 +1,199 @@
+// Device runtime: context (device, stream, tables, HBM budget, kernel timing),
+// and the GPU prover / verifier that keep a proof's witness, generators and
+// fold state resident in HBM across rounds.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "dm_kernels.cuh"
+#include "protocol.h"
+
+namespace dm {
+
+enum Status : int {
+    kOk = 0,
+    kEInval = -1,
+    kENoMem = -2,       // HBM budget exhausted or allocation failed
+    kECuda = -3,
+    kETimeout = -4,
+    kEVerify = -5,      // verification rejected
+    kEInvariant = -6,   // prover recompute check failed
+    kEState = -7,       // call out of order (round mismatch, rounds finished)
+    kESize = -8,        // output buffer too small
+    kEDeserialize = -9,
+    kEUnsupported = -10,
+};
+
+struct KernelStat {
+    uint64_t launches = 0;  // kernel launches (a recorded call may launch more than one)
+    double total_ms = 0.0;
+    double bytes = 0.0;  // algorithmic bytes moved
+    double ops = 0.0;    // algorithmic integer operations
+};
+
+class Context {
+   public:
+    static int create(int device, uint64_t hbm_budget, Context** out, std::string* err);
+    ~Context();
+
+    int device() const { return device_; }
+    cudaStream_t stream() const { return stream_; }
+    const DeviceTables& tables() const { return tables_; }
+
+    // HBM budget accounting (bytes reserved by live provers/verifiers/requests).
+    bool reserve(uint64_t bytes);
+    void release(uint64_t bytes);
+    uint64_t budget() const { return budget_; }
+    uint64_t reserved() const { return reserved_.load(); }
+
+    void set_error(const std::string& e);
+    std::string last_error();
+
+    // Optional per-kernel event timing on the launching stream.
+    void set_profiling(bool on) { profiling_ = on; }
+    bool profiling() const { return profiling_; }
+    void record(const char* name, cudaEvent_t a, cudaEvent_t b, double bytes, double ops, int kernels = 1);
+    void flush_timings();  // resolves recorded event pairs (synchronises the stream)
+    bool stat(const char* name, KernelStat* out);
+    void reset_stats();
+    cudaEvent_t take_event();
+
+    std::mutex& mutex() { return mu_; }
+
+   private:
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    DeviceTables tables_{};
+    uint64_t budget_ = 0;
+    std::atomic<uint64_t> reserved_{0};
+    std::mutex mu_, err_mu_, prof_mu_;
+    std::string last_error_;
+    bool profiling_ = false;
+    struct Pending {
+        std::string name;
+        cudaEvent_t a, b;
+        double bytes, ops;
+        int kernels;
+    };
+    std::vector<Pending> pending_;
+    std::vector<cudaEvent_t> event_pool_;
+    std::map<std::string, KernelStat> stats_;
+    void* flush_buf_ = nullptr;
+
+   public:
+    // Writes a buffer larger than L2 (256 MiB) on the context stream and waits.
+    int flush_l2();
+    // Pinned host staging buffers, recycled across provers.
+    void* get_pinned(size_t bytes);
+    void put_pinned(void* p, size_t bytes);
+
+   private:
+    std::mutex pin_mu_;
+    std::vector<std::pair<size_t, void*>> pinned_free_;
+};
+
+// Scoped device allocation charged against the context budget.
+class DevMem {
+   public:
+    DevMem() = default;
+    ~DevMem() { reset(); }
+    DevMem(const DevMem&) = delete;
+    DevMem& operator=(const DevMem&) = delete;
+    // Stream-ordered allocation from the device pool on `stream` (the context
+    // stream when null); freed on the same stream.
+    int alloc(Context* ctx, size_t bytes, cudaStream_t stream = nullptr);
+    void reset();
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(ptr_);
+    }
+    size_t bytes() const { return bytes_; }
+
+   private:
+    Context* ctx_ = nullptr;
+    void* ptr_ = nullptr;
+    size_t bytes_ = 0;
+    cudaStream_t stream_ = nullptr;
+};
+
+// Round-by-round prover (src/protocol/prover.rs:56-313) on the GPU.
+class GpuProver {
+   public:
+    explicit GpuProver(Context* ctx) : ctx_(ctx) {}
+    ~GpuProver();
+    // file is a host pointer, or a device pointer when file_on_device.
+    int init(const uint8_t* file, uint64_t len, bool file_on_device, const uint8_t seed_generators[32],
+             const uint8_t epoch_seed[32], uint64_t max_preprocess_bytes);
+    int fold_round(uint64_t round_idx, RoundRecord* out);
+    bool final_opening(fq* out) const;
+    const Statement& statement() const { return st_; }
+    uint32_t rounds_total() const { return d_; }
+    uint64_t current_round() const { return round_; }
+    const Module& current_commitment() const { return current_; }
+    uint32_t vector_len() const { return N_; }
+    uint32_t ring_len() const { return n_; }
+    // bytes of device memory this prover holds for a file of len bytes
+    static uint64_t footprint(uint64_t len);
+    // device time from the first operation of init() to the last of the final round
+    double device_ms() const;
+
+   private:
+    int fail(int code, const std::string& msg);
+    int run_init_commit();
+    void release_all();
+    Context* ctx_;
+    cudaStream_t s_ = nullptr;
+    uint32_t d_ = 0, S_ = 0, N_ = 0, n_ = 0;
+    uint64_t round_ = 0;
+    Statement st_{};
+    Transcript tr_;
+    Module current_, pend_l_, pend_r_;
+    fq opening_{};
+    bool have_opening_ = false;
+    bool failed_ = false;
+    DevMem file_, hash_scratch_, file_id_, m_a_, m_b_, g_a_, g_b_, mhat_, ghat_, partials_, comm_, flags_;
+    uint8_t* pinned_ = nullptr;  // host staging for commitments
+    size_t pinned_bytes_ = 0;
+    cudaEvent_t ev_start_ = nullptr, ev_end_ = nullptr;
+};
+
+// Round-by-round verifier (src/protocol/verifier.rs:11-134): commitments and
+// challenges on the host, generator folds enqueued on the device without syncs.
+class GpuVerifier {
+   public:
+    explicit GpuVerifier(Context* ctx) : ctx_(ctx) {}
+    ~GpuVerifier();
+    int init(const uint8_t* statement, size_t len, const uint8_t epoch_seed[32]);
+    int update_commitment(const RoundRecord& rec);
+    int verify_final_opening(const fq& opening);
+    uint64_t round() const { return round_; }
+    uint32_t vector_len() const { return N_; }
+    uint32_t ring_len() const { return current_.n; }
+    static uint64_t footprint(uint64_t N, uint64_t n);
+
+   private:
+    int fail(int code, const std::string& msg);
+    Context* ctx_;
+    cudaStream_t s_ = nullptr;
+    Statement st_{};
+    Transcript tr_;
+    Module current_;
+    uint32_t N_ = 0, n_ = 0;  // generator family dimensions
+    uint64_t round_ = 0, rounds_ = 0;
+    DevMem g_[2];
+    int cur_ = 0;
+};
+
+// One-shot helpers used by the C ABI.
+int prove_all(Context* ctx, const uint8_t* file, uint64_t len, bool on_device, const uint8_t seed[32],
+              const uint8_t epoch[32], std::vector<uint8_t>* proof, double* device_ms = nullptr);
+int verify_proof(Context* ctx, const uint8_t* proof, size_t len, const uint8_t epoch[32]);
+
+}  // namespace dm

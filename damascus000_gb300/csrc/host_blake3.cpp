@@ -1,0 +1,128 @@
+#include "host_blake3.h"
+
+#include <cstring>
+
+#include "dm_blake3.cuh"
+
+namespace dm {
+
+namespace {
+const uint32_t kIV[8] = {DM_B3_IV0, DM_B3_IV1, DM_B3_IV2, DM_B3_IV3, DM_B3_IV4, DM_B3_IV5, DM_B3_IV6, DM_B3_IV7};
+
+void words16(const uint8_t* p, uint32_t m[16]) {
+    for (int i = 0; i < 16; ++i) m[i] = b3_load_le32(p + 4 * i);
+}
+}  // namespace
+
+Blake3Hasher::Blake3Hasher() : flags_(0) {
+    std::memcpy(key_, kIV, sizeof(key_));
+    std::memcpy(cv_, key_, sizeof(cv_));
+}
+
+Blake3Hasher::Blake3Hasher(const uint8_t key[32]) : flags_(kB3Keyed) {
+    for (int i = 0; i < 8; ++i) key_[i] = b3_load_le32(key + 4 * i);
+    std::memcpy(cv_, key_, sizeof(cv_));
+}
+
+void Blake3Hasher::compress_buffered_block() {
+    uint32_t m[16], out[16];
+    words16(buf_, m);
+    const uint32_t f = flags_ | (blocks_done_ == 0 ? kB3ChunkStart : 0u);
+    b3_compress(cv_, m, chunk_counter_, kB3BlockLen, f, out);
+    std::memcpy(cv_, out, 32);
+    ++blocks_done_;
+    buf_len_ = 0;
+}
+
+// Merges completed subtrees: one parent per trailing zero bit of total_chunks.
+void Blake3Hasher::push_chunk_cv(const uint32_t cv_in[8], uint64_t total_chunks) {
+    uint32_t cv[8];
+    std::memcpy(cv, cv_in, 32);
+    while ((total_chunks & 1) == 0) {
+        uint32_t m[16], out[16];
+        std::memcpy(m, stack_[depth_ - 1], 32);
+        std::memcpy(m + 8, cv, 32);
+        b3_compress(key_, m, 0, kB3BlockLen, flags_ | kB3Parent, out);
+        std::memcpy(cv, out, 32);
+        --depth_;
+        total_chunks >>= 1;
+    }
+    std::memcpy(stack_[depth_++], cv, 32);
+}
+
+void Blake3Hasher::update(const void* data, size_t len) {
+    const uint8_t* p = static_cast<const uint8_t*>(data);
+    while (len > 0) {
+        // A full chunk is closed only once more input arrives (its last block needs CHUNK_END).
+        if (blocks_done_ * kB3BlockLen + buf_len_ == kB3ChunkLen) {
+            uint32_t m[16], out[16];
+            words16(buf_, m);
+            b3_compress(cv_, m, chunk_counter_, kB3BlockLen, flags_ | kB3ChunkEnd | (blocks_done_ == 0 ? kB3ChunkStart : 0u),
+                        out);
+            push_chunk_cv(out, chunk_counter_ + 1);
+            ++chunk_counter_;
+            std::memcpy(cv_, key_, 32);
+            blocks_done_ = 0;
+            buf_len_ = 0;
+        }
+        if (buf_len_ == kB3BlockLen) compress_buffered_block();
+        // Fast path: whole blocks straight from the input while more follows.
+        size_t take = kB3BlockLen - buf_len_;
+        const size_t chunk_room = kB3ChunkLen - (blocks_done_ * kB3BlockLen + buf_len_);
+        if (take > chunk_room) take = chunk_room;
+        if (take > len) take = len;
+        std::memcpy(buf_ + buf_len_, p, take);
+        buf_len_ += (uint32_t)take;
+        p += take;
+        len -= take;
+    }
+}
+
+void Blake3Hasher::update_u64(uint64_t v) {
+    uint8_t t[8];
+    for (int i = 0; i < 8; ++i) t[i] = (uint8_t)(v >> (8 * i));
+    update(t, 8);
+}
+
+void Blake3Hasher::finalize(uint8_t out[32]) const {
+    // Pending output: the current chunk's last block.
+    uint32_t cv[8], m[16], outw[16];
+    std::memcpy(cv, cv_, 32);
+    uint8_t block[64];
+    std::memset(block, 0, sizeof(block));
+    std::memcpy(block, buf_, buf_len_);
+    words16(block, m);
+    uint64_t counter = chunk_counter_;
+    uint32_t blen = buf_len_;
+    uint32_t flags = flags_ | kB3ChunkEnd | (blocks_done_ == 0 ? kB3ChunkStart : 0u);
+    for (int d = depth_; d > 0; --d) {
+        b3_compress(cv, m, counter, blen, flags, outw);  // chaining value of the pending node
+        std::memcpy(m, stack_[d - 1], 32);
+        std::memcpy(m + 8, outw, 32);
+        std::memcpy(cv, key_, 32);
+        counter = 0;
+        blen = kB3BlockLen;
+        flags = flags_ | kB3Parent;
+    }
+    b3_compress(cv, m, 0, blen, flags | kB3Root, outw);
+    for (int i = 0; i < 8; ++i) {
+        out[4 * i] = (uint8_t)outw[i];
+        out[4 * i + 1] = (uint8_t)(outw[i] >> 8);
+        out[4 * i + 2] = (uint8_t)(outw[i] >> 16);
+        out[4 * i + 3] = (uint8_t)(outw[i] >> 24);
+    }
+}
+
+void blake3_hash(const void* data, size_t len, uint8_t out[32]) {
+    Blake3Hasher h;
+    h.update(data, len);
+    h.finalize(out);
+}
+
+void blake3_keyed_hash(const uint8_t key[32], const void* data, size_t len, uint8_t out[32]) {
+    Blake3Hasher h(key);
+    h.update(data, len);
+    h.finalize(out);
+}
+
+}  // namespace dm

@@ -1,0 +1,37 @@
+// Incremental BLAKE3 hasher on the host (the Fiat-Shamir transcript stays on
+// the host, src/protocol/transcript.rs:42-64).  Written from the BLAKE3
+// specification; shares the compression function with the device code.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+namespace dm {
+
+class Blake3Hasher {
+   public:
+    Blake3Hasher();
+    explicit Blake3Hasher(const uint8_t key[32]);
+    void update(const void* data, size_t len);
+    void update_u64(uint64_t v);
+    void finalize(uint8_t out[32]) const;
+
+   private:
+    void push_chunk_cv(const uint32_t cv[8], uint64_t total_chunks);
+    void compress_buffered_block();
+    uint32_t key_[8];
+    uint32_t flags_;
+    uint32_t stack_[56][8];
+    int depth_ = 0;
+    // current chunk
+    uint32_t cv_[8];
+    uint64_t chunk_counter_ = 0;
+    uint8_t buf_[64];
+    uint32_t buf_len_ = 0;
+    uint32_t blocks_done_ = 0;
+};
+
+void blake3_hash(const void* data, size_t len, uint8_t out[32]);
+void blake3_keyed_hash(const uint8_t key[32], const void* data, size_t len, uint8_t out[32]);
+
+}  // namespace dm

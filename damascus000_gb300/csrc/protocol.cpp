@@ -1,0 +1,200 @@
+#include "protocol.h"
+
+#include <cstring>
+
+#include "host_blake3.h"
+
+namespace dm {
+
+size_t module_encoded_size(uint32_t n) { return 8 + (size_t)kRank * (8 + 16 * (size_t)n); }
+size_t record_encoded_size(uint32_t nv, uint32_t np) { return 8 + 2 * module_encoded_size(nv) + 2 * module_encoded_size(np); }
+size_t statement_encoded_size(uint32_t n) { return 32 + 8 + 8 + module_encoded_size(n) + 32; }
+size_t proof_encoded_size(uint32_t d) {
+    size_t t = statement_encoded_size(1u << d) + 8 + 16;
+    for (uint32_t j = 0; j < d; ++j) t += record_encoded_size(1u << (d - j), 1u << (d - j - 1));
+    return t;
+}
+
+void put_u64(std::vector<uint8_t>& out, uint64_t v) {
+    for (int i = 0; i < 8; ++i) out.push_back((uint8_t)(v >> (8 * i)));
+}
+static uint64_t get_u64(const uint8_t* p) {
+    uint64_t v = 0;
+    for (int i = 7; i >= 0; --i) v = (v << 8) | p[i];
+    return v;
+}
+
+// module.rs:95-103: a slice of 8 Polys; Poly = Vec<Fp>; Fp = [u8; 16].
+void encode_module(std::vector<uint8_t>& out, const Module& m) {
+    put_u64(out, kRank);
+    const size_t base = out.size();
+    out.resize(base + (size_t)kRank * (8 + 16 * (size_t)m.n));
+    uint8_t* p = out.data() + base;
+    for (int k = 0; k < kRank; ++k) {
+        for (int i = 0; i < 8; ++i) p[i] = (uint8_t)((uint64_t)m.n >> (8 * i));
+        p += 8;
+        for (uint32_t j = 0; j < m.n; ++j, p += 16) fq_to_bytes(m.c[(size_t)k * m.n + j], p);
+    }
+}
+
+void encode_record(std::vector<uint8_t>& out, const RoundRecord& r) {
+    put_u64(out, r.round);
+    encode_module(out, r.l_vec);
+    encode_module(out, r.r_vec);
+    encode_module(out, r.l_poly);
+    encode_module(out, r.r_poly);
+}
+
+void encode_statement(std::vector<uint8_t>& out, const Statement& s) {
+    out.insert(out.end(), s.file_id, s.file_id + 32);
+    put_u64(out, s.original_len_bytes);
+    put_u64(out, s.d);
+    encode_module(out, s.com_0);
+    out.insert(out.end(), s.g_0_seed, s.g_0_seed + 32);
+}
+
+// Vec<Poly> of any length is read in full before the rank (== 8) and the
+// coordinate lengths (module.rs:106-115) are checked.
+bool decode_module(const uint8_t*& pp, const uint8_t* end, Module& m) {
+    const uint8_t* p = pp;
+    if (end - p < 8) return false;
+    const uint64_t count = get_u64(p);
+    p += 8;
+    uint64_t n0 = 0;
+    bool uniform = true;
+    std::vector<fq> c;
+    for (uint64_t k = 0; k < count; ++k) {
+        if (end - p < 8) return false;
+        const uint64_t n = get_u64(p);
+        p += 8;
+        if ((uint64_t)(end - p) / 16 < n) return false;
+        if (k == 0) {
+            n0 = n;
+            if (count == (uint64_t)kRank) c.resize((size_t)kRank * n);
+        }
+        if (n != n0) uniform = false;
+        if (count == (uint64_t)kRank && uniform)
+            for (uint64_t j = 0; j < n; ++j) c[k * n + j] = fq_from_u128_words(fq_from_bytes(p + 16 * j));
+        p += 16 * n;
+    }
+    if (count != (uint64_t)kRank || !uniform || n0 > 0xFFFFFFFFull) return false;
+    m.n = (uint32_t)n0;
+    m.c = std::move(c);
+    pp = p;
+    return true;
+}
+
+bool decode_record(const uint8_t*& p, const uint8_t* end, RoundRecord& r) {
+    if (end - p < 8) return false;
+    r.round = get_u64(p);
+    p += 8;
+    return decode_module(p, end, r.l_vec) && decode_module(p, end, r.r_vec) && decode_module(p, end, r.l_poly) &&
+           decode_module(p, end, r.r_poly);
+}
+
+bool decode_statement(const uint8_t*& p, const uint8_t* end, Statement& s) {
+    if (end - p < 48) return false;
+    std::memcpy(s.file_id, p, 32);
+    s.original_len_bytes = get_u64(p + 32);
+    s.d = get_u64(p + 40);
+    p += 48;
+    if (!decode_module(p, end, s.com_0)) return false;
+    if (end - p < 32) return false;
+    std::memcpy(s.g_0_seed, p, 32);
+    p += 32;
+    return true;
+}
+
+bool module_add_scaled(const Module& a, const Module& b, const fq& s, Module& out) {
+    if (a.n != b.n) return false;
+    Module r;
+    r.n = a.n;
+    r.c.resize(a.c.size());
+    for (size_t i = 0; i < a.c.size(); ++i) r.c[i] = fq_fma(a.c[i], s, b.c[i]);
+    out = std::move(r);
+    return true;
+}
+
+Module module_even(const Module& a) {
+    Module r = Module::zero(a.n / 2);
+    for (int k = 0; k < kRank; ++k)
+        for (uint32_t j = 0; j < a.n / 2; ++j) r.c[(size_t)k * r.n + j] = a.c[(size_t)k * a.n + 2 * j];
+    return r;
+}
+
+uint64_t coeff_count_for_byte_len(uint64_t len) {
+    const uint64_t c = len / kBytesPerCoeff + (len % kBytesPerCoeff ? 1 : 0);
+    return c ? c : 1;
+}
+
+bool square_layout_for_byte_len(uint64_t len, uint32_t* depth, uint64_t* dimension) {
+    const uint64_t coeffs = coeff_count_for_byte_len(len);
+    for (uint32_t d = kMinDepth; d < 32; ++d) {
+        const uint64_t dim = 1ull << d;
+        if (dim * dim >= coeffs) {
+            *depth = d;
+            *dimension = dim;
+            return true;
+        }
+    }
+    return false;
+}
+
+fq fq_from_hash(const uint8_t h[32]) {
+    uint32_t r[8];
+    for (int i = 0; i < 8; ++i)
+        r[i] = (uint32_t)h[4 * i] | ((uint32_t)h[4 * i + 1] << 8) | ((uint32_t)h[4 * i + 2] << 16) |
+               ((uint32_t)h[4 * i + 3] << 24);
+    return fq_reduce8(r);
+}
+
+Transcript::Transcript(const uint8_t epoch_seed[32], const uint8_t file_id[32]) {
+    std::memcpy(epoch_seed_, epoch_seed, 32);
+    std::memcpy(file_id_, file_id, 32);
+}
+
+fq Transcript::challenge_vec(uint64_t round, const Module& c, const Module& l, const Module& r) const {
+    return challenge("vec", round, c, l, r);
+}
+fq Transcript::challenge_poly(uint64_t round, const Module& c, const Module& l, const Module& r) const {
+    return challenge("poly", round, c, l, r);
+}
+
+// transcript.rs:82-90
+static void absorb_commitment(Blake3Hasher& h, const Module& m) {
+    h.update_u64(kRank);
+    std::vector<uint8_t> buf((size_t)m.n * 16);
+    for (int k = 0; k < kRank; ++k) {
+        h.update_u64(m.n);
+        for (uint32_t j = 0; j < m.n; ++j) fq_to_bytes(m.c[(size_t)k * m.n + j], buf.data() + 16 * j);
+        h.update(buf.data(), buf.size());
+    }
+}
+
+// transcript.rs:42-75: the absorbed prefix is shared by every counter value.
+fq Transcript::challenge(const char* label, uint64_t round, const Module& c, const Module& l, const Module& r) const {
+    Blake3Hasher h;
+    h.update(epoch_seed_, 32);
+    const size_t ll = std::strlen(label);
+    h.update_u64(ll);
+    h.update(label, ll);
+    h.update_u64(32);
+    h.update(file_id_, 32);
+    h.update_u64(0);  // epoch_index
+    h.update_u64(round);
+    absorb_commitment(h, c);
+    absorb_commitment(h, l);
+    absorb_commitment(h, r);
+    for (uint32_t counter = 0;; ++counter) {
+        Blake3Hasher t = h;
+        const uint8_t cb[4] = {(uint8_t)counter, (uint8_t)(counter >> 8), (uint8_t)(counter >> 16),
+                               (uint8_t)(counter >> 24)};
+        t.update(cb, 4);
+        uint8_t out[32];
+        t.finalize(out);
+        const fq v = fq_from_hash(out);
+        if (!fq_is_zero(v)) return v;
+    }
+}
+
+}  // namespace dm

@@ -1,0 +1,196 @@
+/*
+ * damascus.h -- C ABI of the GB300 (sm_103a) Damascus Fold prover/verifier.
+ *
+ * A drop-in for the reference crate damascus-core behind DAMASCUS_GPU=1: the
+ * Rust host code links libdamascus_gb300.so from build.rs and calls these
+ * functions through `extern "C"`.  Every entry point names the reference
+ * interface it replaces (paths relative to the reference project root).
+ *
+ * Conventions
+ *  - Field elements (Fp, q = 2^112 - 75) are 16-byte little-endian words, the
+ *    reference's serde form (src/algebra/field.rs:112-129).
+ *  - Serialized objects are bincode 1.x (fixint, little endian) byte-identical to
+ *    bincode::serialize of the reference types: Statement<8>
+ *    (src/commitment/sis.rs:24-30), RoundRecord (src/protocol/prover.rs:14-21).
+ *    A proof is bincode((Statement<8>, Vec<RoundRecord>, Fp)).
+ *  - Buffers are caller-owned host memory unless the name says _device.
+ *  - Return value: 0 on success, a negative DAMASCUS_E* code otherwise; the text
+ *    of the last error of a context is available from damascus_last_error().
+ *  - There is no CPU fallback: without a GB300 the context cannot be created.
+ *  - A context serialises its synchronous calls; provers and verifiers created
+ *    from one context may be driven from different threads (one thread each).
+ */
+#ifndef DAMASCUS_GB300_H
+#define DAMASCUS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DAMASCUS_OK 0
+#define DAMASCUS_EINVAL (-1)
+#define DAMASCUS_ENOMEM_BUDGET (-2)
+#define DAMASCUS_ECUDA (-3)
+#define DAMASCUS_ETIMEOUT (-4)
+#define DAMASCUS_EVERIFY (-5)
+#define DAMASCUS_EINVARIANT (-6)
+#define DAMASCUS_ESTATE (-7)
+#define DAMASCUS_ESIZE (-8)
+#define DAMASCUS_EDESERIALIZE (-9)
+#define DAMASCUS_EUNSUPPORTED (-10)
+
+typedef struct damascus_ctx damascus_ctx;
+typedef struct damascus_prover damascus_prover;
+typedef struct damascus_verifier damascus_verifier;
+
+/* ------------------------------------------------------------------ context */
+/* Replaces the device probe of src/utils/gpu.rs:19-67 (cuda_backend_ready).
+ * hbm_budget_bytes = 0 picks 90% of the free device memory. */
+int damascus_ctx_create(int device, uint64_t hbm_budget_bytes, damascus_ctx** out);
+void damascus_ctx_destroy(damascus_ctx* ctx);
+const char* damascus_last_error(damascus_ctx* ctx);
+/* Text of the last failure of damascus_ctx_create on this thread. */
+const char* damascus_create_error(void);
+uint64_t damascus_ctx_budget(damascus_ctx* ctx);
+uint64_t damascus_ctx_reserved(damascus_ctx* ctx);
+
+/* ------------------------------------------------------------------ field */
+/* src/algebra/field.rs:137-198, 45-63, 106-109 */
+void damascus_fp_add(const uint8_t a[16], const uint8_t b[16], uint8_t out[16]);
+void damascus_fp_sub(const uint8_t a[16], const uint8_t b[16], uint8_t out[16]);
+void damascus_fp_mul(const uint8_t a[16], const uint8_t b[16], uint8_t out[16]);
+void damascus_fp_inv(const uint8_t a[16], uint8_t out[16]);
+void damascus_fp_from_le_bytes_mod_order(const uint8_t* bytes, size_t len, uint8_t out[16]);
+
+/* ------------------------------------------------------------------ host hashing */
+/* blake3::hash / blake3::keyed_hash as used at src/utils/io.rs:33 and
+ * src/commitment/sis.rs:208-210 (host implementation). */
+void damascus_blake3(const uint8_t* data, size_t len, uint8_t out[32]);
+void damascus_blake3_keyed(const uint8_t key[32], const uint8_t* data, size_t len, uint8_t out[32]);
+/* Transcript::challenge_vec / challenge_poly (src/protocol/transcript.rs:22-80).
+ * label is "vec" or "poly"; c, l, r are 8 x n_* field elements each. */
+int damascus_transcript_challenge(const uint8_t epoch_seed[32], const uint8_t file_id[32], const char* label,
+                                  uint64_t round, const uint8_t* c, uint64_t n_c, const uint8_t* l, uint64_t n_l,
+                                  const uint8_t* r, uint64_t n_r, uint8_t out[16]);
+
+/* ------------------------------------------------------------------ layout */
+/* src/utils/io.rs:72-120: coefficient count, depth d and dimension 2^d. */
+uint64_t damascus_coeff_count_for_byte_len(uint64_t byte_len);
+int damascus_layout_for_byte_len(uint64_t byte_len, uint32_t* depth, uint64_t* dimension);
+/* Bytes of one serialized proof / record / statement (bincode sizes). */
+size_t damascus_proof_size(uint64_t file_len);
+size_t damascus_record_size(uint64_t ring_len_vec, uint64_t ring_len_poly);
+size_t damascus_statement_size(uint64_t ring_len);
+/* Device memory one prover holds for a file of file_len bytes. */
+uint64_t damascus_prover_footprint(uint64_t file_len);
+
+/* ------------------------------------------------------------------ commitment */
+/* blake3 file id on the GPU (src/utils/io.rs:33). */
+int damascus_file_id(damascus_ctx* ctx, const uint8_t* file, size_t len, uint8_t out[32]);
+/* derive_generator_families_from_seed (src/commitment/sis.rs:198-245): out is
+ * vector_len x 8 x ring_len field elements, [vec][coord][coeff]. */
+int damascus_derive_generators(damascus_ctx* ctx, const uint8_t g_seed[32], uint64_t vector_len, uint64_t ring_len,
+                               uint8_t* out);
+/* commit_with_generators_ntt (src/commitment/sis.rs:146-167): sum_i g_i * m_i in
+ * R_q^8.  witness [N][n], generators [N][8][n], out [8][n]. */
+int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, const uint8_t* generators,
+                                    uint64_t vector_len, uint64_t ring_len, uint8_t* com_out);
+/* ModuleSisCommitter::new + register_with_ntt (src/commitment/sis.rs:68-70, 179-195)
+ * via expand_file_to_square_polys (src/utils/io.rs:29-70): writes bincode(Statement). */
+int damascus_commit(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                    uint8_t* statement_out, size_t cap, size_t* statement_len);
+/* negacyclic_multiply (src/algebra/ntt.rs:112-195), batched: out_i = a_i * b_i in
+ * R_q with ring degree n (a power of two <= 4096); arrays are count x n elements. */
+int damascus_ring_mul_batch(damascus_ctx* ctx, const uint8_t* a, const uint8_t* b, uint8_t* out, uint64_t n,
+                            uint64_t count);
+/* Same on device-resident arrays (16-byte elements); asynchronous on the context
+ * stream unless sync != 0. */
+int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const void* d_b, void* d_out, uint64_t n,
+                                   uint64_t count, int sync);
+
+/* ------------------------------------------------------------------ prover */
+/* DamascusProver::initialize_with_config (src/protocol/prover.rs:61-111) with
+ * SystemParams.seed_generators / epoch_seed and RuntimeConfig.max_preprocess_bytes
+ * (0 = the reference default of 512 MiB). */
+int damascus_prover_new(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                        const uint8_t epoch_seed[32], uint64_t max_preprocess_bytes, damascus_prover** out);
+void damascus_prover_free(damascus_prover* p);
+uint32_t damascus_prover_rounds_total(const damascus_prover* p);
+uint64_t damascus_prover_current_round(const damascus_prover* p);
+/* current_dimensions (prover.rs:125-127) */
+void damascus_prover_dimensions(const damascus_prover* p, uint64_t* vector_len, uint64_t* ring_len);
+/* statement() serialized (prover.rs:129-131) */
+int damascus_prover_statement(const damascus_prover* p, uint8_t* buf, size_t cap, size_t* len);
+/* current_commitment() as 8 x n field elements (prover.rs:121-123) */
+int damascus_prover_current_commitment(const damascus_prover* p, uint8_t* buf, size_t cap, size_t* len);
+/* fold_round(round) (prover.rs:140-313): writes bincode(RoundRecord). */
+int damascus_prover_fold_round(damascus_prover* p, uint64_t round, uint8_t* record_out, size_t cap,
+                               size_t* record_len);
+/* final_opening (prover.rs:133-138); DAMASCUS_ESTATE before the last round. */
+int damascus_prover_final_opening(const damascus_prover* p, uint8_t out[16]);
+
+/* One-shot commit + d fold rounds + opening: writes
+ * bincode((Statement, Vec<RoundRecord>, Fp)); capacity from damascus_proof_size(). */
+int damascus_prove(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                   const uint8_t epoch_seed[32], uint8_t* proof_out, size_t cap, size_t* proof_len);
+/* Same with the file already in device memory. */
+int damascus_prove_device(damascus_ctx* ctx, const void* d_file, size_t len, const uint8_t seed_generators[32],
+                          const uint8_t epoch_seed[32], uint8_t* proof_out, size_t cap, size_t* proof_len);
+
+/* damascus_prove_device, also returning the device time (CUDA events on the
+ * prover's stream) from its first operation to its last. */
+int damascus_prove_device_timed(damascus_ctx* ctx, const void* d_file, size_t len, const uint8_t seed_generators[32],
+                                const uint8_t epoch_seed[32], uint8_t* proof_out, size_t cap, size_t* proof_len,
+                                double* device_ms);
+
+/* ------------------------------------------------------------------ verifier */
+/* DamascusVerifier::new (src/protocol/verifier.rs:22-43) from bincode(Statement). */
+int damascus_verifier_new(damascus_ctx* ctx, const uint8_t* statement, size_t len, const uint8_t epoch_seed[32],
+                          damascus_verifier** out);
+void damascus_verifier_free(damascus_verifier* v);
+/* update_commitment (verifier.rs:57-120) from bincode(RoundRecord); a record that
+ * does not deserialize returns DAMASCUS_EDESERIALIZE, a rejected one DAMASCUS_EVERIFY. */
+int damascus_verifier_update_commitment(damascus_verifier* v, const uint8_t* record, size_t len);
+/* verify_final_opening (verifier.rs:122-134): 0 accepts, DAMASCUS_EVERIFY rejects. */
+int damascus_verifier_verify_final_opening(damascus_verifier* v, const uint8_t opening[16]);
+uint64_t damascus_verifier_round(const damascus_verifier* v);
+void damascus_verifier_dimensions(const damascus_verifier* v, uint64_t* vector_len, uint64_t* ring_len);
+/* One-shot verification of a damascus_prove() proof: 0 accepts. */
+int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const uint8_t epoch_seed[32]);
+
+/* ------------------------------------------------------------------ reference FFI */
+/* Drop-in for the reference's own CUDA hooks, same signatures and argument
+ * meaning (src/utils/gpu.rs:69-93; cuda/fold_kernel.cu:209, cuda/ntt_kernel.cu:106).
+ * damascus_cuda_fold_batch: out = left + right * challenge (mod q) over len
+ * elements given as split lo/hi 64-bit halves.
+ * damascus_cuda_ntt_batch: for each of the 8 CRT primes, the length-n cyclic
+ * convolution of host_a and host_b (8 x n residues each) into host_out; the root
+ * tables are accepted for ABI compatibility and checked for shape only.
+ * Both return 0 on success and a positive step code on failure, as the
+ * reference's callers expect (gpu.rs:122-131, 191-193). */
+int damascus_cuda_fold_batch(const uint64_t* left_lo, const uint64_t* left_hi, const uint64_t* right_lo,
+                             const uint64_t* right_hi, uint64_t* out_lo, uint64_t* out_hi, size_t len,
+                             uint64_t challenge_lo, uint64_t challenge_hi);
+int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint64_t* host_out, size_t n,
+                            const uint64_t* primes, const uint64_t* stage_roots, const uint64_t* inv_roots,
+                            const uint64_t* inv_sizes);
+
+/* ------------------------------------------------------------------ measurement */
+/* Per-kernel CUDA-event timing on the launching stream (off by default). */
+int damascus_ctx_set_profiling(damascus_ctx* ctx, int on);
+void damascus_ctx_reset_stats(damascus_ctx* ctx);
+/* 0 and fills the totals if the kernel ran since the last reset. */
+int damascus_ctx_kernel_stat(damascus_ctx* ctx, const char* name, uint64_t* launches, double* total_ms,
+                             double* algo_bytes, double* algo_ops);
+/* Waits for all work queued on the device. */
+int damascus_ctx_synchronize(damascus_ctx* ctx);
+/* Writes 256 MiB (more than the 129 MB L2) on the context stream and waits. */
+int damascus_ctx_flush_l2(damascus_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
