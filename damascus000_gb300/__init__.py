@@ -54,7 +54,7 @@ EXPORTED_SYMBOLS = (
     "damascus_verifier_verify_final_opening", "damascus_verifier_round", "damascus_verifier_dimensions",
     "damascus_verify", "damascus_cuda_fold_batch", "damascus_cuda_ntt_batch",
     "damascus_ctx_set_profiling", "damascus_ctx_reset_stats", "damascus_ctx_kernel_stat",
-    "damascus_ctx_synchronize",
+    "damascus_ctx_synchronize", "damascus_file_id_noalloc",
 )
 
 
@@ -149,6 +149,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_ctx_kernel_stat", i32, vp, cp, P(u64), P(ctypes.c_double), P(ctypes.c_double),
         P(ctypes.c_double))
     sig("damascus_ctx_synchronize", i32, vp)
+    sig("damascus_file_id_noalloc", i32, vp, sz, vp, vp)
 
 
 # ------------------------------------------------------------------ encoding helpers

@@ -178,6 +178,22 @@ int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint
                             const uint64_t* primes, const uint64_t* stage_roots, const uint64_t* inv_roots,
                             const uint64_t* inv_sizes);
 
+/* BLAKE3 file id (the blake3::hash of src/utils/io.rs:33) of a file that is
+ * already in device memory, for callers that cannot allocate device memory --
+ * code running while a CUDA graph is being captured, serving loops confined to
+ * a pre-reserved budget, hosts whose allocator belongs to another framework.
+ * No counterpart in the reference, which hashes on the host.
+ * d_file: len bytes of device memory; d_out32: 32 bytes of device memory; the
+ * kernels run asynchronously on `stream` (a cudaStream_t, 0 for the default
+ * stream) on the current device.  The call makes no device allocation: its
+ * scratch is a 4 MiB static device array that every device loading this library
+ * holds until exit, so len is limited to 64 MiB (larger returns DAMASCUS_ESIZE).
+ * The first call on a device resolves that array's address (cudaGetSymbolAddress)
+ * and should come before any stream capture.  All calls share the array and
+ * nothing in it needs clearing between calls; calls that overlap on the GPU
+ * (other streams, or other threads) race on it and must be serialised. */
+int damascus_file_id_noalloc(const void* d_file, size_t len, void* d_out32, void* stream);
+
 /* ------------------------------------------------------------------ measurement */
 /* Per-kernel CUDA-event timing on the launching stream (off by default). */
 int damascus_ctx_set_profiling(damascus_ctx* ctx, int on);
