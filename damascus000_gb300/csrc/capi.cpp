@@ -10,6 +10,7 @@
 #include "../../include/damascus.h"
 #include "dm_tables.h"
 #include "engine.h"
+#include "proof.h"
 #include "host_blake3.h"
 
 using namespace dm;

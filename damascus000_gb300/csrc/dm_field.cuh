@@ -220,6 +220,7 @@ struct PrimeConsts {
     uint32_t k64[kPrimes];    // 2^64 * R mod p
     uint32_t k96[kPrimes];    // 2^96 * R mod p
     uint32_t qres[kPrimes];   // q mod p
+    uint32_t r1p[kPrimes], k32p[kPrimes], k64p[kPrimes], k96p[kPrimes];  // the above times p^-1 mod 2^32
 };
 
 // Residue of a Z_q element (four limbs) modulo prime i: sum_j x_j * 2^(32 j).

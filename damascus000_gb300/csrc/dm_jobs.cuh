@@ -1,0 +1,98 @@
+// Multi-job kernel interfaces.  Every kernel here takes a list of jobs, so one
+// launch serves one request (the plain path) or the same stage of many requests
+// (the batched and serving paths coalesce same-degree rounds into one launch).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dm_kernels.cuh"
+
+namespace dm {
+
+constexpr int kMaxJobs = 48;
+
+// ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][8][2^L] ----
+struct NttJob {
+    const uint4* src;
+    uint32_t* dst;
+    uint32_t npolys;
+    uint32_t cta0;  // filled by the launcher
+};
+
+// ---- multiply-accumulate over columns (all jobs of a launch share L) ----
+// plain: partials[part][k*8+p][slot] = sum_{i<count} G[g_base+i][k][p][slot] * M[m_base+i][p][slot]
+// split: chk over 2^L slots, lp / rp over 2^(L-1) (even/odd cross terms)
+struct MacJobX {
+    const uint32_t* G;
+    const uint32_t* M;
+    uint32_t* out0;  // plain: partials; split: chk partials
+    uint32_t* out1;  // split: lp partials
+    uint32_t* out2;  // split: rp partials
+    uint32_t g_base, m_base, count, parts;
+    uint32_t cta0;
+};
+
+// ---- sum partials, inverse NTT, CRT to Z_q, optional compare (all jobs share L) ----
+struct FinishJobX {
+    const uint32_t* partials;
+    uint4* out;            // [8][2^L]
+    const uint4* expect;   // compared with out when non-null
+    uint32_t* flag;        // set to 1 on mismatch
+    uint32_t parts;
+    uint32_t mode;         // FinishMode
+};
+
+// ---- folds and commitment algebra in the coefficient domain ----
+enum FoldMode : uint32_t {
+    kFoldVec = 0,       // dst[e] = a[e] + x * b[e]
+    kFoldPoly = 1,      // dst[poly][j] = a[poly][2j] + x * a[poly][2j+1]
+    kFoldPolyX = 2,     // dst[poly][j] = a[poly][2j] + x * (X * odd)[j]
+    kCombine = 3,       // dst[e] = a[e] + x * b[e] + y * c[e]
+    kCombineEven = 4,   // dst[k][j] = a[k][2j] + x * b[k][j] + y * c[k][j]
+    kCanon = 5,         // dst[e] = a[e] mod q
+};
+struct FoldJob {
+    uint4* dst;
+    const uint4* a;
+    const uint4* b;
+    const uint4* c;
+    fq x, y;
+    uint64_t n;     // output elements
+    uint32_t mode;
+    uint32_t Lout;  // log2 of the output polynomial length (poly modes, combine_even)
+    uint32_t cta0;
+};
+
+// ---- hashing / expansion ----
+struct GenJob {
+    uint32_t key[8];
+    uint4* dst;
+    uint64_t total;  // N * 8 * 2^log_n
+    uint32_t log_n;
+    uint32_t cta0;
+};
+struct UnpackJob {
+    const uint8_t* file;
+    uint64_t len;
+    uint4* dst;
+    uint64_t total;
+    uint32_t cta0;
+};
+struct HashJob {
+    const uint8_t* file;
+    uint64_t len;
+    uint32_t* scratch;  // 2 * 8 * nchunks words
+    uint32_t* out8;
+    uint32_t cta0;
+};
+
+cudaError_t upload_tables_ext(DeviceTables* t);  // zetap / zinvp
+cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st);
+cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st);
+cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);
+cudaError_t launch_fold_jobs(FoldJob* jobs, int n, cudaStream_t st);
+cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st);
+cudaError_t launch_unpack_jobs(UnpackJob* jobs, int n, cudaStream_t st);
+cudaError_t launch_hash_jobs(HashJob* jobs, int n, cudaStream_t st);  // 2 launches
+
+}  // namespace dm

@@ -19,6 +19,8 @@ struct DeviceTables {
     uint32_t ninv4_r2[kPrimes][kLogMaxRing + 1];
     const uint32_t* zeta;  // device [prime][kMaxRing]
     const uint32_t* zinv;
+    const uint32_t* zetap = nullptr;  // zeta * p^-1 mod 2^32
+    const uint32_t* zinvp = nullptr;
 };
 
 // Uploads the tables to the current device (called once per device).

@@ -82,6 +82,8 @@ HostTables build() {
     HostTables t;
     t.zeta.resize((size_t)kPrimes * kMaxRing);
     t.zinv.resize((size_t)kPrimes * kMaxRing);
+    t.zetap.resize((size_t)kPrimes * kMaxRing);
+    t.zinvp.resize((size_t)kPrimes * kMaxRing);
     for (int i = 0; i < kPrimes; ++i) {
         const uint32_t p = kCrtPrimes[i];
         t.pc.p[i] = p;
@@ -94,6 +96,10 @@ HostTables build() {
         t.pc.k32[i] = (uint32_t)((uint64_t)t.pc.r2[i]);                // 2^32 * R = R^2
         t.pc.k64[i] = (uint32_t)((uint64_t)t.pc.r2[i] * R % p);        // 2^64 * R = R^3
         t.pc.k96[i] = (uint32_t)((uint64_t)t.pc.k64[i] * R % p);       // 2^96 * R = R^4
+        t.pc.r1p[i] = t.pc.r1[i] * inv;
+        t.pc.k32p[i] = t.pc.k32[i] * inv;
+        t.pc.k64p[i] = t.pc.k64[i] * inv;
+        t.pc.k96p[i] = t.pc.k96[i] * inv;
         // q mod p
         unsigned __int128 q = (((unsigned __int128)1) << 112) - 75;
         t.pc.qres[i] = (uint32_t)(q % p);
@@ -106,6 +112,8 @@ HostTables build() {
             uint32_t e = bitrev(k, kLogMaxRing);
             t.zeta[(size_t)i * kMaxRing + k] = to_mont(pow_mod(psi, e, p), p);
             t.zinv[(size_t)i * kMaxRing + k] = to_mont(pow_mod(psi_inv, e, p), p);
+            t.zetap[(size_t)i * kMaxRing + k] = t.zeta[(size_t)i * kMaxRing + k] * t.pc.pinv[i];
+            t.zinvp[(size_t)i * kMaxRing + k] = t.zinv[(size_t)i * kMaxRing + k] * t.pc.pinv[i];
         }
         const uint32_t inv4 = inv_mod(4, p);
         for (int L = 0; L <= kLogMaxRing; ++L) {

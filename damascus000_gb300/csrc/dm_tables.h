@@ -17,6 +17,8 @@ struct HostTables {
     // zeta[i * kMaxRing + k] = psi_i^brv12(k) * R mod p_i, psi_i a primitive
     // 2*kMaxRing-th root of unity; zinv holds the inverses (also Montgomery form).
     std::vector<uint32_t> zeta, zinv;
+    // zetap[i] = zeta[i] * p^-1 mod 2^32 (likewise zinvp): three-multiply Montgomery twiddles
+    std::vector<uint32_t> zetap, zinvp;
     // ninv_r2[i][L] = (2^L)^-1 * R^2 mod p_i : final scale of an inverse NTT of size
     // 2^L applied to Montgomery products (one R^-1 factor pending).
     uint32_t ninv_r2[kPrimes][kLogMaxRing + 1];

@@ -97,6 +97,7 @@ class Context {
    private:
     std::mutex pin_mu_;
     std::vector<std::pair<size_t, void*>> pinned_free_;
+
 };
 
 // Scoped device allocation charged against the context budget.
@@ -121,47 +122,6 @@ class DevMem {
     void* ptr_ = nullptr;
     size_t bytes_ = 0;
     cudaStream_t stream_ = nullptr;
-};
-
-// Round-by-round prover (src/protocol/prover.rs:56-313) on the GPU.
-class GpuProver {
-   public:
-    explicit GpuProver(Context* ctx) : ctx_(ctx) {}
-    ~GpuProver();
-    // file is a host pointer, or a device pointer when file_on_device.
-    int init(const uint8_t* file, uint64_t len, bool file_on_device, const uint8_t seed_generators[32],
-             const uint8_t epoch_seed[32], uint64_t max_preprocess_bytes);
-    int fold_round(uint64_t round_idx, RoundRecord* out);
-    bool final_opening(fq* out) const;
-    const Statement& statement() const { return st_; }
-    uint32_t rounds_total() const { return d_; }
-    uint64_t current_round() const { return round_; }
-    const Module& current_commitment() const { return current_; }
-    uint32_t vector_len() const { return N_; }
-    uint32_t ring_len() const { return n_; }
-    // bytes of device memory this prover holds for a file of len bytes
-    static uint64_t footprint(uint64_t len);
-    // device time from the first operation of init() to the last of the final round
-    double device_ms() const;
-
-   private:
-    int fail(int code, const std::string& msg);
-    int run_init_commit();
-    void release_all();
-    Context* ctx_;
-    cudaStream_t s_ = nullptr;
-    uint32_t d_ = 0, S_ = 0, N_ = 0, n_ = 0;
-    uint64_t round_ = 0;
-    Statement st_{};
-    Transcript tr_;
-    Module current_, pend_l_, pend_r_;
-    fq opening_{};
-    bool have_opening_ = false;
-    bool failed_ = false;
-    DevMem file_, hash_scratch_, file_id_, m_a_, m_b_, g_a_, g_b_, mhat_, ghat_, partials_, comm_, flags_;
-    uint8_t* pinned_ = nullptr;  // host staging for commitments
-    size_t pinned_bytes_ = 0;
-    cudaEvent_t ev_start_ = nullptr, ev_end_ = nullptr;
 };
 
 // Round-by-round verifier (src/protocol/verifier.rs:11-134): commitments and
