@@ -55,6 +55,9 @@ EXPORTED_SYMBOLS = (
     "damascus_verify", "damascus_cuda_fold_batch", "damascus_cuda_ntt_batch",
     "damascus_ctx_set_profiling", "damascus_ctx_reset_stats", "damascus_ctx_kernel_stat",
     "damascus_ctx_synchronize", "damascus_file_id_noalloc",
+    "damascus_engine_create", "damascus_engine_destroy", "damascus_engine_submit", "damascus_engine_submit_device",
+    "damascus_engine_poll",
+    "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
 )
 
 
@@ -150,6 +153,15 @@ def _declare(L: ctypes.CDLL) -> None:
         P(ctypes.c_double))
     sig("damascus_ctx_synchronize", i32, vp)
     sig("damascus_file_id_noalloc", i32, vp, sz, vp, vp)
+    sig("damascus_engine_create", i32, vp, i32, i32, P(vp))
+    sig("damascus_engine_destroy", None, vp)
+    sig("damascus_engine_submit", i32, vp, cp, sz, cp, cp, P(u64))
+    sig("damascus_engine_submit_device", i32, vp, vp, sz, cp, cp, P(u64))
+    sig("damascus_engine_poll", i32, vp, u64, P(sz), P(ctypes.c_double))
+    sig("damascus_engine_wait", i32, vp, u64, P(sz), P(ctypes.c_double))
+    sig("damascus_engine_take", i32, vp, u64, vp, sz)
+    sig("damascus_engine_drain", i32, vp)
+    sig("damascus_engine_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64))
 
 
 # ------------------------------------------------------------------ encoding helpers
@@ -503,6 +515,92 @@ class DamascusVerifier:
         a, b = ctypes.c_uint64(), ctypes.c_uint64()
         self._lib.damascus_verifier_dimensions(self._h, ctypes.byref(a), ctypes.byref(b))
         return a.value, b.value
+
+
+class Engine:
+    """Continuous-batching prover: submit files, collect proofs (identical bytes to Context.prove)."""
+
+    def __init__(self, ctx: Context, host_threads: int = 0, max_waves: int = 0):
+        self._ctx = ctx
+        self._lib = ctx._lib
+        h = ctypes.c_void_p()
+        ctx.check(self._lib.damascus_engine_create(ctx.handle, host_threads, max_waves, ctypes.byref(h)),
+                  "engine create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.damascus_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, data: bytes, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
+               epoch_seed: bytes = DEFAULT_EPOCH_SEED) -> int:
+        t = ctypes.c_uint64()
+        self._ctx.check(self._lib.damascus_engine_submit(self._h, data, len(data), seed_generators, epoch_seed,
+                                                         ctypes.byref(t)), "engine submit")
+        return t.value
+
+    def submit_device(self, d_file: int, length: int, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
+                      epoch_seed: bytes = DEFAULT_EPOCH_SEED) -> int:
+        """Submit a file already in device memory (kept valid by the caller until done)."""
+        t = ctypes.c_uint64()
+        self._ctx.check(self._lib.damascus_engine_submit_device(self._h, ctypes.c_void_p(d_file), length,
+                                                                seed_generators, epoch_seed, ctypes.byref(t)),
+                        "engine submit_device")
+        return t.value
+
+    def submit_ptr(self, ptr: int, length: int, seed_generators: bytes, epoch_seed: bytes) -> int:
+        """Submit from a raw host address (e.g. pinned memory)."""
+        t = ctypes.c_uint64()
+        self._ctx.check(self._lib.damascus_engine_submit(self._h, ctypes.c_char_p(ptr), length, seed_generators,
+                                                         epoch_seed, ctypes.byref(t)), "engine submit")
+        return t.value
+
+    def _result(self, ticket: int, block: bool):
+        n = ctypes.c_size_t()
+        lat = ctypes.c_double()
+        fn = self._lib.damascus_engine_wait if block else self._lib.damascus_engine_poll
+        rc = fn(self._h, ticket, ctypes.byref(n), ctypes.byref(lat))
+        if rc == 0:
+            return None
+        if rc < 0:
+            raise DamascusError(rc, f"engine request {ticket}: {self._ctx.last_error()}")
+        buf = ctypes.create_string_buffer(n.value)
+        self._ctx.check(self._lib.damascus_engine_take(self._h, ticket, buf, n.value), "engine take")
+        return buf.raw, lat.value
+
+    def wait(self, ticket: int):
+        """(proof bytes, latency ms) once the request finished."""
+        return self._result(ticket, True)
+
+    def poll(self, ticket: int):
+        """(proof bytes, latency ms), or None while running."""
+        return self._result(ticket, False)
+
+    def drain(self) -> None:
+        self._ctx.check(self._lib.damascus_engine_drain(self._h), "engine drain")
+
+    def stats(self) -> dict:
+        v = [ctypes.c_uint64() for _ in range(5)]
+        self._ctx.check(self._lib.damascus_engine_stats(self._h, *[ctypes.byref(x) for x in v]), "engine stats")
+        return dict(zip(("completed", "failed", "waves", "launches", "peak_reserved"), (x.value for x in v)))
+
+    def prove_batch(self, items) -> list:
+        """items: iterable of (data, seed_generators, epoch_seed); returns the proofs in order."""
+        tickets = [self.submit(d, s, e) for d, s, e in items]
+        return [self.wait(t)[0] for t in tickets]
 
 
 # ------------------------------------------------------------------ reference FFI drop-ins

@@ -66,8 +66,8 @@ def build(force: bool = False, ptxas_verbose: bool = True, jobs: int | None = No
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda s: _compile(s, ptxas_verbose), srcs))
     tmp = BUILD_DIR / f"{LIB_NAME}.tmp{os.getpid()}"
-    cmd = [_nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", str(tmp)] + [str(o) for o in objs] + \
-        ["-lpthread"]
+    cmd = [_nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-Xlinker", "--export-dynamic", "-o", str(tmp)] + \
+        [str(o) for o in objs] + ["-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

@@ -1,8 +1,12 @@
 // extern "C" entry points declared in include/damascus.h.
 #include <cuda_runtime.h>
+#include <execinfo.h>
+#include <signal.h>
+#include <unistd.h>
 
 #include <cstring>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -11,6 +15,7 @@
 #include "dm_tables.h"
 #include "engine.h"
 #include "proof.h"
+#include "serve.h"
 #include "host_blake3.h"
 
 using namespace dm;
@@ -27,10 +32,40 @@ struct damascus_verifier {
     damascus_ctx* owner;
     GpuVerifier* v;
 };
+struct damascus_engine {
+    damascus_ctx* owner;
+    Engine* e;
+    std::mutex mu;
+    std::map<uint64_t, std::vector<uint8_t>> results;
+    std::map<uint64_t, std::pair<int, double>> status;
+};
 
 namespace {
 
 thread_local std::string g_create_error;
+
+// With DAMASCUS_CRASH_TRACE=1 in the environment, a fatal signal in any thread
+// of the process prints the native backtrace of that thread, then hands the
+// signal to the handler that was installed before (e.g. Python's faulthandler).
+using SigHandler = void (*)(int);
+SigHandler g_prev_handler[32];
+void crash_trace(int sig) {
+    void* frames[64];
+    const int n = backtrace(frames, 64);
+    const char msg[] = "damascus: fatal signal, native backtrace:\n";
+    (void)!write(2, msg, sizeof(msg) - 1);
+    backtrace_symbols_fd(frames, n, 2);
+    SigHandler prev = sig < 32 ? g_prev_handler[sig] : SIG_DFL;
+    signal(sig, prev == SIG_ERR || prev == nullptr ? SIG_DFL : prev);
+    raise(sig);
+}
+struct CrashTraceInstaller {
+    CrashTraceInstaller() {
+        const char* v = getenv("DAMASCUS_CRASH_TRACE");
+        if (v && v[0] == '1')
+            for (int sig : {SIGSEGV, SIGBUS, SIGABRT}) g_prev_handler[sig] = signal(sig, crash_trace);
+    }
+} g_crash_trace_installer;
 
 // Reference default of RuntimeConfig.max_preprocess_bytes (src/utils/config.rs:21, 69-87).
 constexpr uint64_t kDefaultMaxPreprocess = 512ull * 1024 * 1024;
@@ -120,7 +155,7 @@ void damascus_fp_from_le_bytes_mod_order(const uint8_t* bytes, size_t len, uint8
 }
 
 // ------------------------------------------------------------------ hashing
-void damascus_blake3(const uint8_t* data, size_t len, uint8_t out[32]) { blake3_hash(data, len, out); }
+void damascus_blake3(const uint8_t* data, size_t len, uint8_t out[32]) { blake3_hash_parallel(data, len, out); }
 void damascus_blake3_keyed(const uint8_t key[32], const uint8_t* data, size_t len, uint8_t out[32]) {
     blake3_keyed_hash(key, data, len, out);
 }
@@ -463,6 +498,96 @@ void damascus_verifier_dimensions(const damascus_verifier* v, uint64_t* N, uint6
 int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const uint8_t epoch_seed[32]) {
     if (!ctx || !proof || !epoch_seed) return DAMASCUS_EINVAL;
     return verify_proof(ctx->ctx, proof, len, epoch_seed);
+}
+
+// ------------------------------------------------------------------ engine
+int damascus_engine_create(damascus_ctx* ctx, int host_threads, int max_waves, damascus_engine** out) {
+    if (!ctx || !out) return DAMASCUS_EINVAL;
+    *out = new damascus_engine{ctx, new Engine(ctx->ctx, host_threads, max_waves > 0 ? max_waves : 3), {}, {}, {}};
+    return DAMASCUS_OK;
+}
+
+void damascus_engine_destroy(damascus_engine* e) {
+    if (!e) return;
+    delete e->e;
+    delete e;
+}
+
+int damascus_engine_submit(damascus_engine* e, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                           const uint8_t epoch_seed[32], uint64_t* ticket) {
+    if (!e) return DAMASCUS_EINVAL;
+    return e->e->submit(file, len, seed_generators, epoch_seed, ticket);
+}
+
+int damascus_engine_submit_device(damascus_engine* e, const void* d_file, size_t len,
+                                  const uint8_t seed_generators[32], const uint8_t epoch_seed[32], uint64_t* ticket) {
+    if (!e) return DAMASCUS_EINVAL;
+    return e->e->submit(static_cast<const uint8_t*>(d_file), len, seed_generators, epoch_seed, ticket, true);
+}
+
+static int engine_result(damascus_engine* e, uint64_t ticket, bool block, size_t* proof_len, double* latency_ms) {
+    {
+        std::lock_guard<std::mutex> g(e->mu);
+        auto st = e->status.find(ticket);
+        if (st != e->status.end()) {
+            if (proof_len) *proof_len = e->results[ticket].size();
+            if (latency_ms) *latency_ms = st->second.second;
+            return st->second.first;
+        }
+    }
+    std::vector<uint8_t> proof;
+    double lat = 0;
+    std::string err;
+    const int rc = block ? e->e->wait(ticket, &proof, &lat, &err) : e->e->poll(ticket, &proof, &lat, &err);
+    if (rc == 0) return 0;
+    if (rc < 0 && rc == DAMASCUS_EINVAL && err.empty()) return rc;  // unknown ticket
+    std::lock_guard<std::mutex> g(e->mu);
+    if (rc < 0) e->owner->ctx->set_error(err);
+    e->status[ticket] = {rc, lat};
+    if (proof_len) *proof_len = proof.size();
+    if (latency_ms) *latency_ms = lat;
+    e->results[ticket] = std::move(proof);
+    return rc;
+}
+
+int damascus_engine_poll(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms) {
+    if (!e) return DAMASCUS_EINVAL;
+    return engine_result(e, ticket, false, proof_len, latency_ms);
+}
+
+int damascus_engine_wait(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms) {
+    if (!e) return DAMASCUS_EINVAL;
+    return engine_result(e, ticket, true, proof_len, latency_ms);
+}
+
+int damascus_engine_take(damascus_engine* e, uint64_t ticket, uint8_t* proof_out, size_t cap) {
+    if (!e) return DAMASCUS_EINVAL;
+    std::lock_guard<std::mutex> g(e->mu);
+    auto it = e->results.find(ticket);
+    if (it == e->results.end()) return DAMASCUS_ESTATE;
+    if (!proof_out || cap < it->second.size()) return DAMASCUS_ESIZE;
+    std::memcpy(proof_out, it->second.data(), it->second.size());
+    e->results.erase(it);
+    e->status.erase(ticket);
+    return DAMASCUS_OK;
+}
+
+int damascus_engine_drain(damascus_engine* e) {
+    if (!e) return DAMASCUS_EINVAL;
+    e->e->drain();
+    return DAMASCUS_OK;
+}
+
+int damascus_engine_stats(damascus_engine* e, uint64_t* completed, uint64_t* failed, uint64_t* waves,
+                          uint64_t* launches, uint64_t* peak_reserved_bytes) {
+    if (!e) return DAMASCUS_EINVAL;
+    const EngineStats s = e->e->stats();
+    if (completed) *completed = s.completed;
+    if (failed) *failed = s.failed;
+    if (waves) *waves = s.waves;
+    if (launches) *launches = s.launches;
+    if (peak_reserved_bytes) *peak_reserved_bytes = s.peak_reserved;
+    return DAMASCUS_OK;
 }
 
 // ------------------------------------------------------------------ reference FFI

@@ -237,10 +237,76 @@ DM_HD uint32_t residue(const fq& x, const PrimeConsts& c, int i) {
 // src/algebra/ntt.rs:400-427 does with BigUint).
 struct CrtConsts {
     uint32_t inv[kPrimes][kPrimes];  // inv[j][i] = p_j^-1 * R mod p_i   (j < i)
+    uint32_t invp[kPrimes][kPrimes]; // inv[j][i] * p_i^-1 mod 2^32
     uint32_t half_digits[kPrimes];   // mixed-radix digits of (P - 1) / 2
     fq radix_mod_q[kPrimes];         // prod_{j<i} p_j mod q
     fq p_mod_q;                      // P mod q
 };
+
+// Same result as crt_to_fq with three-multiply Montgomery steps and one
+// multi-limb accumulation of sum v_i * (prod_{j<i} p_j mod q) (< 2^147) before a
+// single reduction mod q.
+DM_HD fq crt_to_fq_fast(const uint32_t r[kPrimes], const PrimeConsts& pc, const CrtConsts& cc) {
+    uint32_t v[kPrimes];
+    DM_UNROLL
+    for (int i = 0; i < kPrimes; ++i) {
+        const uint32_t p = pc.p[i];
+        uint32_t t = r[i];
+        DM_UNROLL
+        for (int j = 0; j < i; ++j) {
+            // v_j mod p_i as v_j * R * R^-1
+            uint32_t th, mh;
+#if defined(__CUDA_ARCH__)
+            th = __umulhi(v[j], pc.r1[i]);
+            mh = __umulhi(v[j] * pc.r1p[i], p);
+#else
+            th = (uint32_t)(((uint64_t)v[j] * pc.r1[i]) >> 32);
+            mh = (uint32_t)(((uint64_t)(uint32_t)(v[j] * pc.r1p[i]) * p) >> 32);
+#endif
+            const uint32_t vj = th < mh ? th - mh + p : th - mh;
+            const uint32_t d = sub_mod(t, vj, p);
+#if defined(__CUDA_ARCH__)
+            th = __umulhi(d, cc.inv[j][i]);
+            mh = __umulhi(d * cc.invp[j][i], p);
+#else
+            th = (uint32_t)(((uint64_t)d * cc.inv[j][i]) >> 32);
+            mh = (uint32_t)(((uint64_t)(uint32_t)(d * cc.invp[j][i]) * p) >> 32);
+#endif
+            t = th < mh ? th - mh + p : th - mh;
+        }
+        v[i] = t;
+    }
+    int gt = 0, decided = 0;
+    DM_UNROLL
+    for (int i = kPrimes - 1; i >= 0; --i) {
+        if (!decided && v[i] != cc.half_digits[i]) {
+            gt = v[i] > cc.half_digits[i];
+            decided = 1;
+        }
+    }
+    uint64_t acc[6] = {0, 0, 0, 0, 0, 0};
+    DM_UNROLL
+    for (int i = 0; i < kPrimes; ++i)
+        DM_UNROLL
+        for (int w = 0; w < 4; ++w) {
+            const uint64_t prod = (uint64_t)v[i] * cc.radix_mod_q[i].w[w];
+            acc[w] += (uint32_t)prod;
+            acc[w + 1] += prod >> 32;
+        }
+    uint32_t x8[8];
+    uint64_t carry = 0;
+    DM_UNROLL
+    for (int w = 0; w < 6; ++w) {
+        carry += acc[w];
+        x8[w] = (uint32_t)carry;
+        carry >>= 32;
+    }
+    x8[6] = (uint32_t)carry;
+    x8[7] = 0;
+    fq x = fq_reduce8(x8);
+    if (gt) x = fq_sub(x, cc.p_mod_q);
+    return x;
+}
 
 // r[i] < p_i -> the integer X with |X| < P/2 congruent to r, reduced mod q.
 DM_HD fq crt_to_fq(const uint32_t r[kPrimes], const PrimeConsts& pc, const CrtConsts& cc) {

@@ -89,6 +89,8 @@ struct HashJob {
 cudaError_t upload_tables_ext(DeviceTables* t);  // zetap / zinvp
 cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st);
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st);
+// Triple MAC (count = h column pairs): out0 = full sum, out1 = L, out2 = R.
+cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st);
 cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);
 cudaError_t launch_fold_jobs(FoldJob* jobs, int n, cudaStream_t st);
 cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st);

@@ -126,6 +126,8 @@ HostTables build() {
     for (int j = 0; j < kPrimes; ++j)
         for (int i = 0; i < kPrimes; ++i)
             t.cc.inv[j][i] = (j < i) ? to_mont(inv_mod(kCrtPrimes[j] % kCrtPrimes[i], kCrtPrimes[i]), kCrtPrimes[i]) : 0;
+    for (int j = 0; j < kPrimes; ++j)
+        for (int i = 0; i < kPrimes; ++i) t.cc.invp[j][i] = t.cc.inv[j][i] * t.pc.pinv[i];
     U256 prod;
     prod.w[0] = 1;
     for (int i = 0; i < kPrimes; ++i) {

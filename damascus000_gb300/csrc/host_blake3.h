@@ -32,6 +32,12 @@ class Blake3Hasher {
 };
 
 void blake3_hash(const void* data, size_t len, uint8_t out[32]);
+// Same digest; chunk chaining values are computed on the host worker pool for
+// inputs of 64 KiB and more, then merged pairwise (left-complete tree).
+void blake3_hash_parallel(const void* data, size_t len, uint8_t out[32]);
+
+// Fixed pool of host threads: fn(begin, end) over a split of [0, n).
+void host_parallel_for(size_t n, size_t min_per_task, void (*fn)(void*, size_t, size_t), void* arg);
 void blake3_keyed_hash(const uint8_t key[32], const void* data, size_t len, uint8_t out[32]);
 
 }  // namespace dm

@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(NttShape<L>::THREADS)
     if (active) {
         const uint4* src = jb.src + (poly << L);
 #pragma unroll
-        for (int r = 0; r < kNttE; ++r) a[r] = residue_fast(ldq(src, ntt_place(L, 0, t, r)), pc, pi);
+        for (int r = 0; r < kNttE; ++r) a[r] = residue_lazy(ldq(src, ntt_place(L, 0, t, r)), pc, pi);
     } else {
 #pragma unroll
         for (int r = 0; r < kNttE; ++r) a[r] = 0;
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(NttShape<L>::THREADS)
     uint32_t* srow = sm + row * (1u << L);
 #pragma unroll
     for (int pass = 0; pass < S::PASSES; ++pass) {
-        ntt_fwd_pass(a, L, pass, t, zt, ztp, p);
+        ntt_fwd_pass_lazy(a, L, pass, t, zt, ztp, p);
         if (pass + 1 < S::PASSES) {
 #pragma unroll
             for (int r = 0; r < kNttE; ++r) srow[ntt_swz(ntt_place(L, pass, t, r))] = a[r];
@@ -84,6 +84,8 @@ __global__ void __launch_bounds__(NttShape<L>::THREADS)
         }
     }
     if (active) {
+#pragma unroll
+        for (int r = 0; r < kNttE; ++r) a[r] = normalize_lazy(a[r], pc, pi);
         uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * kNttE);
         dst[0] = make_uint4(a[0], a[1], a[2], a[3]);
         dst[1] = make_uint4(a[4], a[5], a[6], a[7]);
@@ -164,6 +166,46 @@ __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> 
     }
     for (; i < i1; ++i) acc0 += mont_mul(__ldg(g + i * gstride), __ldg(m + i * mstride), p, pv);
     jb.out0[(((uint64_t)part * 64 + kp) << L) + slot] = reduce_u64(acc0 + acc1, p, pv, pc.r1[pi], pc.r2[pi]);
+}
+
+// Triple MAC over h = count column pairs (i, i + h): one read of every generator
+// column gives the full sum (out0), L = sum G[i+h] M[i] (out1) and
+// R = sum G[i] M[i+h] (out2).
+__global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+    const MacJobX jb = J.j[find_job(J)];
+    const uint32_t s = 1u << L;
+    const uint32_t nblk = slot_block_count(s);
+    uint32_t c = blockIdx.x - jb.cta0;
+    const uint32_t blk = c % nblk;
+    c /= nblk;
+    const uint32_t kp = c % 64;
+    const uint32_t part = c / 64;
+    const uint32_t slot = blk * kMacThreads + threadIdx.x;
+    if (slot >= s) return;
+    const uint32_t k = kp >> 3, pi = kp & 7u;
+    const uint32_t h = jb.count;
+    const uint32_t i0 = (uint32_t)((uint64_t)h * part / jb.parts);
+    const uint32_t i1 = (uint32_t)((uint64_t)h * (part + 1) / jb.parts);
+    const uint32_t p = pc.p[pi], pv = pc.pinv[pi];
+    const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
+    const uint64_t mstride = (uint64_t)kPrimes << L;
+    const uint32_t* g = jb.G + ((((uint64_t)k) * kPrimes + pi) << L) + slot;
+    const uint32_t* m = jb.M + (((uint64_t)pi) << L) + slot;
+    const uint64_t gh = (uint64_t)h * gstride, mh = (uint64_t)h * mstride;
+    uint64_t ac = 0, al = 0, ar = 0;
+    for (uint32_t i = i0; i < i1; ++i) {
+        const uint32_t gl = __ldg(g + i * gstride), gr = __ldg(g + i * gstride + gh);
+        const uint32_t ml = __ldg(m + i * mstride), mr = __ldg(m + i * mstride + mh);
+        ac += mont_mul(gl, ml, p, pv);
+        ac += mont_mul(gr, mr, p, pv);
+        al += mont_mul(gr, ml, p, pv);
+        ar += mont_mul(gl, mr, p, pv);
+    }
+    const uint32_t r1 = pc.r1[pi], r2 = pc.r2[pi];
+    const uint64_t o = (((uint64_t)part * 64 + kp) << L) + slot;
+    jb.out0[o] = reduce_u64(ac, p, pv, r1, r2);
+    jb.out1[o] = reduce_u64(al, p, pv, r1, r2);
+    jb.out2[o] = reduce_u64(ar, p, pv, r1, r2);
 }
 
 // Split MAC: thread per slot pair of ring 2^L (L >= 1).
@@ -285,7 +327,7 @@ __global__ void __launch_bounds__(FinShape<L>::THREADS)
         uint32_t rr[kPrimes];
 #pragma unroll
         for (int q = 0; q < kPrimes; ++q) rr[q] = sm[q * s + c];
-        const fq v = crt_to_fq(rr, pc, cc);
+        const fq v = crt_to_fq_fast(rr, pc, cc);
         const uint64_t o = ((uint64_t)k << L) + c;
         stq(jb.out, o, v);
         if (jb.expect) {
@@ -339,7 +381,7 @@ __global__ void finish_small_kernel(JobList<FinishJobX> J, PrimeConsts pc, CrtCo
         uint32_t rr[kPrimes];
 #pragma unroll
         for (int q = 0; q < kPrimes; ++q) rr[q] = sm[kk][q][c];
-        const fq v = crt_to_fq(rr, pc, cc);
+        const fq v = crt_to_fq_fast(rr, pc, cc);
         const uint64_t o = ((uint64_t)kk << L) + c;
         stq(jb.out, o, v);
         if (jb.expect) {
@@ -614,6 +656,23 @@ cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t
         case 12: return ntt_launch_L<12>(T, JL, jobs, n, st);
     }
     return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxJobs) return cudaErrorInvalidValue;
+    JobList<MacJobX> JL;
+    const uint32_t slots = 1u << L;
+    uint64_t total = 0;
+    JL.n = n;
+    for (int i = 0; i < n; ++i) {
+        jobs[i].cta0 = (uint32_t)total;
+        JL.j[i] = jobs[i];
+        total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * 64 * jobs[i].parts;
+    }
+    const unsigned bx = slots < (uint32_t)kMacThreads ? slots : kMacThreads;
+    mac_triple_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st) {

@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kNttThreads) finish_kernel(FinishJobs jobs, Pr
             const uint32_t f = (J.mode == kFinishPlain) ? sc.ninv_r2[pi][L] : sc.ninv4_r2[pi][L];
             r[pi] = mont_mul(sm[(pi << L) + c], f, pc.p[pi], pc.pinv[pi]);
         }
-        const fq v = crt_to_fq(r, pc, cc);
+        const fq v = crt_to_fq_fast(r, pc, cc);
         J.out[((uint64_t)k << L) + c] = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
     }
 }
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kNttThreads) ring_mul_kernel(const uint32_t* _
         uint32_t r[kPrimes];
 #pragma unroll
         for (int pi = 0; pi < kPrimes; ++pi) r[pi] = mont_mul(sm[(pi << L) + c], sc.ninv_r2[pi][L], pc.p[pi], pc.pinv[pi]);
-        const fq v = crt_to_fq(r, pc, cc);
+        const fq v = crt_to_fq_fast(r, pc, cc);
         out[(pair << L) + c] = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
     }
 }

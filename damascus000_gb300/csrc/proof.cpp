@@ -53,6 +53,7 @@ void Plan::clear() {
         ntt[L].clear();
         mac[L].clear();
         split[L].clear();
+        triple[L].clear();
         finish[L].clear();
     }
     d2h.clear();
@@ -61,7 +62,8 @@ void Plan::clear() {
 bool Plan::empty() const {
     if (!hash.empty() || !unpack.empty() || !gen.empty() || !fold.empty()) return false;
     for (int L = 0; L <= kLogMaxProverRing; ++L)
-        if (!ntt[L].empty() || !mac[L].empty() || !split[L].empty() || !finish[L].empty()) return false;
+        if (!ntt[L].empty() || !mac[L].empty() || !split[L].empty() || !triple[L].empty() || !finish[L].empty())
+            return false;
     return d2h.empty();
 }
 
@@ -137,19 +139,26 @@ int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
              })))
             return rc;
     }
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < 3; ++pass) {
         for (int L = 0; L <= kLogMaxProverRing; ++L) {
-            auto& v = pass == 0 ? mac[L] : split[L];
+            auto& v = pass == 0 ? mac[L] : (pass == 1 ? split[L] : triple[L]);
             if (v.empty()) continue;
-            double macs = 0;
-            for (auto& j : v) macs += (double)j.count * 64.0 * (double)(1u << L) * (pass == 0 ? 1.0 : 2.0);
-            // bytes: G residues (4 B per column, coordinate, prime, slot) + M residues (shared by 8 coordinates)
-            double bytes = 0;
-            for (auto& j : v) bytes += (double)j.count * (double)(1u << L) * (64.0 * 4 + 8.0 * 4);
-            if ((rc = timed(pass == 0 ? "mac" : "mac_split", bytes, macs, [&] {
+            // columns read: count (plain, split) or 2 * count (triple pairs)
+            const double cols_per_count = pass == 2 ? 2.0 : 1.0;
+            const double macs_per_col = pass == 0 ? 1.0 : 2.0;
+            double macs = 0, bytes = 0;
+            for (auto& j : v) {
+                const double cols = (double)j.count * cols_per_count;
+                macs += cols * 64.0 * (double)(1u << L) * macs_per_col;
+                // G residues (4 B per column, coordinate, prime, slot) + M residues (shared by 8 coordinates)
+                bytes += cols * (double)(1u << L) * (64.0 * 4 + 8.0 * 4);
+            }
+            const char* name = pass == 0 ? "mac" : (pass == 1 ? "mac_split" : "mac");
+            if ((rc = timed(name, bytes, macs, [&] {
                      for (size_t i = 0; i < v.size(); i += kMaxJobs) {
                          const int n = (int)std::min<size_t>(kMaxJobs, v.size() - i);
-                         cudaError_t e = launch_mac_jobs(T, v.data() + i, n, (uint32_t)L, pass == 1, st);
+                         cudaError_t e = pass == 2 ? launch_mac_triple_jobs(T, v.data() + i, n, (uint32_t)L, st)
+                                                   : launch_mac_jobs(T, v.data() + i, n, (uint32_t)L, pass == 1, st);
                          if (e != cudaSuccess) return (int)e;
                          ++launches;
                      }
@@ -303,18 +312,17 @@ void ProofState::plan_stage(Plan& P) {
         P.ntt[L].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), S, 0});
         P.ntt[L].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * S, 0});
         const int nj = S >= 2 ? 3 : 1;
-        parts_ = mac_parts(S, nj, S / 2 ? S / 2 : 1);
+        parts_ = mac_parts(S, 1, S / 2 ? S / 2 : 1);
         const size_t pstride = (size_t)parts_ * 64 * S;
-        P.mac[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, S, parts_, 0});
-        P.finish[L].push_back(FinishJobX{part, cs(kC), nullptr, nullptr, parts_, kFinishPlain});
         if (nj == 3) {
-            P.mac[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part + pstride, nullptr, nullptr, S / 2,
-                                       0, S / 2, parts_, 0});
-            P.mac[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part + 2 * pstride, nullptr, nullptr, 0,
-                                       S / 2, S / 2, parts_, 0});
+            P.triple[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
+                                          part + 2 * pstride, 0, 0, S / 2, parts_, 0});
             P.finish[L].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain});
             P.finish[L].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain});
+        } else {
+            P.mac[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, S, parts_, 0});
         }
+        P.finish[L].push_back(FinishJobX{part, cs(kC), nullptr, nullptr, parts_, kFinishPlain});
         P.d2h.push_back(Copy{tail, misc_.as<uint8_t>(), 32});
         P.d2h.push_back(Copy{pinned_, cs(kC), slot * 16});
         if (nj == 3) {
@@ -357,18 +365,17 @@ void ProofState::plan_stage(Plan& P) {
         P.ntt[Ln].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
         P.ntt[Ln].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
         const int nj = h >= 2 ? 3 : 1;
-        parts_ = mac_parts(h, nj, h / 2 ? h / 2 : 1);
+        parts_ = mac_parts(h, 1, h / 2 ? h / 2 : 1);
         const size_t pstride = (size_t)parts_ * 64 * h;
-        P.mac[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, h, parts_, 0});
-        P.finish[Ln].push_back(FinishJobX{part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain});
         if (nj == 3) {
-            P.mac[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part + pstride, nullptr, nullptr, h / 2,
-                                        0, h / 2, parts_, 0});
-            P.mac[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part + 2 * pstride, nullptr, nullptr, 0,
-                                        h / 2, h / 2, parts_, 0});
+            P.triple[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
+                                           part + 2 * pstride, 0, 0, h / 2, parts_, 0});
             P.finish[Ln].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain});
             P.finish[Ln].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain});
+        } else {
+            P.mac[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, h, parts_, 0});
         }
+        P.finish[Ln].push_back(FinishJobX{part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain});
         P.d2h.push_back(Copy{pinned_, cs(kC), (size_t)kRank * h * 16});
         if (nj == 3) {
             P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kL), (size_t)kRank * h * 16});

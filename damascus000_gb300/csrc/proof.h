@@ -36,6 +36,7 @@ class Plan {
     std::vector<NttJob> ntt[kLogMaxProverRing + 1];
     std::vector<MacJobX> mac[kLogMaxProverRing + 1];
     std::vector<MacJobX> split[kLogMaxProverRing + 1];
+    std::vector<MacJobX> triple[kLogMaxProverRing + 1];
     std::vector<FinishJobX> finish[kLogMaxProverRing + 1];
     std::vector<Copy> d2h;
     // Launches every non-empty job kind in dependency order on `st`, then the copies.

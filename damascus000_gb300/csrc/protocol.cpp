@@ -160,38 +160,45 @@ fq Transcript::challenge_poly(uint64_t round, const Module& c, const Module& l, 
     return challenge("poly", round, c, l, r);
 }
 
-// transcript.rs:82-90
-static void absorb_commitment(Blake3Hasher& h, const Module& m) {
-    h.update_u64(kRank);
-    std::vector<uint8_t> buf((size_t)m.n * 16);
+// transcript.rs:82-90: u64 K || per coordinate u64 n || n x 16-byte LE words
+static void append_commitment(std::vector<uint8_t>& msg, const Module& m) {
+    put_u64(msg, kRank);
     for (int k = 0; k < kRank; ++k) {
-        h.update_u64(m.n);
-        for (uint32_t j = 0; j < m.n; ++j) fq_to_bytes(m.c[(size_t)k * m.n + j], buf.data() + 16 * j);
-        h.update(buf.data(), buf.size());
+        put_u64(msg, m.n);
+        const size_t base = msg.size();
+        msg.resize(base + (size_t)m.n * 16);
+        uint8_t* p = msg.data() + base;
+        const fq* c = m.c.data() + (size_t)k * m.n;
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+        std::memcpy(p, c, (size_t)m.n * 16);  // limbs are little-endian words
+#else
+        for (uint32_t j = 0; j < m.n; ++j) fq_to_bytes(c[j], p + 16 * j);
+#endif
     }
 }
 
-// transcript.rs:42-75: the absorbed prefix is shared by every counter value.
+// transcript.rs:42-75: the absorbed bytes are assembled once and hashed in
+// parallel; only the trailing u32 counter changes between attempts.
 fq Transcript::challenge(const char* label, uint64_t round, const Module& c, const Module& l, const Module& r) const {
-    Blake3Hasher h;
-    h.update(epoch_seed_, 32);
+    std::vector<uint8_t> msg;
+    msg.reserve(128 + 3 * (8 + (size_t)kRank * 8) + 16 * (c.c.size() + l.c.size() + r.c.size()));
+    msg.insert(msg.end(), epoch_seed_, epoch_seed_ + 32);
     const size_t ll = std::strlen(label);
-    h.update_u64(ll);
-    h.update(label, ll);
-    h.update_u64(32);
-    h.update(file_id_, 32);
-    h.update_u64(0);  // epoch_index
-    h.update_u64(round);
-    absorb_commitment(h, c);
-    absorb_commitment(h, l);
-    absorb_commitment(h, r);
+    put_u64(msg, ll);
+    msg.insert(msg.end(), label, label + ll);
+    put_u64(msg, 32);
+    msg.insert(msg.end(), file_id_, file_id_ + 32);
+    put_u64(msg, 0);  // epoch_index
+    put_u64(msg, round);
+    append_commitment(msg, c);
+    append_commitment(msg, l);
+    append_commitment(msg, r);
+    const size_t prefix = msg.size();
+    msg.resize(prefix + 4);
     for (uint32_t counter = 0;; ++counter) {
-        Blake3Hasher t = h;
-        const uint8_t cb[4] = {(uint8_t)counter, (uint8_t)(counter >> 8), (uint8_t)(counter >> 16),
-                               (uint8_t)(counter >> 24)};
-        t.update(cb, 4);
+        for (int i = 0; i < 4; ++i) msg[prefix + i] = (uint8_t)(counter >> (8 * i));
         uint8_t out[32];
-        t.finalize(out);
+        blake3_hash_parallel(msg.data(), msg.size(), out);
         const fq v = fq_from_hash(out);
         if (!fq_is_zero(v)) return v;
     }

@@ -1,0 +1,290 @@
+#include "serve.h"
+
+#include <chrono>
+#include <cstring>
+#include <limits>
+
+namespace dm {
+
+using Clock = std::chrono::steady_clock;
+
+struct Engine::Request {
+    uint64_t ticket = 0;
+    uint8_t* pinned_file = nullptr;  // staged copy of the file (pinned host memory)
+    size_t pinned_bytes = 0;
+    const uint8_t* device_file = nullptr;  // caller-owned device copy instead
+    uint64_t len = 0;
+    uint8_t seed[32], epoch[32];
+    std::unique_ptr<ProofState> ps;
+    enum State { Queued, Active, Done, Failed } state = Queued;
+    std::vector<uint8_t> proof;
+    std::string err;
+    int err_code = 0;
+    uint64_t footprint = 0;
+    Clock::time_point t_submit, t_done;
+};
+
+struct Engine::Wave {
+    Engine* eng;
+    std::vector<Request*> reqs;
+    int stream_idx;
+};
+
+Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_waves_(max_waves > 0 ? max_waves : 2) {
+    cudaSetDevice(ctx_->device());
+    cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&admit_ev_, cudaEventDisableTiming);
+    wave_streams_.resize(max_waves_);
+    wave_stream_busy_.assign(max_waves_, false);
+    for (auto& s : wave_streams_) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    int n = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency() - 1;
+    if (n < 1) n = 1;
+    sched_thread_ = std::thread([this] { scheduler(); });
+    for (int i = 0; i < n; ++i) workers_.emplace_back([this] { worker(); });
+}
+
+Engine::~Engine() {
+    drain();
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        stop_ = true;
+    }
+    sched_cv_.notify_all();
+    work_cv_.notify_all();
+    if (sched_thread_.joinable()) sched_thread_.join();
+    for (auto& t : workers_) t.join();
+    cudaSetDevice(ctx_->device());
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (auto& kv : all_) {
+        Request* r = kv.second.get();
+        if (r->ps) r->ps->release();
+        if (r->pinned_file) ctx_->put_pinned(r->pinned_file, r->pinned_bytes);
+    }
+    all_.clear();
+    for (auto& s : wave_streams_) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    if (admit_ev_) cudaEventDestroy(admit_ev_);
+    if (stream_) {
+        cudaStreamSynchronize(stream_);
+        cudaStreamDestroy(stream_);
+    }
+}
+
+int Engine::take_wave_stream() {
+    for (int i = 0; i < (int)wave_stream_busy_.size(); ++i)
+        if (!wave_stream_busy_[i]) {
+            wave_stream_busy_[i] = true;
+            return i;
+        }
+    return -1;
+}
+
+int Engine::submit(const uint8_t* file, uint64_t len, const uint8_t seed[32], const uint8_t epoch[32],
+                   uint64_t* ticket, bool on_device) {
+    if ((!file && len) || !seed || !epoch || !ticket) return kEInval;
+    std::unique_ptr<Request> r(new Request());
+    r->len = len;
+    std::memcpy(r->seed, seed, 32);
+    std::memcpy(r->epoch, epoch, 32);
+    r->footprint = ProofState::footprint(len);
+    if (on_device) {
+        r->device_file = file;
+    } else {
+        r->pinned_bytes = len ? len : 1;
+        r->pinned_file = static_cast<uint8_t*>(ctx_->get_pinned(r->pinned_bytes));
+        if (!r->pinned_file) return kENoMem;
+        if (len) std::memcpy(r->pinned_file, file, len);
+    }
+    r->ps.reset(new ProofState(ctx_));
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        r->ticket = next_ticket_++;
+        *ticket = r->ticket;
+        queued_.push_back(r.get());
+        all_[r->ticket] = std::move(r);
+        stats_.submitted++;
+    }
+    sched_cv_.notify_one();
+    return kOk;
+}
+
+void CUDART_CB Engine::on_wave_done(void* arg) {
+    Wave* w = static_cast<Wave*>(arg);
+    Engine* e = w->eng;
+    {
+        std::lock_guard<std::mutex> g(e->mu_);
+        for (Request* r : w->reqs) e->host_q_.push_back(r);
+        e->inflight_waves_--;
+        e->wave_stream_busy_[w->stream_idx] = false;
+    }
+    e->work_cv_.notify_all();
+    e->sched_cv_.notify_one();
+    delete w;
+}
+
+void Engine::scheduler() {
+    cudaSetDevice(ctx_->device());
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+        sched_cv_.wait(lk, [&] {
+            return stop_ ||
+                   (inflight_waves_ < max_waves_ && (!ready_.empty() || (!queued_.empty() && !admit_blocked_)));
+        });
+        if (stop_) return;
+        // Admission in arrival order while the HBM budget holds the request's footprint.
+        while (!queued_.empty()) {
+            Request* r = queued_.front();
+            const uint64_t reserved = ctx_->reserved();
+            if (reserved + r->footprint > ctx_->budget()) {
+                const bool idle = ready_.empty() && host_q_.empty() && inflight_waves_ == 0 && reserved == 0;
+                if (!idle) {
+                    admit_blocked_ = true;  // wait for running requests to release memory
+                    break;
+                }
+            }
+            queued_.pop_front();
+            lk.unlock();
+            const bool dev = r->device_file != nullptr;
+            const int rc = r->ps->setup(dev ? r->device_file : r->pinned_file, r->len, dev, r->seed, r->epoch,
+                                        std::numeric_limits<uint64_t>::max(), stream_);
+            lk.lock();
+            if (rc != kOk) {
+                r->err = r->ps->error();
+                r->err_code = rc;
+                lk.unlock();
+                finish_request(r);
+                lk.lock();
+                continue;
+            }
+            r->state = Request::Active;
+            ready_.push_back(r);
+            if (ctx_->reserved() > stats_.peak_reserved) stats_.peak_reserved = ctx_->reserved();
+        }
+        if (ready_.empty() || inflight_waves_ >= max_waves_) continue;
+        const int si = take_wave_stream();
+        if (si < 0) continue;
+        Wave* w = new Wave{this, {}, si};
+        w->reqs.swap(ready_);
+        inflight_waves_++;
+        lk.unlock();
+        cudaStream_t ws = wave_streams_[si];
+        // admissions (allocations, file copies) on stream_ precede the wave's kernels
+        cudaEventRecord(admit_ev_, stream_);
+        cudaStreamWaitEvent(ws, admit_ev_, 0);
+        Plan plan;
+        for (Request* r : w->reqs) r->ps->plan_stage(plan);
+        std::string err;
+        const int n = plan.launch(ctx_, ws, &err);
+        cudaError_t e = cudaSuccess;
+        if (n >= 0) e = cudaLaunchHostFunc(ws, on_wave_done, w);
+        lk.lock();
+        if (n < 0 || e != cudaSuccess) {
+            inflight_waves_--;
+            wave_stream_busy_[si] = false;
+            std::vector<Request*> reqs = w->reqs;
+            delete w;
+            lk.unlock();
+            for (Request* r : reqs) {
+                r->err = n < 0 ? err : std::string("cudaLaunchHostFunc: ") + cudaGetErrorString(e);
+                r->err_code = kECuda;
+                finish_request(r);
+            }
+            lk.lock();
+            continue;
+        }
+        stats_.waves++;
+        stats_.launches += (uint64_t)n;
+    }
+}
+
+void Engine::worker() {
+    cudaSetDevice(ctx_->device());
+    for (;;) {
+        Request* r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            work_cv_.wait(lk, [&] { return stop_ || !host_q_.empty(); });
+            if (host_q_.empty()) return;
+            r = host_q_.front();
+            host_q_.pop_front();
+        }
+        const int rc = r->ps->complete_stage();
+        if (rc != kOk) {
+            r->err = r->ps->error();
+            r->err_code = rc;
+            finish_request(r);
+            continue;
+        }
+        if (r->ps->stage() == Stage::Done) {
+            r->ps->encode_proof(&r->proof);
+            finish_request(r);
+            continue;
+        }
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            ready_.push_back(r);
+        }
+        sched_cv_.notify_one();
+    }
+}
+
+void Engine::finish_request(Request* r) {
+    const bool ok = r->err_code == 0;
+    r->ps->release();  // stream-ordered frees; returns the budget
+    r->t_done = Clock::now();
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        if (r->pinned_file) ctx_->put_pinned(r->pinned_file, r->pinned_bytes);
+        r->pinned_file = nullptr;
+        r->state = ok ? Request::Done : Request::Failed;
+        admit_blocked_ = false;
+        if (ok) {
+            stats_.completed++;
+            stats_.bytes_done += r->len;
+        } else {
+            stats_.failed++;
+        }
+    }
+    done_cv_.notify_all();
+    sched_cv_.notify_one();
+}
+
+int Engine::poll(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err) {
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = all_.find(ticket);
+    if (it == all_.end()) return kEInval;
+    Request* r = it->second.get();
+    if (r->state != Request::Done && r->state != Request::Failed) return 0;
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    const int rc = r->state == Request::Done ? 1 : (r->err_code ? r->err_code : kECuda);
+    if (proof) *proof = std::move(r->proof);
+    if (err) *err = r->err;
+    all_.erase(it);
+    return rc;
+}
+
+int Engine::wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err) {
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        auto it = all_.find(ticket);
+        if (it == all_.end()) return kEInval;
+        Request* r = it->second.get();
+        done_cv_.wait(lk, [&] { return r->state == Request::Done || r->state == Request::Failed; });
+    }
+    return poll(ticket, proof, latency_ms, err);
+}
+
+void Engine::drain() {
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return stats_.completed + stats_.failed == stats_.submitted; });
+}
+
+EngineStats Engine::stats() {
+    std::lock_guard<std::mutex> g(mu_);
+    return stats_;
+}
+
+}  // namespace dm

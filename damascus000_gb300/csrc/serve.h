@@ -1,0 +1,83 @@
+// Continuous-batching proof engine.
+//
+// Requests (commit + prove of one file) are admitted against the context's HBM
+// budget and keep their witness, generators and fold state resident on the
+// device until their last round.  A scheduler thread gathers the next GPU stage
+// of every ready request into one Plan ("wave"): same-degree rounds of different
+// requests land in the same kernel launches.  A host callback after each wave's
+// device->host copies hands its requests to a pool of host workers, which run
+// the Fiat-Shamir part of the stage (transcript hashing, recompute verdicts,
+// records) and return the requests to the ready set.  Several waves are in
+// flight at once, so the GPU works on some requests while the host hashes for
+// others.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "proof.h"
+
+namespace dm {
+
+struct EngineStats {
+    uint64_t submitted = 0, completed = 0, failed = 0, waves = 0, launches = 0;
+    uint64_t bytes_done = 0;
+    uint64_t peak_reserved = 0;
+};
+
+class Engine {
+   public:
+    Engine(Context* ctx, int host_threads, int max_waves);
+    ~Engine();
+
+    // Copies the file; returns a ticket.  Never blocks on the GPU.  With
+    // on_device the file is a device pointer that must stay valid until the
+    // request finishes (no copy is made).
+    int submit(const uint8_t* file, uint64_t len, const uint8_t seed[32], const uint8_t epoch[32], uint64_t* ticket,
+               bool on_device = false);
+    // 1 = finished (proof moved out), 0 = still running, < 0 = the request failed.
+    int poll(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err);
+    // Blocks until the ticket finishes; same results as poll.
+    int wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err);
+    void drain();  // blocks until every submitted request has finished
+    EngineStats stats();
+
+   private:
+    struct Request;
+    struct Wave;
+    int take_wave_stream();  // index of an idle wave stream (called with mu_ held)
+    static void CUDART_CB on_wave_done(void* arg);
+    void scheduler();
+    void worker();
+    void finish_request(Request* r);
+
+    Context* ctx_;
+    int max_waves_;
+    cudaStream_t stream_ = nullptr;            // admission: allocations, file copies, frees
+    std::vector<cudaStream_t> wave_streams_;  // one per in-flight wave, so waves overlap on the GPU
+    std::vector<bool> wave_stream_busy_;
+    cudaEvent_t admit_ev_ = nullptr;
+    std::mutex mu_;
+    std::condition_variable sched_cv_, done_cv_, work_cv_;
+    std::deque<Request*> queued_;  // submitted, not admitted
+    std::vector<Request*> ready_;  // next stage can be launched
+    std::deque<Request*> host_q_;  // stage copies landed, host part pending
+    std::map<uint64_t, std::unique_ptr<Request>> all_;
+    uint64_t next_ticket_ = 1;
+    int inflight_waves_ = 0;
+    bool admit_blocked_ = false;  // the queue head waits for memory; cleared when a request finishes
+    bool stop_ = false;
+    EngineStats stats_;
+    std::thread sched_thread_;
+    std::vector<std::thread> workers_;
+};
+
+}  // namespace dm

@@ -161,6 +161,34 @@ void damascus_verifier_dimensions(const damascus_verifier* v, uint64_t* vector_l
 /* One-shot verification of a damascus_prove() proof: 0 accepts. */
 int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const uint8_t epoch_seed[32]);
 
+/* ------------------------------------------------------------------ batching / serving */
+/* Continuous-batching engine (no counterpart in the reference, which proves one
+ * file at a time): submitted commit+prove requests are admitted against the
+ * context's HBM budget, keep their state on the device across rounds, and the
+ * same stage of every ready request runs in shared launches while host threads
+ * compute the Fiat-Shamir challenges of others.  host_threads / max_waves <= 0
+ * pick defaults (cores - 1 / 3).  Proofs are the same bytes damascus_prove
+ * returns. */
+typedef struct damascus_engine damascus_engine;
+int damascus_engine_create(damascus_ctx* ctx, int host_threads, int max_waves, damascus_engine** out);
+void damascus_engine_destroy(damascus_engine* e);
+/* Copies the file and returns at once with a ticket. */
+int damascus_engine_submit(damascus_engine* e, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
+                           const uint8_t epoch_seed[32], uint64_t* ticket);
+/* Same with the file already in device memory; d_file must stay valid until the
+ * request finishes. */
+int damascus_engine_submit_device(damascus_engine* e, const void* d_file, size_t len,
+                                  const uint8_t seed_generators[32], const uint8_t epoch_seed[32], uint64_t* ticket);
+/* 1 = finished (proof kept for damascus_engine_take), 0 = running, < 0 = failed. */
+int damascus_engine_poll(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms);
+/* Blocks until the ticket finishes; same results as poll. */
+int damascus_engine_wait(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms);
+/* Copies a finished proof out and forgets it (DAMASCUS_ESIZE keeps it). */
+int damascus_engine_take(damascus_engine* e, uint64_t ticket, uint8_t* proof_out, size_t cap);
+int damascus_engine_drain(damascus_engine* e);
+int damascus_engine_stats(damascus_engine* e, uint64_t* completed, uint64_t* failed, uint64_t* waves,
+                          uint64_t* launches, uint64_t* peak_reserved_bytes);
+
 /* ------------------------------------------------------------------ reference FFI */
 /* Drop-in for the reference's own CUDA hooks, same signatures and argument
  * meaning (src/utils/gpu.rs:69-93; cuda/fold_kernel.cu:209, cuda/ntt_kernel.cu:106).

@@ -1,0 +1,95 @@
+"""Continuous-batching engine: every proof is byte-identical to the plain
+one-at-a-time path (and to the oracle for small files), whether the request ran
+alone or mixed with others of different depths; admission respects the HBM
+budget; a failing request does not disturb the others."""
+import random
+
+import pytest
+
+import damascus000_gb300 as D
+from damascus000_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+EPOCH = bytes([11]) * 32
+
+
+def _files(seed, sizes):
+    return [synth.random_file(seed, n, i) for i, n in enumerate(sizes)]
+
+
+def test_engine_proofs_match_plain_path_and_oracle(ctx, oracle_lib):
+    sizes = [1, 8192, 53_248, 60_000, 200_000, 300_000, 900_000]
+    files = _files(31, sizes)
+    with D.Engine(ctx) as eng:
+        proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
+    for (d, s), p in zip(files, proofs):
+        assert p == ctx.prove(d, s, EPOCH), len(d)
+    for (d, s), p in list(zip(files, proofs))[:3]:
+        assert p == oracle_lib.prove(d, s, EPOCH)
+    assert ctx.verify(proofs[-1], EPOCH)
+
+
+def test_engine_result_same_alone_and_in_mix(ctx):
+    target = synth.random_file(77, 150_000, 0)
+    with D.Engine(ctx) as eng:
+        alone = eng.wait(eng.submit(*target, EPOCH))[0]
+    rng = random.Random(5)
+    others = _files(78, [rng.choice([2_000, 60_000, 400_000, 1 << 20, 3 << 20]) for _ in range(24)])
+    with D.Engine(ctx, host_threads=4, max_waves=3) as eng:
+        tickets = [eng.submit(d, s, EPOCH) for d, s in others[:12]]
+        t = eng.submit(*target, EPOCH)
+        tickets += [eng.submit(d, s, EPOCH) for d, s in others[12:]]
+        mixed = eng.wait(t)[0]
+        rest = [eng.wait(x)[0] for x in tickets]
+        st = eng.stats()
+    assert mixed == alone
+    assert st["completed"] == 25 and st["failed"] == 0
+    # coalescing: far fewer waves than the per-request stage count
+    assert st["waves"] < 25 * 2 * 9
+    for (d, s), p in list(zip(others, rest))[::6]:
+        assert p == ctx.prove(d, s, EPOCH)
+
+
+def test_engine_admission_respects_budget():
+    big = D.prover_footprint(1 << 20)
+    c = D.Context(0, hbm_budget_bytes=int(big * 2.5))
+    try:
+        files = _files(91, [1 << 20] * 6 + [30_000] * 4)
+        with D.Engine(c) as eng:
+            proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
+            st = eng.stats()
+        assert st["completed"] == 10
+        assert st["peak_reserved"] <= c.budget
+        assert c.reserved == 0
+        for (d, s), p in list(zip(files, proofs))[::4]:
+            assert c.verify(p, EPOCH)
+    finally:
+        c.close()
+
+
+def test_engine_failure_is_isolated(ctx):
+    good = _files(92, [40_000, 70_000])
+    with D.Engine(ctx) as eng:
+        t0 = eng.submit(*good[0], EPOCH)
+        # 54.5 MB + 1 byte lands on depth 12, above the supported maximum
+        bad = eng.submit(bytes(2048 * 2048 * 13 + 1), bytes(32), EPOCH)
+        t1 = eng.submit(*good[1], EPOCH)
+        p0 = eng.wait(t0)[0]
+        with pytest.raises(D.DamascusError) as e:
+            eng.wait(bad)
+        p1 = eng.wait(t1)[0]
+    assert e.value.code == D.EUNSUPPORTED
+    assert p0 == ctx.prove(*good[0], EPOCH)
+    assert p1 == ctx.prove(*good[1], EPOCH)
+
+
+def test_engine_device_resident_submission(ctx):
+    torch = pytest.importorskip("torch")
+    files = _files(93, [50_000, 500_000])
+    dev = [torch.frombuffer(bytearray(d), dtype=torch.uint8).cuda() for d, _ in files]
+    torch.cuda.synchronize()
+    with D.Engine(ctx) as eng:
+        ts = [eng.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s) in zip(dev, files)]
+        proofs = [eng.wait(t)[0] for t in ts]
+    for (d, s), p in zip(files, proofs):
+        assert p == ctx.prove(d, s, EPOCH)

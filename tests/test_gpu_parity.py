@@ -250,6 +250,18 @@ def test_d9_prove_verifies_on_gpu_and_oracle(ctx, oracle_lib):
     assert oracle_lib.verify(proof, EPOCH) == 0
 
 
+@pytest.mark.parametrize("nbytes,seed", [(5_689_247, 5), (14_000_000, 5), (3_500_000, 5)])
+def test_deep_proofs_verify_and_match_engine(ctx, nbytes, seed):
+    """Depths 10 and 11 on files whose transforms meet products with a zero
+    Montgomery quotient (v * w * p^-1 = 0 mod 2^32): the prover's recompute
+    checks pass, the proof verifies, and the engine gives the same bytes."""
+    data, fseed = synth.random_file(seed, nbytes, 1)
+    proof = ctx.prove(data, fseed, EPOCH)
+    assert ctx.verify(proof, EPOCH)
+    with D.Engine(ctx, max_waves=2) as eng:
+        assert eng.wait(eng.submit(data, fseed, EPOCH))[0] == proof
+
+
 @pytest.mark.slow
 def test_d11_prove_verifies_on_gpu(ctx):
     data, seed = synth.random_file(11, 16 << 20, 0)

@@ -101,3 +101,25 @@ def test_context_without_gpu_fails_loudly():
         return
     ctx.close()
     pytest.skip("a GPU is present; the no-GPU failure path is not reachable here")
+
+
+def test_parallel_hashing_from_many_threads(oracle_lib):
+    """The host hashing pool is shared by every prover and engine worker: many
+    concurrent large hashes must all complete with the right digest."""
+    import threading
+    data = [bytes((i * 7 + k) & 0xFF for i in range(300_000 + 1024 * k)) for k in range(4)]
+    want = [oracle_lib.blake3(d) for d in data]
+    errors = []
+
+    def run(k):
+        for it in range(60):
+            j = (k + it) % 4
+            if D.blake3(data[j]) != want[j]:
+                errors.append((k, it))
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
