@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/damascus.h"
+#include "dm_jobs.cuh"
 #include "dm_tables.h"
 #include "engine.h"
 #include "proof.h"
@@ -234,30 +235,37 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
                                     uint64_t n, uint8_t* com_out) {
     if (!ctx || !witness || !generators || !com_out || N == 0 || !pow2(n) || n > (1u << kLogMaxProverRing))
         return set_err(ctx, DAMASCUS_EINVAL, "bad commitment shape");
-    // CRT headroom of the single NTT-domain sum: N * n * q^2 < P / 2.
-    if (N * n > (1ull << 22)) return set_err(ctx, DAMASCUS_EUNSUPPORTED, "N * n above 2^22 exceeds the CRT range");
+    // CRT headroom of the single NTT-domain sum: N * n * q^2 < P / 2 (P > 2^269).
+    if (N * n > (1ull << 24)) return set_err(ctx, DAMASCUS_EUNSUPPORTED, "N * n above 2^24 exceeds the CRT range");
+    if (N > 0xFFFFFFFFull / kRank) return set_err(ctx, DAMASCUS_EINVAL, "too many columns");
     Context* C = ctx->ctx;
     std::lock_guard<std::mutex> g(C->mutex());
     cudaSetDevice(C->device());
     const DeviceTables& T = C->tables();
     const uint32_t L = log2u(n);
+    const uint32_t rows = kRank * kPrimes;
+    uint32_t parts = (uint32_t)((1216 + ((n + 127) / 128) * rows - 1) / (((n + 127) / 128) * rows));
+    if (parts > 16) parts = 16;
+    if (parts > N) parts = (uint32_t)N;
     Scratch m, gg, mh, gh, part, out;
-    const uint32_t parts = 1;
-    if (m.alloc(C, N * n * 16) || gg.alloc(C, N * kRank * n * 16) || mh.alloc(C, N * n * 32) ||
-        gh.alloc(C, N * kRank * n * 32) || part.alloc(C, (size_t)parts * 64 * n * 4) || out.alloc(C, kRank * n * 16))
+    if (m.alloc(C, N * n * 16) || gg.alloc(C, N * kRank * n * 16) || mh.alloc(C, N * kPrimes * n * 4) ||
+        gh.alloc(C, N * kRank * kPrimes * n * 4) || part.alloc(C, (size_t)parts * rows * n * 4) ||
+        out.alloc(C, kRank * n * 16))
         return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
     cudaStream_t s = C->stream();
-    MacJob job{0, 0, (uint32_t)N};
-    FinishJob fj{part.m.as<uint32_t>(), parts, L, kFinishPlain, out.m.as<uint4>()};
+    NttJob nj[2] = {{m.m.as<uint4>(), mh.m.as<uint32_t>(), (uint32_t)N, 0},
+                    {gg.m.as<uint4>(), gh.m.as<uint32_t>(), (uint32_t)(N * kRank), 0}};
+    MacJobX mj{gh.m.as<uint32_t>(), mh.m.as<uint32_t>(), part.m.as<uint32_t>(), nullptr, nullptr, 0, 0, (uint32_t)N,
+               parts, 0};
+    FinishJobX fj{part.m.as<uint32_t>(), out.m.as<uint4>(), nullptr, nullptr, parts, kFinishPlain, rows, 0};
     cudaError_t e = cudaMemcpyAsync(m.m.as<uint8_t>(), witness, N * n * 16, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(gg.m.as<uint8_t>(), generators, N * kRank * n * 16, cudaMemcpyHostToDevice, s);
     // inputs may be any 128-bit words: reduce them mod q first
     if (e == cudaSuccess) e = launch_canon(m.m.as<uint4>(), N * n, s);
     if (e == cudaSuccess) e = launch_canon(gg.m.as<uint4>(), N * kRank * n, s);
-    if (e == cudaSuccess) e = launch_ntt_fwd(T, m.m.as<uint4>(), mh.m.as<uint32_t>(), N, L, s);
-    if (e == cudaSuccess) e = launch_ntt_fwd(T, gg.m.as<uint4>(), gh.m.as<uint32_t>(), N * kRank, L, s);
-    if (e == cudaSuccess) e = launch_mac(T, gh.m.as<uint32_t>(), mh.m.as<uint32_t>(), L, &job, 1, parts, part.m.as<uint32_t>(), s);
-    if (e == cudaSuccess) e = launch_finish(T, &fj, 1, s);
+    if (e == cudaSuccess) e = launch_ntt_jobs(T, nj, 2, L, s);
+    if (e == cudaSuccess) e = launch_mac_jobs(T, &mj, 1, L, false, s);
+    if (e == cudaSuccess) e = launch_finish_jobs(T, &fj, 1, L, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(com_out, out.m.as<uint8_t>(), kRank * n * 16, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("commit_with_generators: ") + cudaGetErrorString(e));
@@ -313,13 +321,15 @@ int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const voi
                                    uint64_t count, int sync) {
     if (!ctx || !pow2(n) || n > (1u << kLogMaxProverRing)) return set_err(ctx, DAMASCUS_EINVAL, "bad ring shape");
     if (count == 0) return DAMASCUS_OK;
+    if (count * kPrimes > 0xFFFFFFFFull || ((count * kPrimes * n) >> 8) > 0xFFFFFFFFull)
+        return set_err(ctx, DAMASCUS_EINVAL, "too many products in one call");
     Context* C = ctx->ctx;
     std::lock_guard<std::mutex> g(C->mutex());
     cudaSetDevice(C->device());
     const DeviceTables& T = C->tables();
     const uint32_t L = log2u(n);
     Scratch ra, rb;
-    if (ra.alloc(C, count * n * 32) || rb.alloc(C, count * n * 32))
+    if (ra.alloc(C, count * kPrimes * n * 4) || rb.alloc(C, count * kPrimes * n * 4))
         return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
     cudaStream_t s = C->stream();
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -327,20 +337,25 @@ int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const voi
         e0 = C->take_event();
         cudaEventRecord(e0, s);
     }
-    cudaError_t e = launch_ntt_fwd(T, static_cast<const uint4*>(d_a), ra.m.as<uint32_t>(), count, L, s);
-    if (e == cudaSuccess) e = launch_ntt_fwd(T, static_cast<const uint4*>(d_b), rb.m.as<uint32_t>(), count, L, s);
+    NttJob nj[2] = {{static_cast<const uint4*>(d_a), ra.m.as<uint32_t>(), (uint32_t)count, 0},
+                    {static_cast<const uint4*>(d_b), rb.m.as<uint32_t>(), (uint32_t)count, 0}};
+    cudaError_t e = launch_ntt_jobs(T, nj, 2, L, s);
     if (e0) {
         e1 = C->take_event();
         cudaEventRecord(e1, s);
-        C->record("ntt_fwd", e0, e1, (double)count * n * 96, (double)2 * count * 8 * (n / 2) * L);
+        C->record("ntt_fwd", e0, e1, (double)count * n * (32 + 2 * kPrimes * 4), (double)2 * count * kPrimes * (n / 2) * L);
         e0 = C->take_event();
         cudaEventRecord(e0, s);
     }
-    if (e == cudaSuccess) e = launch_ring_mul(T, ra.m.as<uint32_t>(), rb.m.as<uint32_t>(), static_cast<uint4*>(d_out), count, L, s);
+    PointwiseJob pj{ra.m.as<uint32_t>(), rb.m.as<uint32_t>(), ra.m.as<uint32_t>(), count, 0};
+    FinishJobX fj{ra.m.as<uint32_t>(), static_cast<uint4*>(d_out), nullptr, nullptr, 1, kFinishPlain,
+                  (uint32_t)(count * kPrimes), 0};
+    if (e == cudaSuccess) e = launch_pointwise_jobs(T, &pj, 1, L, s);
+    if (e == cudaSuccess) e = launch_finish_jobs(T, &fj, 1, L, s);
     if (e0) {
         e1 = C->take_event();
         cudaEventRecord(e1, s);
-        C->record("ring_mul", e0, e1, (double)count * n * (64 + 16), (double)count * 8 * (n / 2) * L);
+        C->record("ring_mul", e0, e1, (double)count * n * (3 * kPrimes * 4 + 16), (double)count * kPrimes * (n / 2) * L, 3);
     }
     // Scratch is released when this returns: wait for the kernels that read it.
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -637,15 +652,15 @@ int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint
                             const uint64_t* inv_sizes) {
     if (!host_a || !host_b || !host_out || !primes || !stage_roots || !inv_roots || !inv_sizes || !pow2(n)) return 1;
     if (n > (1u << kLogMaxProverRing)) return 12;
-    for (int i = 0; i < kPrimes; ++i)
-        if (primes[i] != host_tables().pc.p[i]) return 13;  // the kernels are specialised to the reference's primes
+    for (int i = 0; i < kRefPrimes; ++i)
+        if (primes[i] != kRefCrtPrimes[i]) return 13;  // the kernels are specialised to the reference's primes
     damascus_ctx* ctx = default_ctx();
     if (!ctx) return 2;
     Context* C = ctx->ctx;
     std::lock_guard<std::mutex> g(C->mutex());
     cudaSetDevice(C->device());
     Scratch b;
-    const size_t words = (size_t)kPrimes * n;
+    const size_t words = (size_t)kRefPrimes * n;
     if (b.alloc(C, 3 * words * 4)) return 3;
     std::vector<uint32_t> ha(words), hb(words), ho(words);
     for (size_t i = 0; i < words; ++i) {
@@ -658,7 +673,7 @@ int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint
     cudaStream_t s = C->stream();
     if (cudaMemcpyAsync(da, ha.data(), words * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 6;
     if (cudaMemcpyAsync(db, hb.data(), words * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) return 7;
-    if (launch_cyclic_conv(C->tables(), da, db, dout, log2u(n), s) != cudaSuccess) return 8;
+    if (launch_cyclic_conv(C->ref_tables(), da, db, dout, log2u(n), s) != cudaSuccess) return 8;
     if (cudaMemcpyAsync(ho.data(), dout, words * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 15;
     if (cudaStreamSynchronize(s) != cudaSuccess) return 16;
     for (size_t i = 0; i < words; ++i) host_out[i] = ho[i];

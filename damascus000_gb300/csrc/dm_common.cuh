@@ -22,8 +22,14 @@ namespace dm {
 
 // Module rank K of R_q^K (src/utils/config.rs:7).
 constexpr int kRank = 8;
-// Number of CRT primes (src/utils/config.rs:9-18).
-constexpr int kPrimes = 8;
+// NTT primes carrying the ring products: nine primes p < 2^30 with p = 1 mod 2^14
+// (their product P > 2^269 bounds every commitment sum up to depth 12).
+constexpr int kPrimes = 9;
+// Primes per thread block of the transforms (kPrimes / 3 blocks per polynomial).
+constexpr int kPrimesPerBlock = 3;
+// The reference's eight CRT primes (src/utils/config.rs:9-18), used only by the
+// reference-compatible FFI convolution hook, whose caller passes them in.
+constexpr int kRefPrimes = 8;
 // Largest negacyclic NTT the twiddle tables cover: 2^13 points (the prover uses
 // ring degrees up to 2^12; the reference-compatible cyclic convolution of
 // length n <= 2^12 zero-pads to 2n).
@@ -31,8 +37,8 @@ constexpr int kLogMaxRing = 13;
 // Largest ring degree of the commitment / fold kernels.
 constexpr int kLogMaxProverRing = 12;
 constexpr uint32_t kMaxRing = 1u << kLogMaxRing;
-// Depth limit for which summing all N columns in the NTT domain stays inside the
-// CRT range: N * n * q^2 < P / 2 holds up to d = 11 (2^246 < 2^247.016).
+// Deepest fold the prover accepts: the ring of degree 2^d must fit the transform
+// kernels (2^12) and N * n * q^2 < P / 2 must hold (2^248 < 2^268 at d = 12).
 constexpr int kMaxDepth = 11;
 // Minimum fold depth (src/utils/config.rs:5).
 constexpr int kMinDepth = 6;

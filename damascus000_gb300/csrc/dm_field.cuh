@@ -4,9 +4,13 @@
 //    serde form of src/algebra/field.rs:112-129).  Multiplication is a 4x4 limb
 //    schoolbook product reduced with 2^112 = 75 (mod q), the same pseudo-Mersenne
 //    identity as field.rs:229-258.
-//  * Montgomery arithmetic modulo the eight 29..32-bit CRT primes of
-//    src/utils/config.rs:9-18, with R = 2^32.  Five primes exceed 2^31, so lazy
-//    [0, 2p) butterflies do not fit a 32-bit word; every value stays in [0, p).
+//  * Arithmetic modulo the nine NTT primes p < 2^30 (p = 1 mod 2^14) that carry
+//    every ring product: Shoup products by constants give [0, 2p), so the
+//    transforms keep values in [0, 4p) < 2^32 between butterflies (Harvey's lazy
+//    butterflies), and products of two reduced residues fit 60 bits.
+//  * Garner recombination of the nine residues into Z_q with a centred lift
+//    (the integer result of src/algebra/ntt.rs:372-427; P > 2^269 leaves room for
+//    any commitment sum up to depth 12).
 #pragma once
 
 #include "dm_common.cuh"
@@ -172,28 +176,28 @@ inline fq fq_inv(const fq& a) {
     return fq_pow(a, qm2);
 }
 
-// ====================== arithmetic modulo a CRT prime ======================
+// ====================== arithmetic modulo an NTT prime ======================
 
-// Montgomery product a * b * 2^-32 mod p, for a < 2^32 and b < p.  Signed
-// variant: t - m*p has zero low word, so the result is hi(t) - hi(m*p) in (-p, p).
-DM_HD uint32_t mont_mul(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
+DM_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
 #if defined(__CUDA_ARCH__)
-    uint32_t tl = a * b;
-    uint32_t th = __umulhi(a, b);
-    uint32_t m = tl * pinv;
-    uint32_t mh = __umulhi(m, p);
+    return __umulhi(a, b);
 #else
-    uint64_t t = (uint64_t)a * b;
-    uint32_t tl = (uint32_t)t;
-    uint32_t th = (uint32_t)(t >> 32);
-    uint32_t m = tl * pinv;
-    uint32_t mh = (uint32_t)(((uint64_t)m * p) >> 32);
-    (void)tl;
+    return (uint32_t)(((uint64_t)a * b) >> 32);
 #endif
-    uint32_t r = th - mh;
-    return th < mh ? r + p : r;
+}
+DM_HD uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
+
+// x mod p in [0, m) for x in [0, 2m): min(x, x - m) (x - m wraps when x < m).
+DM_HD uint32_t red_below(uint32_t x, uint32_t m) { return umin32(x, x - m); }
+
+// Shoup product x * w mod p in [0, 2p) for any x < 2^32, with w < p < 2^30 and
+// ws = floor(w * 2^32 / p): q = floor(x * ws / 2^32) is floor(x w / p) or one less.
+DM_HD uint32_t shoup_mul(uint32_t x, uint32_t w, uint32_t ws, uint32_t p) {
+    const uint32_t q = mulhi32(x, ws);
+    return x * w - q * p;
 }
 
+// Generic reductions (any p < 2^32) used by the reference-prime FFI path too.
 DM_HD uint32_t add_mod(uint32_t a, uint32_t b, uint32_t p) {
     uint32_t s = a + b;
     return (s < a || s >= p) ? s - p : s;
@@ -202,79 +206,75 @@ DM_HD uint32_t sub_mod(uint32_t a, uint32_t b, uint32_t p) {
     uint32_t d = a - b;
     return a < b ? d + p : d;
 }
-// A 64-bit accumulator hi * 2^32 + lo reduced mod p: mont_mul(hi, R^2) = hi * R,
-// mont_mul(lo, R) = lo (mod p).
-DM_HD uint32_t reduce_u64(uint64_t x, uint32_t p, uint32_t pinv, uint32_t r1, uint32_t r2) {
-    uint32_t h = mont_mul((uint32_t)(x >> 32), r2, p, pinv);
-    uint32_t l = mont_mul((uint32_t)x, r1, p, pinv);
-    return add_mod(h, l, p);
-}
 
-// Constants of the eight primes handed to kernels by value (kernel-parameter space).
+// Constants of the nine NTT primes handed to kernels by value.
 struct PrimeConsts {
     uint32_t p[kPrimes];
-    uint32_t pinv[kPrimes];   // p^-1 mod 2^32
-    uint32_t r1[kPrimes];     // R mod p (Montgomery form of 1)
-    uint32_t r2[kPrimes];     // R^2 mod p
-    uint32_t k32[kPrimes];    // 2^32 * R mod p
-    uint32_t k64[kPrimes];    // 2^64 * R mod p
-    uint32_t k96[kPrimes];    // 2^96 * R mod p
-    uint32_t qres[kPrimes];   // q mod p
-    uint32_t r1p[kPrimes], k32p[kPrimes], k64p[kPrimes], k96p[kPrimes];  // the above times p^-1 mod 2^32
+    uint32_t one_s[kPrimes];  // floor(2^32 / p): Shoup constant of 1
+    uint32_t c1[kPrimes];     // 2^32 mod p
+    uint32_t c1s[kPrimes];    // floor(c1 * 2^32 / p)
+    uint32_t c2[kPrimes];     // 2^64 mod p
+    uint32_t c2s[kPrimes];
+    uint32_t c3[kPrimes];     // 2^96 mod p
 };
 
-// Residue of a Z_q element (four limbs) modulo prime i: sum_j x_j * 2^(32 j).
-DM_HD uint32_t residue(const fq& x, const PrimeConsts& c, int i) {
-    uint32_t p = c.p[i], pi = c.pinv[i];
-    uint32_t r = mont_mul(x.w[0], c.r1[i], p, pi);
-    r = add_mod(r, mont_mul(x.w[1], c.k32[i], p, pi), p);
-    r = add_mod(r, mont_mul(x.w[2], c.k64[i], p, pi), p);
-    r = add_mod(r, mont_mul(x.w[3], c.k96[i], p, pi), p);
-    return r;
+// A 64-bit value mod p in [0, 4p): hi * (2^32 mod p) + lo * 1, two Shoup products.
+DM_HD uint32_t red64_lazy(uint64_t t, const PrimeConsts& c, int i) {
+    const uint32_t p = c.p[i];
+    return shoup_mul((uint32_t)(t >> 32), c.c1[i], c.c1s[i], p) + shoup_mul((uint32_t)t, 1u, c.one_s[i], p);
+}
+DM_HD uint32_t red64(uint64_t t, const PrimeConsts& c, int i) {
+    const uint32_t p = c.p[i];
+    return red_below(red_below(red64_lazy(t, c, i), 2 * p), p);
+}
+// hi * 2^64 + lo (hi < 2^32) mod p in [0, p).
+DM_HD uint32_t red96(uint32_t hi, uint64_t lo, const PrimeConsts& c, int i) {
+    const uint32_t p = c.p[i];
+    const uint32_t a = red_below(red64_lazy(lo, c, i), 2 * p);            // [0, 2p)
+    const uint32_t b = shoup_mul(hi, c.c2[i], c.c2s[i], p);                 // [0, 2p)
+    return red_below(red_below(a + b, 2 * p), p);
 }
 
-// Garner constants for recombining residues into Z_q (a centered lift, as
+// Residue of a 128-bit word x = sum_j x_j 2^(32 j) modulo prime i, in [0, 4p):
+// x_0 + x_1 c1 + x_2 c2 + x_3 c3 < 2^32 + 3 * 2^62 fits one 64-bit accumulation.
+DM_HD uint32_t residue_lazy(const fq& x, const PrimeConsts& c, int i) {
+    const uint64_t t = (uint64_t)x.w[0] + (uint64_t)x.w[1] * c.c1[i] + (uint64_t)x.w[2] * c.c2[i] +
+                       (uint64_t)x.w[3] * c.c3[i];
+    return red64_lazy(t, c, i);
+}
+DM_HD uint32_t residue(const fq& x, const PrimeConsts& c, int i) {
+    const uint32_t p = c.p[i];
+    return red_below(red_below(residue_lazy(x, c, i), 2 * p), p);
+}
+
+// Garner constants for recombining residues into Z_q (a centred lift, as
 // src/algebra/ntt.rs:400-427 does with BigUint).
 struct CrtConsts {
-    uint32_t inv[kPrimes][kPrimes];  // inv[j][i] = p_j^-1 * R mod p_i   (j < i)
-    uint32_t invp[kPrimes][kPrimes]; // inv[j][i] * p_i^-1 mod 2^32
-    uint32_t half_digits[kPrimes];   // mixed-radix digits of (P - 1) / 2
-    fq radix_mod_q[kPrimes];         // prod_{j<i} p_j mod q
-    fq p_mod_q;                      // P mod q
+    uint32_t inv[kPrimes][kPrimes];   // inv[j][i] = p_j^-1 mod p_i   (j < i)
+    uint32_t invs[kPrimes][kPrimes];  // Shoup constants of inv
+    uint32_t half_digits[kPrimes];    // mixed-radix digits of (P - 1) / 2
+    fq radix_mod_q[kPrimes];          // prod_{j<i} p_j mod q
+    fq p_mod_q;                       // P mod q
 };
 
-// Same result as crt_to_fq with three-multiply Montgomery steps and one
-// multi-limb accumulation of sum v_i * (prod_{j<i} p_j mod q) (< 2^147) before a
-// single reduction mod q.
-DM_HD fq crt_to_fq_fast(const uint32_t r[kPrimes], const PrimeConsts& pc, const CrtConsts& cc) {
+// r[i] < p_i -> the integer X with |X| < P/2 congruent to r, reduced mod q.
+// Mixed-radix digits by Garner (each step one Shoup product), then one
+// multi-limb accumulation of sum v_i * (prod_{j<i} p_j mod q) (< 2^147) and a
+// single reduction mod q; X > (P-1)/2 (a negative value) subtracts P mod q.
+DM_HD fq crt_to_fq(const uint32_t r[kPrimes], const PrimeConsts& pc, const CrtConsts& cc) {
     uint32_t v[kPrimes];
     DM_UNROLL
     for (int i = 0; i < kPrimes; ++i) {
         const uint32_t p = pc.p[i];
-        uint32_t t = r[i];
+        uint32_t t = r[i];  // [0, p), then [0, 2p) after each step
         DM_UNROLL
         for (int j = 0; j < i; ++j) {
-            // v_j mod p_i as v_j * R * R^-1
-            uint32_t th, mh;
-#if defined(__CUDA_ARCH__)
-            th = __umulhi(v[j], pc.r1[i]);
-            mh = __umulhi(v[j] * pc.r1p[i], p);
-#else
-            th = (uint32_t)(((uint64_t)v[j] * pc.r1[i]) >> 32);
-            mh = (uint32_t)(((uint64_t)(uint32_t)(v[j] * pc.r1p[i]) * p) >> 32);
-#endif
-            const uint32_t vj = th < mh ? th - mh + p : th - mh;
-            const uint32_t d = sub_mod(t, vj, p);
-#if defined(__CUDA_ARCH__)
-            th = __umulhi(d, cc.inv[j][i]);
-            mh = __umulhi(d * cc.invp[j][i], p);
-#else
-            th = (uint32_t)(((uint64_t)d * cc.inv[j][i]) >> 32);
-            mh = (uint32_t)(((uint64_t)(uint32_t)(d * cc.invp[j][i]) * p) >> 32);
-#endif
-            t = th < mh ? th - mh + p : th - mh;
+            // v_j < p_j < 2^30 < 2 p_i: one conditional subtraction gives v_j mod p_i
+            const uint32_t vj = red_below(v[j], p);
+            const uint32_t tr = red_below(t, p);
+            t = shoup_mul(tr + p - vj, cc.inv[j][i], cc.invs[j][i], p);
         }
-        v[i] = t;
+        v[i] = red_below(t, p);
     }
     int gt = 0, decided = 0;
     DM_UNROLL
@@ -306,36 +306,6 @@ DM_HD fq crt_to_fq_fast(const uint32_t r[kPrimes], const PrimeConsts& pc, const 
     fq x = fq_reduce8(x8);
     if (gt) x = fq_sub(x, cc.p_mod_q);
     return x;
-}
-
-// r[i] < p_i -> the integer X with |X| < P/2 congruent to r, reduced mod q.
-DM_HD fq crt_to_fq(const uint32_t r[kPrimes], const PrimeConsts& pc, const CrtConsts& cc) {
-    uint32_t v[kPrimes];
-DM_UNROLL
-    for (int i = 0; i < kPrimes; ++i) {
-        uint32_t p = pc.p[i], pi = pc.pinv[i];
-        uint32_t t = r[i];
-DM_UNROLL
-        for (int j = 0; j < i; ++j) {
-            uint32_t vj = mont_mul(v[j], pc.r1[i], p, pi);  // v_j mod p_i
-            t = mont_mul(sub_mod(t, vj, p), cc.inv[j][i], p, pi);
-        }
-        v[i] = t;
-    }
-    // X > (P-1)/2  <=>  digits compare greater from the top.
-    int gt = 0, decided = 0;
-DM_UNROLL
-    for (int i = kPrimes - 1; i >= 0; --i) {
-        if (!decided && v[i] != cc.half_digits[i]) {
-            gt = v[i] > cc.half_digits[i];
-            decided = 1;
-        }
-    }
-    fq acc = fq_zero();
-DM_UNROLL
-    for (int i = 0; i < kPrimes; ++i) acc = fq_add(acc, fq_mul(fq_from_u32(v[i]), cc.radix_mod_q[i]));
-    if (gt) acc = fq_sub(acc, cc.p_mod_q);
-    return acc;
 }
 
 }  // namespace dm

@@ -11,7 +11,7 @@ namespace dm {
 
 constexpr int kMaxJobs = 48;
 
-// ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][8][2^L] ----
+// ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][9][2^L] ----
 struct NttJob {
     const uint4* src;
     uint32_t* dst;
@@ -20,7 +20,7 @@ struct NttJob {
 };
 
 // ---- multiply-accumulate over columns (all jobs of a launch share L) ----
-// plain: partials[part][k*8+p][slot] = sum_{i<count} G[g_base+i][k][p][slot] * M[m_base+i][p][slot]
+// plain: partials[part][k*9+p][slot] = sum_{i<count} G[g_base+i][k][p][slot] * M[m_base+i][p][slot]
 // split: chk over 2^L slots, lp / rp over 2^(L-1) (even/odd cross terms)
 struct MacJobX {
     const uint32_t* G;
@@ -33,13 +33,28 @@ struct MacJobX {
 };
 
 // ---- sum partials, inverse NTT, CRT to Z_q, optional compare (all jobs share L) ----
+enum FinishMode : uint32_t { kFinishPlain = 0, kFinishSplitL = 1, kFinishSplitR = 2 };
+// partials: [parts][rows][2^L] residues, rows = npolys * 9 (coordinate-major:
+// row = poly * 9 + prime).  The inverse transform writes its residues over part
+// 0 (each row belongs to one block), then the CRT reads them back.
 struct FinishJobX {
-    const uint32_t* partials;
-    uint4* out;            // [8][2^L]
+    uint32_t* partials;
+    uint4* out;            // [npolys][2^L]
     const uint4* expect;   // compared with out when non-null
     uint32_t* flag;        // set to 1 on mismatch
     uint32_t parts;
     uint32_t mode;         // FinishMode
+    uint32_t rows;         // npolys * kPrimes
+    uint32_t cta0;         // filled by the launcher
+};
+
+// ---- pointwise products of two transformed sets (ring products of pairs) ----
+struct PointwiseJob {
+    const uint32_t* a;  // [npolys][9][2^L]
+    const uint32_t* b;
+    uint32_t* out;
+    uint64_t npolys;
+    uint32_t cta0;
 };
 
 // ---- folds and commitment algebra in the coefficient domain ----
@@ -86,12 +101,12 @@ struct HashJob {
     uint32_t cta0;
 };
 
-cudaError_t upload_tables_ext(DeviceTables* t);  // zetap / zinvp
 cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st);
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st);
 // Triple MAC (count = h column pairs): out0 = full sum, out1 = L, out2 = R.
 cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st);
-cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);
+cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);  // 2 launches
+cudaError_t launch_pointwise_jobs(const DeviceTables& T, PointwiseJob* jobs, int n, uint32_t L, cudaStream_t st);
 cudaError_t launch_fold_jobs(FoldJob* jobs, int n, cudaStream_t st);
 cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st);
 cudaError_t launch_unpack_jobs(UnpackJob* jobs, int n, cudaStream_t st);

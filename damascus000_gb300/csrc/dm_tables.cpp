@@ -4,8 +4,8 @@
 
 namespace dm {
 
-const uint32_t kCrtPrimes[kPrimes] = {3892314113u, 2281701377u, 2013265921u, 2885681153u,
-                                      2483027969u, 1811939329u, 469762049u,  4194304001u};
+const uint32_t kRefCrtPrimes[kRefPrimes] = {3892314113u, 2281701377u, 2013265921u, 2885681153u,
+                                            2483027969u, 1811939329u, 469762049u,  4194304001u};
 
 uint32_t pow_mod(uint32_t b, uint64_t e, uint32_t p) {
     uint64_t r = 1, x = b % p;
@@ -24,7 +24,33 @@ uint32_t bitrev(uint32_t x, int bits) {
     return r;
 }
 
+uint32_t shoup_const(uint32_t w, uint32_t p) { return (uint32_t)(((uint64_t)w << 32) / p); }
+
 namespace {
+
+// Deterministic Miller-Rabin for n < 2^32 (bases 2, 7, 61).
+bool is_prime_u32(uint32_t n) {
+    if (n < 2) return false;
+    for (uint32_t sp : {2u, 3u, 5u, 7u, 11u, 13u, 61u})
+        if (n % sp == 0) return n == sp;
+    uint32_t d = n - 1;
+    int s = 0;
+    while ((d & 1) == 0) {
+        d >>= 1;
+        ++s;
+    }
+    for (uint32_t a : {2u, 7u, 61u}) {
+        uint64_t x = pow_mod(a, d, n);
+        if (x == 1 || x == n - 1) continue;
+        bool comp = true;
+        for (int r = 1; r < s && comp; ++r) {
+            x = x * x % n;
+            if (x == n - 1) comp = false;
+        }
+        if (comp) return false;
+    }
+    return true;
+}
 
 // Smallest generator of Z_p^* (checks x^((p-1)/f) != 1 for each prime f | p-1).
 uint32_t generator_of(uint32_t p) {
@@ -48,98 +74,138 @@ uint32_t generator_of(uint32_t p) {
 uint32_t inv_mod(uint32_t a, uint32_t p) { return pow_mod(a, p - 2, p); }
 uint32_t to_mont(uint32_t a, uint32_t p) { return (uint32_t)((((uint64_t)a) << 32) % p); }
 
-// Minimal little-endian 256-bit integer for the CRT constants.
-struct U256 {
-    uint64_t w[4] = {0, 0, 0, 0};
+// Minimal little-endian 384-bit integer for the CRT constants (P < 2^270).
+struct U384 {
+    uint64_t w[6] = {0, 0, 0, 0, 0, 0};
 };
-void mul_small(U256& a, uint64_t m) {
+void mul_small(U384& a, uint64_t m) {
     unsigned __int128 c = 0;
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < 6; ++i) {
         c += (unsigned __int128)a.w[i] * m;
         a.w[i] = (uint64_t)c;
         c >>= 64;
     }
 }
-uint64_t divmod_small(U256& a, uint64_t m) {  // a /= m, returns remainder
+uint64_t divmod_small(U384& a, uint64_t m) {  // a /= m, returns remainder
     unsigned __int128 r = 0;
-    for (int i = 3; i >= 0; --i) {
+    for (int i = 5; i >= 0; --i) {
         unsigned __int128 cur = (r << 64) | a.w[i];
         a.w[i] = (uint64_t)(cur / m);
         r = cur % m;
     }
     return (uint64_t)r;
 }
-fq mod_q(const U256& a) {
-    uint32_t r[8];
+// a mod q via 2^256 mod q folding: split into 256-bit low part and the rest.
+fq mod_q(const U384& a) {
+    // a < 2^384: a = lo + hi * 2^256, 2^256 mod q computed by fq arithmetic.
+    uint32_t lo[8], hi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int i = 0; i < 4; ++i) {
-        r[2 * i] = (uint32_t)a.w[i];
-        r[2 * i + 1] = (uint32_t)(a.w[i] >> 32);
+        lo[2 * i] = (uint32_t)a.w[i];
+        lo[2 * i + 1] = (uint32_t)(a.w[i] >> 32);
     }
-    return fq_reduce8(r);
+    for (int i = 0; i < 2; ++i) {
+        hi[2 * i] = (uint32_t)a.w[4 + i];
+        hi[2 * i + 1] = (uint32_t)(a.w[4 + i] >> 32);
+    }
+    const fq l = fq_reduce8(lo), h = fq_reduce8(hi);
+    uint32_t two256[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // 2^255 reduced, then doubled
+    two256[7] = 0x80000000u;
+    fq t = fq_reduce8(two256);
+    t = fq_add(t, t);
+    return fq_add(l, fq_mul(h, t));
 }
 
 HostTables build() {
     HostTables t;
-    t.zeta.resize((size_t)kPrimes * kMaxRing);
-    t.zinv.resize((size_t)kPrimes * kMaxRing);
-    t.zetap.resize((size_t)kPrimes * kMaxRing);
-    t.zinvp.resize((size_t)kPrimes * kMaxRing);
+    // the nine largest primes below 2^30 of the form k * 2^14 + 1
+    int found = 0;
+    for (uint32_t k = ((1u << 30) - 1) >> 14; found < kPrimes && k > 0; --k) {
+        const uint32_t p = (k << 14) + 1;
+        if (p < (1u << 30) && is_prime_u32(p)) t.primes[found++] = p;
+    }
+    const size_t tab = (size_t)kPrimes * kMaxRing;
+    t.zeta.resize(tab);
+    t.zetas.resize(tab);
+    t.zinv.resize(tab);
+    t.zinvs.resize(tab);
     for (int i = 0; i < kPrimes; ++i) {
-        const uint32_t p = kCrtPrimes[i];
+        const uint32_t p = t.primes[i];
+        PrimeConsts& c = t.pc;
+        c.p[i] = p;
+        c.one_s[i] = shoup_const(1, p);
+        c.c1[i] = (uint32_t)((1ull << 32) % p);
+        c.c1s[i] = shoup_const(c.c1[i], p);
+        c.c2[i] = (uint32_t)((uint64_t)c.c1[i] * c.c1[i] % p);
+        c.c2s[i] = shoup_const(c.c2[i], p);
+        c.c3[i] = (uint32_t)((uint64_t)c.c2[i] * c.c1[i] % p);
+
+        const uint32_t g = generator_of(p);
+        const uint32_t psi = pow_mod(g, (p - 1) / (2ull * kMaxRing), p);
+        const uint32_t psi_inv = inv_mod(psi, p);
+        for (uint32_t k = 0; k < kMaxRing; ++k) {
+            const uint32_t e = bitrev(k, kLogMaxRing);
+            const size_t at = (size_t)i * kMaxRing + k;
+            t.zeta[at] = pow_mod(psi, e, p);
+            t.zetas[at] = shoup_const(t.zeta[at], p);
+            t.zinv[at] = pow_mod(psi_inv, e, p);
+            t.zinvs[at] = shoup_const(t.zinv[at], p);
+        }
+        const uint32_t inv4 = inv_mod(4, p);
+        for (int L = 0; L <= kLogMaxRing; ++L) {
+            const uint32_t ninv = inv_mod(pow_mod(2, L, p), p);
+            t.ninv[i][L] = ninv;
+            t.ninvs[i][L] = shoup_const(ninv, p);
+            t.ninv4[i][L] = (uint32_t)((uint64_t)ninv * inv4 % p);
+            t.ninv4s[i][L] = shoup_const(t.ninv4[i][L], p);
+        }
+    }
+    // Garner constants.
+    for (int j = 0; j < kPrimes; ++j)
+        for (int i = 0; i < kPrimes; ++i) {
+            t.cc.inv[j][i] = (j < i) ? inv_mod(t.primes[j] % t.primes[i], t.primes[i]) : 0;
+            t.cc.invs[j][i] = shoup_const(t.cc.inv[j][i], t.primes[i]);
+        }
+    U384 prod;
+    prod.w[0] = 1;
+    for (int i = 0; i < kPrimes; ++i) {
+        t.cc.radix_mod_q[i] = mod_q(prod);
+        mul_small(prod, t.primes[i]);
+    }
+    t.cc.p_mod_q = mod_q(prod);
+    // (P - 1) / 2 in mixed radix; P is odd so P - 1 only clears bit 0.
+    U384 half = prod;
+    half.w[0] -= 1;
+    for (int i = 0; i < 6; ++i) half.w[i] = (half.w[i] >> 1) | (i < 5 ? half.w[i + 1] << 63 : 0);
+    for (int i = 0; i < kPrimes; ++i) t.cc.half_digits[i] = (uint32_t)divmod_small(half, t.primes[i]);
+    return t;
+}
+
+RefHostTables build_ref() {
+    RefHostTables t;
+    t.zeta.resize((size_t)kRefPrimes * kMaxRing);
+    t.zinv.resize((size_t)kRefPrimes * kMaxRing);
+    for (int i = 0; i < kRefPrimes; ++i) {
+        const uint32_t p = kRefCrtPrimes[i];
         t.pc.p[i] = p;
         uint32_t inv = 1;  // Newton iteration for p^-1 mod 2^32
         for (int k = 0; k < 5; ++k) inv *= 2u - p * inv;
         t.pc.pinv[i] = inv;
         const uint64_t R = ((uint64_t)1 << 32) % p;
-        t.pc.r1[i] = (uint32_t)R;
-        t.pc.r2[i] = (uint32_t)(R * R % p);
-        t.pc.k32[i] = (uint32_t)((uint64_t)t.pc.r2[i]);                // 2^32 * R = R^2
-        t.pc.k64[i] = (uint32_t)((uint64_t)t.pc.r2[i] * R % p);        // 2^64 * R = R^3
-        t.pc.k96[i] = (uint32_t)((uint64_t)t.pc.k64[i] * R % p);       // 2^96 * R = R^4
-        t.pc.r1p[i] = t.pc.r1[i] * inv;
-        t.pc.k32p[i] = t.pc.k32[i] * inv;
-        t.pc.k64p[i] = t.pc.k64[i] * inv;
-        t.pc.k96p[i] = t.pc.k96[i] * inv;
-        // q mod p
-        unsigned __int128 q = (((unsigned __int128)1) << 112) - 75;
-        t.pc.qres[i] = (uint32_t)(q % p);
-
+        const uint32_t r2 = (uint32_t)(R * R % p);
         const uint32_t g = generator_of(p);
         const uint32_t psi = pow_mod(g, (p - 1) / (2ull * kMaxRing), p);
-        t.psi[i] = psi;
         const uint32_t psi_inv = inv_mod(psi, p);
         for (uint32_t k = 0; k < kMaxRing; ++k) {
-            uint32_t e = bitrev(k, kLogMaxRing);
+            const uint32_t e = bitrev(k, kLogMaxRing);
             t.zeta[(size_t)i * kMaxRing + k] = to_mont(pow_mod(psi, e, p), p);
             t.zinv[(size_t)i * kMaxRing + k] = to_mont(pow_mod(psi_inv, e, p), p);
-            t.zetap[(size_t)i * kMaxRing + k] = t.zeta[(size_t)i * kMaxRing + k] * t.pc.pinv[i];
-            t.zinvp[(size_t)i * kMaxRing + k] = t.zinv[(size_t)i * kMaxRing + k] * t.pc.pinv[i];
         }
-        const uint32_t inv4 = inv_mod(4, p);
         for (int L = 0; L <= kLogMaxRing; ++L) {
-            uint32_t ninv = inv_mod(pow_mod(2, L, p), p);
-            t.ninv_r2[i][L] = (uint32_t)((uint64_t)ninv * t.pc.r2[i] % p);
-            t.ninv4_r2[i][L] = (uint32_t)((uint64_t)ninv * inv4 % p * t.pc.r2[i] % p);
+            const uint32_t ninv = inv_mod(pow_mod(2, L, p), p);
+            t.pc.ninv_r2[i][L] = (uint32_t)((uint64_t)ninv * r2 % p);
         }
     }
-    // Garner constants.
-    for (int j = 0; j < kPrimes; ++j)
-        for (int i = 0; i < kPrimes; ++i)
-            t.cc.inv[j][i] = (j < i) ? to_mont(inv_mod(kCrtPrimes[j] % kCrtPrimes[i], kCrtPrimes[i]), kCrtPrimes[i]) : 0;
-    for (int j = 0; j < kPrimes; ++j)
-        for (int i = 0; i < kPrimes; ++i) t.cc.invp[j][i] = t.cc.inv[j][i] * t.pc.pinv[i];
-    U256 prod;
-    prod.w[0] = 1;
-    for (int i = 0; i < kPrimes; ++i) {
-        t.cc.radix_mod_q[i] = mod_q(prod);
-        mul_small(prod, kCrtPrimes[i]);
-    }
-    t.cc.p_mod_q = mod_q(prod);
-    // (P - 1) / 2 in mixed radix; P is odd so P - 1 only clears bit 0.
-    U256 half = prod;
-    half.w[0] -= 1;
-    for (int i = 0; i < 4; ++i) half.w[i] = (half.w[i] >> 1) | (i < 3 ? half.w[i + 1] << 63 : 0);
-    for (int i = 0; i < kPrimes; ++i) t.cc.half_digits[i] = (uint32_t)divmod_small(half, kCrtPrimes[i]);
     return t;
 }
 
@@ -149,6 +215,13 @@ const HostTables& host_tables() {
     static HostTables* tables = nullptr;
     static std::once_flag once;
     std::call_once(once, [] { tables = new HostTables(build()); });
+    return *tables;
+}
+
+const RefHostTables& ref_host_tables() {
+    static RefHostTables* tables = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] { tables = new RefHostTables(build_ref()); });
     return *tables;
 }
 

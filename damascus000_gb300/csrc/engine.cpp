@@ -41,7 +41,7 @@ int Context::create(int device, uint64_t hbm_budget, Context** out, std::string*
         *err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
         return kECuda;
     }
-    if ((e = upload_tables(&c->tables_)) != cudaSuccess || (e = upload_tables_ext(&c->tables_)) != cudaSuccess) {
+    if ((e = upload_tables(&c->tables_)) != cudaSuccess || (e = upload_ref_tables(&c->ref_tables_)) != cudaSuccess) {
         *err = std::string("table upload: ") + cudaGetErrorString(e);
         return kECuda;
     }
@@ -98,10 +98,8 @@ Context::~Context() {
 
     flush_timings();
     for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
-    if (tables_.zeta) cudaFree(const_cast<uint32_t*>(tables_.zeta));
-    if (tables_.zinv) cudaFree(const_cast<uint32_t*>(tables_.zinv));
-    if (tables_.zetap) cudaFree(const_cast<uint32_t*>(tables_.zetap));
-    if (tables_.zinvp) cudaFree(const_cast<uint32_t*>(tables_.zinvp));
+    free_tables(&tables_);
+    free_ref_tables(&ref_tables_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "dm_kernels.cuh"
+#include "dm_ref.cuh"
 #include "protocol.h"
 
 namespace dm {
@@ -46,6 +47,7 @@ class Context {
     int device() const { return device_; }
     cudaStream_t stream() const { return stream_; }
     const DeviceTables& tables() const { return tables_; }
+    const RefDeviceTables& ref_tables() const { return ref_tables_; }
 
     // HBM budget accounting (bytes reserved by live provers/verifiers/requests).
     bool reserve(uint64_t bytes);
@@ -71,6 +73,7 @@ class Context {
     int device_ = 0;
     cudaStream_t stream_ = nullptr;
     DeviceTables tables_{};
+    RefDeviceTables ref_tables_{};
     uint64_t budget_ = 0;
     std::atomic<uint64_t> reserved_{0};
     std::mutex mu_, err_mu_, prof_mu_;

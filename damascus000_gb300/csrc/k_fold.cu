@@ -1,6 +1,7 @@
-// Challenge-weighted folds of the witness and generator vectors and the
-// commitment updates, all in the coefficient domain mod q
-// (src/protocol/prover.rs:182-263, 332-457; src/protocol/verifier.rs:57-120).
+// Coefficient-domain kernels outside the prover's job lists: the verifier's
+// generator folds (src/protocol/verifier.rs:57-120, 141-178), canonicalisation of
+// caller-provided 128-bit words, and the reference FFI's split-word fold
+// (src/protocol/prover.rs:343-362 through src/utils/gpu.rs:69-93).
 #include <cuda_runtime.h>
 
 #include "dm_kernels.cuh"
@@ -23,25 +24,7 @@ unsigned grid_for(uint64_t n, unsigned bx = 256) {
 #define GRID_STRIDE(i, n) \
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (uint64_t)gridDim.x * blockDim.x)
 
-__global__ void fold_vec_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, uint64_t half, fq c) {
-    GRID_STRIDE(e, half) { st(dst, e, fq_fma(ld(src, e), c, ld(src, e + half))); }
-}
 
-__global__ void fold_poly_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, uint64_t total,
-                                 uint32_t L_out, fq c, int shift) {
-    const uint32_t h = 1u << L_out;
-    GRID_STRIDE(e, total) {
-        const uint64_t poly = e >> L_out;
-        const uint32_t j = (uint32_t)(e & (h - 1));
-        const uint64_t base = poly << (L_out + 1);
-        fq odd;
-        if (shift)
-            odd = j == 0 ? fq_neg(ld(src, base + 2 * h - 1)) : ld(src, base + 2 * j - 1);
-        else
-            odd = ld(src, base + 2 * j + 1);
-        st(dst, e, fq_fma(ld(src, base + 2 * j), c, odd));
-    }
-}
 
 // Generator folds of one verifier round: vector stage g' = g_L + x^-1 g_R, then the
 // poly stage g'' = g'_e + y^-1 X g'_o.  dst is [N'][8][n'] with N' = N/2 (or N) and
@@ -73,29 +56,8 @@ __global__ void fold_gen_round_kernel(const uint4* __restrict__ src, uint4* __re
     }
 }
 
-__global__ void combine_kernel(const uint4* __restrict__ c, const uint4* __restrict__ l, const uint4* __restrict__ r,
-                               fq a, fq b, uint4* __restrict__ out, uint64_t n) {
-    GRID_STRIDE(e, n) { st(out, e, fq_add(fq_fma(ld(c, e), a, ld(l, e)), fq_mul(b, ld(r, e)))); }
-}
 
-__global__ void combine_even_kernel(const uint4* __restrict__ ct, const uint4* __restrict__ lp,
-                                    const uint4* __restrict__ rp, fq a, fq b, uint4* __restrict__ out, uint32_t Lh) {
-    const uint64_t total = (uint64_t)kRank << Lh;
-    GRID_STRIDE(e, total) {
-        const uint64_t k = e >> Lh;
-        const uint32_t j = (uint32_t)(e & ((1u << Lh) - 1));
-        const fq even = ld(ct, (k << (Lh + 1)) + 2 * j);
-        st(out, e, fq_add(fq_fma(even, a, ld(lp, e)), fq_mul(b, ld(rp, e))));
-    }
-}
 
-__global__ void compare_kernel(const uint4* __restrict__ a, const uint4* __restrict__ b, uint64_t n,
-                               uint32_t* __restrict__ flag) {
-    GRID_STRIDE(e, n) {
-        const uint4 x = a[e], y = b[e];
-        if (x.x != y.x || x.y != y.y || x.z != y.z || x.w != y.w) atomicOr(flag, 1u);
-    }
-}
 
 // Reference FFI fold on split halves (cuda/fold_kernel.cu:189-206); inputs are
 // reduced mod q first so any 128-bit words are accepted.
@@ -136,19 +98,7 @@ cudaError_t launch_fold_split(const uint64_t* l_lo, const uint64_t* l_hi, const 
     return cudaGetLastError();
 }
 
-cudaError_t launch_fold_vec(const uint4* d_src, uint4* d_dst, uint64_t half, fq c, cudaStream_t s) {
-    if (!half) return cudaSuccess;
-    fold_vec_kernel<<<grid_for(half), 256, 0, s>>>(d_src, d_dst, half, c);
-    return cudaGetLastError();
-}
 
-cudaError_t launch_fold_poly(const uint4* d_src, uint4* d_dst, uint64_t npolys, uint32_t L_out, fq c, bool shift,
-                             cudaStream_t s) {
-    const uint64_t total = npolys << L_out;
-    if (!total) return cudaSuccess;
-    fold_poly_kernel<<<grid_for(total), 256, 0, s>>>(d_src, d_dst, total, L_out, c, shift ? 1 : 0);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_fold_gen_round(const uint4* d_src, uint4* d_dst, uint64_t N, uint32_t L, fq x_inv, fq y_inv,
                                   bool vec_stage, bool poly_stage, cudaStream_t s) {
@@ -159,23 +109,7 @@ cudaError_t launch_fold_gen_round(const uint4* d_src, uint4* d_dst, uint64_t N, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_combine(const uint4* d_c, const uint4* d_l, const uint4* d_r, fq a, fq b, uint4* d_out, uint64_t n,
-                           cudaStream_t s) {
-    if (!n) return cudaSuccess;
-    combine_kernel<<<grid_for(n), 256, 0, s>>>(d_c, d_l, d_r, a, b, d_out, n);
-    return cudaGetLastError();
-}
 
-cudaError_t launch_combine_even(const uint4* d_ct, const uint4* d_lp, const uint4* d_rp, fq a, fq b, uint4* d_out,
-                                uint32_t Lh, cudaStream_t s) {
-    combine_even_kernel<<<grid_for((uint64_t)kRank << Lh), 256, 0, s>>>(d_ct, d_lp, d_rp, a, b, d_out, Lh);
-    return cudaGetLastError();
-}
 
-cudaError_t launch_compare(const uint4* d_a, const uint4* d_b, uint64_t n, uint32_t* d_flag, cudaStream_t s) {
-    if (!n) return cudaSuccess;
-    compare_kernel<<<grid_for(n), 256, 0, s>>>(d_a, d_b, n, d_flag);
-    return cudaGetLastError();
-}
 
 }  // namespace dm

@@ -1,0 +1,588 @@
+// Ring arithmetic of the commitment and fold stages on the nine NTT primes:
+// forward negacyclic transforms, column multiply-accumulates in the NTT domain,
+// and the finish (sum of column partials, inverse transform, Garner CRT into
+// Z_q, optional compare).  The product of two rings in R_q is exact: every
+// commitment sum |X| < N n q^2 < P / 2 is recovered from its residues
+// (src/algebra/ntt.rs:112-224, 372-427 computes the same integers per product).
+//
+// Forward transform: Cooley-Tukey with the negacyclic twist merged into the
+// twiddles (zeta[k] = psi^brv(k), psi a primitive 2n-th root), natural order in,
+// bit-reversed evaluation order out: slot j holds a(psi^(2 brv(j) + 1)).  Slots
+// 2i and 2i+1 are the evaluations at +w_i and -w_i with w_i = zeta[n/2 + i], so
+// the even/odd halves of a polynomial are one butterfly layer away.  Inverse:
+// Gentleman-Sande with zeta^-1 and a final n^-1.
+//
+// Block shape of the transforms: rows of 2^L residues (one polynomial under one
+// prime), 2^(L-4) threads per row holding 16 residues each in registers, three
+// primes of a polynomial per block (three blocks per polynomial), and for small
+// rings several polynomials per block (192 threads for L <= 10).
+#include <cuda_runtime.h>
+
+#include "dm_jobkit.cuh"
+#include "dm_ntt.cuh"
+#include "dm_tables.h"
+
+namespace dm {
+
+namespace {
+
+using namespace jobkit;
+
+constexpr int kGroups = kPrimes / kPrimesPerBlock;  // blocks per polynomial group
+constexpr int kRows = kRank * kPrimes;              // MAC rows per job (coordinate, prime)
+
+template <int L>
+struct RowShape {
+    static constexpr int T = 1 << (L - 4);                   // threads per row
+    static constexpr int P = T >= 64 ? 1 : 64 / T;            // polynomials per block
+    static constexpr int ROWS = P * kPrimesPerBlock;          // rows per block
+    static constexpr int THREADS = ROWS * T;
+    static constexpr int PASSES = (L + 3) / 4;
+    static constexpr size_t SMEM = PASSES > 1 ? (size_t)ROWS * (1u << L) * sizeof(uint32_t) : 0;
+};
+
+// ================================================================ forward NTT
+
+template <int L>
+__global__ void __launch_bounds__(RowShape<L>::THREADS)
+    ntt_fwd_kernel(JobList<NttJob> J, PrimeConsts pc, const uint32_t* __restrict__ zeta,
+                   const uint32_t* __restrict__ zetas) {
+    using S = RowShape<L>;
+    extern __shared__ __align__(16) uint32_t sm[];
+    const NttJob jb = J.j[find_job(J)];
+    const uint32_t lcta = blockIdx.x - jb.cta0;
+    const uint32_t grp = lcta / kGroups, third = lcta % kGroups;
+    const uint32_t row = threadIdx.x / S::T;
+    const uint32_t t = threadIdx.x % S::T;
+    const uint64_t poly = (uint64_t)grp * S::P + row / kPrimesPerBlock;
+    const uint32_t pi = third * kPrimesPerBlock + row % kPrimesPerBlock;
+    const bool active = poly < jb.npolys;
+    const uint32_t p = pc.p[pi];
+    const uint32_t* zt = zeta + pi * kMaxRing;
+    const uint32_t* zs = zetas + pi * kMaxRing;
+    uint32_t a[kNttE];
+    if (active) {
+        const uint4* src = jb.src + (poly << L);
+#pragma unroll
+        for (int r = 0; r < kNttE; ++r) a[r] = residue_lazy(ldq(src, ntt_place(L, 0, t, r)), pc, pi);
+    } else {
+#pragma unroll
+        for (int r = 0; r < kNttE; ++r) a[r] = 0;
+    }
+    const uint32_t base = row << L;
+#pragma unroll
+    for (int pass = 0; pass < S::PASSES; ++pass) {
+        ntt_fwd_pass(a, L, pass, t, zt, zs, p);
+        if (pass + 1 < S::PASSES) {
+#pragma unroll
+            for (int r = 0; r < kNttE; ++r) sm[ntt_swz(base + ntt_place(L, pass, t, r))] = a[r];
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kNttE; ++r) a[r] = sm[ntt_swz(base + ntt_place(L, pass + 1, t, r))];
+            __syncthreads();
+        }
+    }
+    if (active) {
+        const uint32_t p2 = 2 * p;
+#pragma unroll
+        for (int r = 0; r < kNttE; ++r) a[r] = red_below(red_below(a[r], p2), p);
+        // the last pass holds slots 16 t .. 16 t + 15
+        uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * kNttE);
+        dst[0] = make_uint4(a[0], a[1], a[2], a[3]);
+        dst[1] = make_uint4(a[4], a[5], a[6], a[7]);
+        dst[2] = make_uint4(a[8], a[9], a[10], a[11]);
+        dst[3] = make_uint4(a[12], a[13], a[14], a[15]);
+    }
+}
+
+// Rings smaller than 16: one thread per (polynomial, prime), all in registers.
+template <int L>
+__global__ void __launch_bounds__(128) ntt_fwd_small_kernel(JobList<NttJob> J, PrimeConsts pc,
+                                                            const uint32_t* __restrict__ zeta,
+                                                            const uint32_t* __restrict__ zetas) {
+    constexpr int s = 1 << L;
+    const NttJob jb = J.j[find_job(J)];
+    const uint64_t item = (uint64_t)(blockIdx.x - jb.cta0) * blockDim.x + threadIdx.x;
+    const uint64_t poly = item / kPrimes;
+    const uint32_t pi = (uint32_t)(item % kPrimes);
+    if (poly >= jb.npolys) return;
+    const uint32_t p = pc.p[pi];
+    uint32_t a[s];
+#pragma unroll
+    for (int c = 0; c < s; ++c) a[c] = residue_lazy(ldq(jb.src + (poly << L), c), pc, pi);
+    ntt_fwd_small<L>(a, zeta + pi * kMaxRing, zetas + pi * kMaxRing, p);
+#pragma unroll
+    for (int c = 0; c < s; ++c) jb.dst[((poly * kPrimes + pi) << L) + c] = red_below(red_below(a[c], 2 * p), p);
+}
+
+// ================================================================ MAC
+// Residues are < p < 2^30, so a product fits 60 bits and 16 of them fit a
+// 64-bit word; block sums go into a 96-bit accumulator (64-bit low word + carry
+// count) reduced once per output.
+constexpr int kMacThreads = 128;
+
+DM_D uint32_t slot_block_count(uint32_t s) { return (s + kMacThreads - 1) / kMacThreads; }
+DM_D void acc96(uint64_t& lo, uint32_t& hi, uint64_t v) {
+    lo += v;
+    hi += lo < v ? 1u : 0u;
+}
+DM_D uint64_t mul64(uint32_t a, uint32_t b) { return (uint64_t)a * b; }
+
+// grid: per job, nblk * 72 * parts blocks; block -> (part, row, slot block).
+__global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+    const MacJobX jb = J.j[find_job(J)];
+    const uint32_t s = 1u << L;
+    const uint32_t nblk = slot_block_count(s);
+    uint32_t c = blockIdx.x - jb.cta0;
+    const uint32_t blk = c % nblk;
+    c /= nblk;
+    const uint32_t kp = c % kRows;
+    const uint32_t part = c / kRows;
+    const uint32_t slot = blk * kMacThreads + threadIdx.x;
+    if (slot >= s) return;
+    const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
+    const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
+    const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
+    const uint64_t gstride = (uint64_t)kRank * kPrimes << L;  // one generator vector
+    const uint64_t mstride = (uint64_t)kPrimes << L;
+    const uint32_t* g = jb.G + ((((uint64_t)jb.g_base * kRank + k) * kPrimes + pi) << L) + slot;
+    const uint32_t* m = jb.M + (((uint64_t)jb.m_base * kPrimes + pi) << L) + slot;
+    uint64_t lo = 0;
+    uint32_t hi = 0;
+    uint32_t i = i0;
+    for (; i + 8 <= i1; i += 8) {
+        uint64_t b0 = 0, b1 = 0;
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+            b0 += mul64(__ldg(g + (i + u) * gstride), __ldg(m + (i + u) * mstride));
+            b1 += mul64(__ldg(g + (i + u + 1) * gstride), __ldg(m + (i + u + 1) * mstride));
+        }
+        acc96(lo, hi, b0);
+        acc96(lo, hi, b1);
+    }
+    uint64_t b = 0;
+    for (; i < i1; ++i) b += mul64(__ldg(g + i * gstride), __ldg(m + i * mstride));
+    acc96(lo, hi, b);
+    jb.out0[(((uint64_t)part * kRows + kp) << L) + slot] = red96(hi, lo, pc, pi);
+}
+
+// Triple MAC over h = count column pairs (i, i + h): one read of every generator
+// column gives the full sum (out0), L = sum G[i+h] M[i] (out1) and
+// R = sum G[i] M[i+h] (out2).
+__global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+    const MacJobX jb = J.j[find_job(J)];
+    const uint32_t s = 1u << L;
+    const uint32_t nblk = slot_block_count(s);
+    uint32_t c = blockIdx.x - jb.cta0;
+    const uint32_t blk = c % nblk;
+    c /= nblk;
+    const uint32_t kp = c % kRows;
+    const uint32_t part = c / kRows;
+    const uint32_t slot = blk * kMacThreads + threadIdx.x;
+    if (slot >= s) return;
+    const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
+    const uint32_t h = jb.count;
+    const uint32_t i0 = (uint32_t)((uint64_t)h * part / jb.parts);
+    const uint32_t i1 = (uint32_t)((uint64_t)h * (part + 1) / jb.parts);
+    const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
+    const uint64_t mstride = (uint64_t)kPrimes << L;
+    const uint32_t* g = jb.G + ((((uint64_t)k) * kPrimes + pi) << L) + slot;
+    const uint32_t* m = jb.M + (((uint64_t)pi) << L) + slot;
+    const uint64_t gh = (uint64_t)h * gstride, mh = (uint64_t)h * mstride;
+    uint64_t cl = 0, ll = 0, rl = 0;
+    uint32_t ch = 0, lh = 0, rh = 0;
+    uint32_t i = i0;
+    while (i < i1) {
+        const uint32_t e = i + 8 < i1 ? i + 8 : i1;  // <= 16 products per block sum
+        uint64_t bc = 0, bl = 0, br = 0;
+        for (; i < e; ++i) {
+            const uint32_t gl = __ldg(g + i * gstride), gr = __ldg(g + i * gstride + gh);
+            const uint32_t ml = __ldg(m + i * mstride), mr = __ldg(m + i * mstride + mh);
+            bc += mul64(gl, ml) + mul64(gr, mr);
+            bl += mul64(gr, ml);
+            br += mul64(gl, mr);
+        }
+        acc96(cl, ch, bc);
+        acc96(ll, lh, bl);
+        acc96(rl, rh, br);
+    }
+    const uint64_t o = (((uint64_t)part * kRows + kp) << L) + slot;
+    jb.out0[o] = red96(ch, cl, pc, pi);
+    jb.out1[o] = red96(lh, ll, pc, pi);
+    jb.out2[o] = red96(rh, rl, pc, pi);
+}
+
+// Split MAC: thread per slot pair (2 i2, 2 i2 + 1) of ring 2^L (L >= 1): the
+// recompute check over all slots and the even/odd cross terms
+// (g(w) - g(-w)) (m(w) + m(-w)) and (g(w) + g(-w)) (m(w) - m(-w)) at 2^(L-1).
+__global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+    const MacJobX jb = J.j[find_job(J)];
+    const uint32_t hs = 1u << (L - 1);
+    const uint32_t nblk = slot_block_count(hs);
+    uint32_t c = blockIdx.x - jb.cta0;
+    const uint32_t blk = c % nblk;
+    c /= nblk;
+    const uint32_t kp = c % kRows;
+    const uint32_t part = c / kRows;
+    const uint32_t i2 = blk * kMacThreads + threadIdx.x;
+    if (i2 >= hs) return;
+    const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
+    const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
+    const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
+    const uint32_t p = pc.p[pi];
+    const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
+    const uint64_t mstride = (uint64_t)kPrimes << L;
+    const uint32_t* g = jb.G + ((((uint64_t)jb.g_base * kRank + k) * kPrimes + pi) << L) + 2 * i2;
+    const uint32_t* m = jb.M + (((uint64_t)jb.m_base * kPrimes + pi) << L) + 2 * i2;
+    uint64_t l0 = 0, l1 = 0, ll = 0, lr = 0;
+    uint32_t h0 = 0, h1 = 0, hl = 0, hr = 0;
+    uint32_t i = i0;
+    while (i < i1) {
+        const uint32_t e = i + 16 < i1 ? i + 16 : i1;
+        uint64_t b0 = 0, b1 = 0, bl = 0, br = 0;
+        for (; i < e; ++i) {
+            const uint2 gv = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
+            const uint2 mv = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
+            b0 += mul64(gv.x, mv.x);
+            b1 += mul64(gv.y, mv.y);
+            bl += mul64(red_below(gv.x + p - gv.y, p), red_below(mv.x + mv.y, p));
+            br += mul64(red_below(gv.x + gv.y, p), red_below(mv.x + p - mv.y, p));
+        }
+        acc96(l0, h0, b0);
+        acc96(l1, h1, b1);
+        acc96(ll, hl, bl);
+        acc96(lr, hr, br);
+    }
+    *reinterpret_cast<uint2*>(jb.out0 + (((uint64_t)part * kRows + kp) << L) + 2 * i2) =
+        make_uint2(red96(h0, l0, pc, pi), red96(h1, l1, pc, pi));
+    jb.out1[(((uint64_t)part * kRows + kp) << (L - 1)) + i2] = red96(hl, ll, pc, pi);
+    jb.out2[(((uint64_t)part * kRows + kp) << (L - 1)) + i2] = red96(hr, lr, pc, pi);
+}
+
+// ================================================================ finish
+struct FinishConsts {
+    uint32_t f[kPrimes], fs[kPrimes];  // final inverse-transform scale and its Shoup constant
+};
+
+DM_D uint32_t twist(uint32_t x, uint32_t mode, uint32_t idx, const uint32_t* zeta, const uint32_t* zetas,
+                    const uint32_t* zinv, const uint32_t* zinvs, uint32_t p) {
+    if (mode == kFinishSplitL) return shoup_mul(x, zeta[idx], zetas[idx], p);
+    if (mode == kFinishSplitR) return shoup_mul(x, zinv[idx], zinvs[idx], p);
+    return x;
+}
+
+// Block -> ROWS consecutive rows of one job.  Sums the column partials of each
+// row, applies the split twist (w_i or w_i^-1; the 1/4 is in the final scale),
+// inverse-transforms, scales, and writes the residues over the row's part-0
+// partials.
+template <int L>
+__global__ void __launch_bounds__(RowShape<L>::THREADS)
+    inv_rows_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
+                    const uint32_t* __restrict__ zeta, const uint32_t* __restrict__ zetas,
+                    const uint32_t* __restrict__ zinv, const uint32_t* __restrict__ zinvs) {
+    using S = RowShape<L>;
+    constexpr uint32_t s = 1u << L;
+    extern __shared__ __align__(16) uint32_t sm[];
+    const FinishJobX jb = J.j[find_job(J)];
+    const uint32_t brow = threadIdx.x / S::T;
+    const uint32_t t = threadIdx.x % S::T;
+    const uint32_t row = (blockIdx.x - jb.cta0) * S::ROWS + brow;
+    const bool active = row < jb.rows;
+    const uint32_t pi = active ? row % kPrimes : 0;
+    const uint32_t p = pc.p[pi];
+    uint32_t a[kNttE];
+#pragma unroll
+    for (int r = 0; r < kNttE; ++r) a[r] = 0;
+    if (active) {
+        for (uint32_t part = 0; part < jb.parts; ++part) {
+            const uint4* src =
+                reinterpret_cast<const uint4*>(jb.partials + (((uint64_t)part * jb.rows + row) << L) + t * kNttE);
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) {
+                const uint4 v = src[q4];
+                a[4 * q4] = red_below(a[4 * q4] + v.x, p);
+                a[4 * q4 + 1] = red_below(a[4 * q4 + 1] + v.y, p);
+                a[4 * q4 + 2] = red_below(a[4 * q4 + 2] + v.z, p);
+                a[4 * q4 + 3] = red_below(a[4 * q4 + 3] + v.w, p);
+            }
+        }
+        if (jb.mode != kFinishPlain) {
+#pragma unroll
+            for (int r = 0; r < kNttE; ++r)
+                a[r] = twist(a[r], jb.mode, pi * kMaxRing + s + t * kNttE + r, zeta, zetas, zinv, zinvs, p);
+        }
+    }
+    const uint32_t* zi = zinv + pi * kMaxRing;
+    const uint32_t* zis = zinvs + pi * kMaxRing;
+    const uint32_t base = brow << L;
+#pragma unroll
+    for (int pass = S::PASSES - 1; pass >= 0; --pass) {
+        ntt_inv_pass(a, L, pass, t, zi, zis, p);
+        if (pass > 0) {
+#pragma unroll
+            for (int r = 0; r < kNttE; ++r) sm[ntt_swz(base + ntt_place(L, pass, t, r))] = a[r];
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kNttE; ++r) a[r] = sm[ntt_swz(base + ntt_place(L, pass - 1, t, r))];
+            __syncthreads();
+        }
+    }
+    if (active) {
+        const FinishConsts& fc = (jb.mode == kFinishPlain) ? plain : split;
+        const uint32_t f = fc.f[pi], fs = fc.fs[pi];
+        uint32_t* dst = jb.partials + ((uint64_t)row << L);
+#pragma unroll
+        for (int r = 0; r < kNttE; ++r) dst[ntt_place(L, 0, t, r)] = red_below(shoup_mul(a[r], f, fs, p), p);
+    }
+}
+
+// Rings below 16 coefficients: one thread per row.
+template <int L>
+__global__ void __launch_bounds__(128)
+    inv_rows_small_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
+                          const uint32_t* __restrict__ zeta, const uint32_t* __restrict__ zetas,
+                          const uint32_t* __restrict__ zinv, const uint32_t* __restrict__ zinvs) {
+    constexpr uint32_t s = 1u << L;
+    const FinishJobX jb = J.j[find_job(J)];
+    const uint32_t row = (blockIdx.x - jb.cta0) * blockDim.x + threadIdx.x;
+    if (row >= jb.rows) return;
+    const uint32_t pi = row % kPrimes;
+    const uint32_t p = pc.p[pi];
+    uint32_t a[s];
+#pragma unroll
+    for (uint32_t c = 0; c < s; ++c) {
+        uint32_t acc = 0;
+        for (uint32_t part = 0; part < jb.parts; ++part)
+            acc = red_below(acc + jb.partials[(((uint64_t)part * jb.rows + row) << L) + c], p);
+        a[c] = twist(acc, jb.mode, pi * kMaxRing + s + c, zeta, zetas, zinv, zinvs, p);
+    }
+    ntt_inv_small<L>(a, zinv + pi * kMaxRing, zinvs + pi * kMaxRing, p);
+    const FinishConsts& fc = (jb.mode == kFinishPlain) ? plain : split;
+#pragma unroll
+    for (uint32_t c = 0; c < s; ++c)
+        jb.partials[((uint64_t)row << L) + c] = red_below(shoup_mul(a[c], fc.f[pi], fc.fs[pi], p), p);
+}
+
+// Thread per output coefficient: the nine residues of (poly, slot) -> Z_q.
+constexpr int kCrtThreads = 256;
+__global__ void __launch_bounds__(kCrtThreads) crt_jobs_kernel(JobList<FinishJobX> J, uint32_t L, PrimeConsts pc,
+                                                               CrtConsts cc) {
+    const FinishJobX jb = J.j[find_job(J)];
+    const uint64_t e = (uint64_t)(blockIdx.x - jb.cta0) * kCrtThreads + threadIdx.x;
+    const uint64_t npolys = jb.rows / kPrimes;
+    if (e >= (npolys << L)) return;
+    const uint64_t poly = e >> L;
+    const uint32_t slot = (uint32_t)(e & ((1u << L) - 1));
+    uint32_t r[kPrimes];
+#pragma unroll
+    for (int i = 0; i < kPrimes; ++i) r[i] = jb.partials[((poly * kPrimes + i) << L) + slot];
+    const fq v = crt_to_fq(r, pc, cc);
+    stq(jb.out, e, v);
+    if (jb.expect) {
+        const uint4 x = jb.expect[e];
+        if (x.x != v.w[0] || x.y != v.w[1] || x.z != v.w[2] || x.w != v.w[3]) atomicOr(jb.flag, 1u);
+    }
+}
+
+// ================================================================ pointwise
+constexpr int kPointThreads = 256;
+__global__ void __launch_bounds__(kPointThreads) pointwise_jobs_kernel(JobList<PointwiseJob> J, uint32_t L,
+                                                                       PrimeConsts pc) {
+    const PointwiseJob jb = J.j[find_job(J)];
+    const uint64_t e = (uint64_t)(blockIdx.x - jb.cta0) * kPointThreads + threadIdx.x;
+    if (e >= (jb.npolys * kPrimes) << L) return;
+    const uint32_t pi = (uint32_t)((e >> L) % kPrimes);
+    jb.out[e] = red64(mul64(jb.a[e], jb.b[e]), pc, pi);
+}
+
+// ---------------------------------------------------------------- launch helpers
+template <int L>
+cudaError_t ntt_launch_L(const DeviceTables& T, JobList<NttJob>& JL, NttJob* jobs, int n, cudaStream_t st) {
+    if constexpr (L < 4) {
+        const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
+            return ((uint64_t)j.npolys * kPrimes + 127) / 128;
+        });
+        if (!ctas) return cudaSuccess;
+        ntt_fwd_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, T.zeta, T.zetas);
+    } else {
+        using S = RowShape<L>;
+        const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
+            return ((uint64_t)(j.npolys + S::P - 1) / S::P) * kGroups;
+        });
+        if (!ctas) return cudaSuccess;
+        ntt_fwd_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.zeta, T.zetas);
+    }
+    return cudaGetLastError();
+}
+
+template <int L>
+cudaError_t inv_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJobX* jobs, int n,
+                         const FinishConsts& plain, const FinishConsts& split, cudaStream_t st) {
+    if constexpr (L < 4) {
+        const uint32_t ctas = assign_ctas<FinishJobX>(jobs, n, JL, [](const FinishJobX& j) -> uint64_t {
+            return ((uint64_t)j.rows + 127) / 128;
+        });
+        if (!ctas) return cudaSuccess;
+        inv_rows_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, plain, split, T.zeta, T.zetas, T.zinv, T.zinvs);
+    } else {
+        using S = RowShape<L>;
+        const uint32_t ctas = assign_ctas<FinishJobX>(jobs, n, JL, [](const FinishJobX& j) -> uint64_t {
+            return ((uint64_t)j.rows + S::ROWS - 1) / S::ROWS;
+        });
+        if (!ctas) return cudaSuccess;
+        inv_rows_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, plain, split, T.zeta, T.zetas, T.zinv,
+                                                             T.zinvs);
+    }
+    return cudaGetLastError();
+}
+
+#define DM_DISPATCH_L(L, CALL)                                                                                 \
+    switch (L) {                                                                                               \
+        case 0: return CALL(0);                                                                                \
+        case 1: return CALL(1);                                                                                \
+        case 2: return CALL(2);                                                                                \
+        case 3: return CALL(3);                                                                                \
+        case 4: return CALL(4);                                                                                \
+        case 5: return CALL(5);                                                                                \
+        case 6: return CALL(6);                                                                                \
+        case 7: return CALL(7);                                                                                \
+        case 8: return CALL(8);                                                                                \
+        case 9: return CALL(9);                                                                                \
+        case 10: return CALL(10);                                                                              \
+        case 11: return CALL(11);                                                                              \
+        case 12: return CALL(12);                                                                              \
+    }
+
+}  // namespace
+
+cudaError_t upload_tables(DeviceTables* out) {
+    const HostTables& H = host_tables();
+    out->pc = H.pc;
+    out->cc = H.cc;
+    const size_t bytes = sizeof(uint32_t) * H.zeta.size();
+    const std::vector<uint32_t>* src[4] = {&H.zeta, &H.zetas, &H.zinv, &H.zinvs};
+    uint32_t* dst[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
+        e = cudaMalloc(&dst[i], bytes);
+        if (e == cudaSuccess) e = cudaMemcpy(dst[i], src[i]->data(), bytes, cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        for (uint32_t* d : dst)
+            if (d) cudaFree(d);
+        return e;
+    }
+    out->zeta = dst[0];
+    out->zetas = dst[1];
+    out->zinv = dst[2];
+    out->zinvs = dst[3];
+    return cudaSuccess;
+}
+
+void free_tables(DeviceTables* t) {
+    for (const uint32_t* d : {t->zeta, t->zetas, t->zinv, t->zinvs})
+        if (d) cudaFree(const_cast<uint32_t*>(d));
+    t->zeta = t->zetas = t->zinv = t->zinvs = nullptr;
+}
+
+cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
+    JobList<NttJob> JL;
+#define DM_NTT_CALL(l) ntt_launch_L<l>(T, JL, jobs, n, st)
+    DM_DISPATCH_L(L, DM_NTT_CALL)
+#undef DM_NTT_CALL
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxJobs) return cudaErrorInvalidValue;
+    JobList<MacJobX> JL;
+    const uint32_t slots = 1u << L;
+    uint64_t total = 0;
+    JL.n = n;
+    for (int i = 0; i < n; ++i) {
+        jobs[i].cta0 = (uint32_t)total;
+        JL.j[i] = jobs[i];
+        total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
+    }
+    const unsigned bx = slots < (uint32_t)kMacThreads ? slots : kMacThreads;
+    mac_triple_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxJobs || (split && L == 0)) return cudaErrorInvalidValue;
+    JobList<MacJobX> JL;
+    const uint32_t slots = split ? (1u << (L - 1)) : (1u << L);
+    uint64_t total = 0;
+    JL.n = n;
+    for (int i = 0; i < n; ++i) {
+        jobs[i].cta0 = (uint32_t)total;
+        JL.j[i] = jobs[i];
+        total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
+    }
+    const unsigned bx = slots < (uint32_t)kMacThreads ? slots : kMacThreads;
+    if (split)
+        mac_split_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+    else
+        mac_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
+    const HostTables& H = host_tables();
+    FinishConsts plain, split;
+    for (int i = 0; i < kPrimes; ++i) {
+        plain.f[i] = H.ninv[i][L];
+        plain.fs[i] = H.ninvs[i][L];
+        split.f[i] = H.ninv4[i][L];
+        split.fs[i] = H.ninv4s[i][L];
+    }
+    cudaError_t e = cudaErrorInvalidValue;
+    {
+        JobList<FinishJobX> JL;
+#define DM_INV_CALL(l) inv_launch_L<l>(T, JL, jobs, n, plain, split, st)
+        auto inv = [&]() -> cudaError_t {
+            DM_DISPATCH_L(L, DM_INV_CALL)
+            return cudaErrorInvalidValue;
+        };
+#undef DM_INV_CALL
+        e = inv();
+    }
+    if (e != cudaSuccess) return e;
+    JobList<FinishJobX> JC;
+    const uint32_t Lc = L;
+    uint64_t total = 0;
+    JC.n = n;
+    for (int i = 0; i < n; ++i) {
+        JC.j[i] = jobs[i];
+        JC.j[i].cta0 = (uint32_t)total;
+        total += ((((uint64_t)jobs[i].rows / kPrimes) << Lc) + kCrtThreads - 1) / kCrtThreads;
+    }
+    if (!total) return cudaSuccess;
+    crt_jobs_kernel<<<(unsigned)total, kCrtThreads, 0, st>>>(JC, L, T.pc, T.cc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pointwise_jobs(const DeviceTables& T, PointwiseJob* jobs, int n, uint32_t L, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxJobs) return cudaErrorInvalidValue;
+    JobList<PointwiseJob> JL;
+    uint64_t total = 0;
+    JL.n = n;
+    for (int i = 0; i < n; ++i) {
+        jobs[i].cta0 = (uint32_t)total;
+        JL.j[i] = jobs[i];
+        total += (((jobs[i].npolys * kPrimes) << L) + kPointThreads - 1) / kPointThreads;
+    }
+    if (!total) return cudaSuccess;
+    pointwise_jobs_kernel<<<(unsigned)total, kPointThreads, 0, st>>>(JL, L, T.pc);
+    return cudaGetLastError();
+}
+
+}  // namespace dm

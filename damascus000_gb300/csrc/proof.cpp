@@ -13,8 +13,10 @@ enum Slot { kC = 0, kL = 1, kR = 2, kCt = 3, kV = 4, kLp = 5, kRp = 6, kChk = 7,
 constexpr uint32_t kMaxParts = 16;
 constexpr size_t kTail = 128;  // pinned tail: [0,32) file id, [32,40) flags, [48,64) m*
 
+constexpr uint32_t kRows = kRank * kPrimes;  // MAC rows per job: (coordinate, prime)
+
 uint32_t mac_parts(uint32_t slots, int njobs, uint32_t count) {
-    const uint32_t ctas = ((slots + 127) / 128) * 64u * (uint32_t)njobs;
+    const uint32_t ctas = ((slots + 127) / 128) * kRows * (uint32_t)njobs;
     uint32_t parts = (1216u + ctas - 1) / ctas;
     if (parts > kMaxParts) parts = kMaxParts;
     if (parts > count) parts = count ? count : 1;
@@ -126,8 +128,8 @@ int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
         if (ntt[L].empty()) continue;
         double polys = 0;
         for (auto& j : ntt[L]) polys += j.npolys;
-        const double bytes = polys * (double)(1u << L) * 48;             // 16 B read + 32 B written per coefficient
-        const double ops = polys * 8.0 * (double)(1u << L) / 2 * L;      // butterflies
+        const double bytes = polys * (double)(1u << L) * (16 + 4 * kPrimes);  // 16 B read + 9 residues written
+        const double ops = polys * (double)kPrimes * (double)(1u << L) / 2 * L;  // butterflies
         if ((rc = timed("ntt_fwd", bytes, ops, [&] {
                  for (size_t i = 0; i < ntt[L].size(); i += kMaxJobs) {
                      const int n = (int)std::min<size_t>(kMaxJobs, ntt[L].size() - i);
@@ -149,9 +151,9 @@ int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
             double macs = 0, bytes = 0;
             for (auto& j : v) {
                 const double cols = (double)j.count * cols_per_count;
-                macs += cols * 64.0 * (double)(1u << L) * macs_per_col;
+                macs += cols * (double)kRows * (double)(1u << L) * macs_per_col;
                 // G residues (4 B per column, coordinate, prime, slot) + M residues (shared by 8 coordinates)
-                bytes += cols * (double)(1u << L) * (64.0 * 4 + 8.0 * 4);
+                bytes += cols * (double)(1u << L) * (kRows * 4.0 + kPrimes * 4.0);
             }
             const char* name = pass == 0 ? "mac" : (pass == 1 ? "mac_split" : "mac");
             if ((rc = timed(name, bytes, macs, [&] {
@@ -170,13 +172,13 @@ int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
     for (int L = kLogMaxProverRing; L >= 0; --L) {
         if (finish[L].empty()) continue;
         double bytes = 0;
-        for (auto& j : finish[L]) bytes += (double)j.parts * 64 * (1u << L) * 4 + 8.0 * (1u << L) * 16;
+        for (auto& j : finish[L]) bytes += ((double)j.parts + 2.0) * j.rows * (1u << L) * 4 + (j.rows / kPrimes) * (1u << L) * 16.0;
         if ((rc = timed("finish", bytes, 0, [&] {
                  for (size_t i = 0; i < finish[L].size(); i += kMaxJobs) {
                      const int n = (int)std::min<size_t>(kMaxJobs, finish[L].size() - i);
                      cudaError_t e = launch_finish_jobs(T, finish[L].data() + i, n, (uint32_t)L, st);
                      if (e != cudaSuccess) return (int)e;
-                     ++launches;
+                     launches += 2;  // inverse transform + CRT
                  }
                  return 0;
              })))
@@ -201,7 +203,7 @@ uint64_t ProofState::footprint(uint64_t len) {
     const uint64_t S2 = S * S;
     auto r = [](uint64_t b) { return (b + 255) & ~255ull; };
     return r(len + 16) + r(file_hash_scratch_words(len) * 4) + r(S2 * 16) + r(S2 / 2 * 16) + r(8 * S2 * 16) +
-           r(4 * S2 * 16) + r(S2 * 32) + r(8 * S2 * 32) + r(3ull * kMaxParts * 64 * S * 4) +
+           r(4 * S2 * 16) + r(S2 * kPrimes * 4) + r(8 * S2 * kPrimes * 4) + r(3ull * kMaxParts * kRows * S * 4) +
            r((uint64_t)kSlots * kRank * S * 16) + r(64);
 }
 
@@ -264,9 +266,9 @@ int ProofState::setup(const uint8_t* file, uint64_t len, bool on_device, const u
     need(m_b_, S2 / 2 * 16);
     need(g_a_, 8 * S2 * 16);
     need(g_b_, 4 * S2 * 16);
-    need(mhat_, S2 * 32);
-    need(ghat_, 8 * S2 * 32);
-    need(partials_, 3ull * kMaxParts * 64 * S * 4);
+    need(mhat_, S2 * kPrimes * 4);
+    need(ghat_, 8 * S2 * kPrimes * 4);
+    need(partials_, 3ull * kMaxParts * kRows * S * 4);
     need(comm_, (uint64_t)kSlots * kRank * S * 16);
     need(misc_, 64);
     if (rc != kOk) return fail(rc, "HBM budget exhausted allocating prover state (" + std::to_string(footprint(len)) + " bytes)");
@@ -313,16 +315,16 @@ void ProofState::plan_stage(Plan& P) {
         P.ntt[L].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * S, 0});
         const int nj = S >= 2 ? 3 : 1;
         parts_ = mac_parts(S, 1, S / 2 ? S / 2 : 1);
-        const size_t pstride = (size_t)parts_ * 64 * S;
+        const size_t pstride = (size_t)parts_ * kRows * S;
         if (nj == 3) {
             P.triple[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
                                           part + 2 * pstride, 0, 0, S / 2, parts_, 0});
-            P.finish[L].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain});
-            P.finish[L].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain});
+            P.finish[L].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
+            P.finish[L].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
         } else {
             P.mac[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, S, parts_, 0});
         }
-        P.finish[L].push_back(FinishJobX{part, cs(kC), nullptr, nullptr, parts_, kFinishPlain});
+        P.finish[L].push_back(FinishJobX{part, cs(kC), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
         P.d2h.push_back(Copy{tail, misc_.as<uint8_t>(), 32});
         P.d2h.push_back(Copy{pinned_, cs(kC), slot * 16});
         if (nj == 3) {
@@ -343,12 +345,12 @@ void ProofState::plan_stage(Plan& P) {
         P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
         parts_ = mac_parts(h, 1, h);
         uint32_t* pchk = part;
-        uint32_t* plp = part + (size_t)parts_ * 64 * s;
-        uint32_t* prp = plp + (size_t)parts_ * 64 * h;
+        uint32_t* plp = part + (size_t)parts_ * kRows * s;
+        uint32_t* prp = plp + (size_t)parts_ * kRows * h;
         P.split[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, h, parts_, 0});
-        P.finish[L].push_back(FinishJobX{pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain});
-        P.finish[L - 1].push_back(FinishJobX{plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL});
-        P.finish[L - 1].push_back(FinishJobX{prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR});
+        P.finish[L].push_back(FinishJobX{pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain, kRows, 0});
+        P.finish[L - 1].push_back(FinishJobX{plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL, kRows, 0});
+        P.finish[L - 1].push_back(FinishJobX{prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR, kRows, 0});
         P.d2h.push_back(Copy{pinned_, cs(kCt), (size_t)kRank * s * 16});
         P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kLp), (size_t)kRank * h * 16});
         P.d2h.push_back(Copy{pinned_ + 2 * slot * 16, cs(kRp), (size_t)kRank * h * 16});
@@ -366,16 +368,16 @@ void ProofState::plan_stage(Plan& P) {
         P.ntt[Ln].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
         const int nj = h >= 2 ? 3 : 1;
         parts_ = mac_parts(h, 1, h / 2 ? h / 2 : 1);
-        const size_t pstride = (size_t)parts_ * 64 * h;
+        const size_t pstride = (size_t)parts_ * kRows * h;
         if (nj == 3) {
             P.triple[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
                                            part + 2 * pstride, 0, 0, h / 2, parts_, 0});
-            P.finish[Ln].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain});
-            P.finish[Ln].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain});
+            P.finish[Ln].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
+            P.finish[Ln].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
         } else {
             P.mac[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, h, parts_, 0});
         }
-        P.finish[Ln].push_back(FinishJobX{part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain});
+        P.finish[Ln].push_back(FinishJobX{part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain, kRows, 0});
         P.d2h.push_back(Copy{pinned_, cs(kC), (size_t)kRank * h * 16});
         if (nj == 3) {
             P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kL), (size_t)kRank * h * 16});
