@@ -197,6 +197,12 @@ DM_HD uint32_t shoup_mul(uint32_t x, uint32_t w, uint32_t ws, uint32_t p) {
     return x * w - q * p;
 }
 
+// A twiddle (or any constant factor) with its Shoup constant, loaded as one 8-byte word.
+struct alignas(8) Tw {
+    uint32_t w, s;
+};
+DM_HD uint32_t shoup_mul(uint32_t x, Tw t, uint32_t p) { return shoup_mul(x, t.w, t.s, p); }
+
 // Generic reductions (any p < 2^32) used by the reference-prime FFI path too.
 DM_HD uint32_t add_mod(uint32_t a, uint32_t b, uint32_t p) {
     uint32_t s = a + b;

@@ -17,10 +17,8 @@ namespace dm {
 struct DeviceTables {
     PrimeConsts pc;
     CrtConsts cc;
-    const uint32_t* zeta = nullptr;   // [prime][kMaxRing]: psi^brv(k)
-    const uint32_t* zetas = nullptr;  // Shoup constants of zeta
-    const uint32_t* zinv = nullptr;   // inverses
-    const uint32_t* zinvs = nullptr;
+    const Tw* fwd = nullptr;  // [prime][kMaxRing]: psi^brv(k) with Shoup constants
+    const Tw* inv = nullptr;  // inverses
 };
 
 // Uploads the tables to the current device and sets the kernels' shared-memory

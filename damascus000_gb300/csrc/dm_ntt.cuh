@@ -38,28 +38,35 @@ DM_HD uint32_t ntt_place(int L, int pass, uint32_t t, uint32_t r) {
 DM_HD uint32_t ntt_swz(uint32_t i) { return i ^ ((i >> 4) & 31u); }
 
 // ---- Harvey butterflies on [0, 4p) (p < 2^30) ----
+//
+// Twiddle of the butterfly on register r in stage st of a pass:
+// k = 2^st + (j >> (bb + 1)) with j = place(t, r) and bb = L - 1 - st.  The
+// register field sits at bits [lo, lo + 4) of j and bb = lo + rb, so
+// k = 2^st + ((t >> lo) << (3 - rb)) + (r >> (rb + 1)): a stage needs only
+// 8 >> rb distinct twiddles per thread (15 per four-stage pass, not 32).
 
 // Forward (Cooley-Tukey) stages [4*pass, min(4*pass+4, L)) on the 16 registers
-// of thread t; inputs and outputs in [0, 4p).  zeta / zetas: this prime's
-// bit-reversed twiddles psi^brv(k) and their Shoup constants.
-DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const uint32_t* zeta, const uint32_t* zetas,
-                        uint32_t p) {
+// of thread t; inputs and outputs in [0, 4p).  tw: this prime's bit-reversed
+// twiddles psi^brv(k) with Shoup constants.
+DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p) {
     const int lo = ntt_pass_lo(L, pass);
     const int st_end = (4 * pass + 4 < L) ? 4 * pass + 4 : L;
     const uint32_t p2 = 2 * p;
+    const uint32_t th = t >> lo;
     DM_UNROLL
     for (int st = 4 * pass; st < st_end; ++st) {
-        const int bb = L - 1 - st;  // bit of the butterfly distance
-        const int rb = bb - lo;     // same bit within r
+        const int rb = L - 1 - st - lo;  // bit of the butterfly distance within r
+        const uint32_t kb = (1u << st) + (th << (3 - rb));
+        Tw w[8];
+        DM_UNROLL
+        for (int g = 0; g < (8 >> rb); ++g) w[g] = tw[kb + g];
         DM_UNROLL
         for (int r = 0; r < kNttE; ++r) {
             if (r & (1 << rb)) continue;
-            const uint32_t j = ntt_place(L, pass, t, (uint32_t)r);
-            const uint32_t k = (1u << st) + (j >> (bb + 1));
-            const uint32_t u = red_below(a[r], p2);                          // [0, 2p)
-            const uint32_t v = shoup_mul(a[r | (1 << rb)], zeta[k], zetas[k], p);  // [0, 2p)
-            a[r] = u + v;                                                   // [0, 4p)
-            a[r | (1 << rb)] = u - v + p2;                                  // (0, 4p)
+            const uint32_t u = red_below(a[r], p2);                           // [0, 2p)
+            const uint32_t v = shoup_mul(a[r | (1 << rb)], w[r >> (rb + 1)], p);  // [0, 2p)
+            a[r] = u + v;                                                    // [0, 4p)
+            a[r | (1 << rb)] = u - v + p2;                                   // (0, 4p)
         }
     }
 }
@@ -67,31 +74,41 @@ DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const ui
 // Inverse (Gentleman-Sande) stages of the same pass in reverse order (passes
 // from last to first, stages within a pass from the deepest up); inputs and
 // outputs in [0, 2p).
-DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const uint32_t* zinv, const uint32_t* zinvs,
-                        uint32_t p) {
+DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p) {
     const int lo = ntt_pass_lo(L, pass);
     const int st_end = (4 * pass + 4 < L) ? 4 * pass + 4 : L;
     const uint32_t p2 = 2 * p;
+    const uint32_t th = t >> lo;
     DM_UNROLL
     for (int st = st_end - 1; st >= 4 * pass; --st) {
-        const int bb = L - 1 - st;
-        const int rb = bb - lo;
+        const int rb = L - 1 - st - lo;
+        const uint32_t kb = (1u << st) + (th << (3 - rb));
+        Tw w[8];
+        DM_UNROLL
+        for (int g = 0; g < (8 >> rb); ++g) w[g] = tw[kb + g];
         DM_UNROLL
         for (int r = 0; r < kNttE; ++r) {
             if (r & (1 << rb)) continue;
-            const uint32_t j = ntt_place(L, pass, t, (uint32_t)r);
-            const uint32_t k = (1u << st) + (j >> (bb + 1));
             const uint32_t u = a[r], v = a[r | (1 << rb)];
             a[r] = red_below(u + v, p2);
-            a[r | (1 << rb)] = shoup_mul(u - v + p2, zinv[k], zinvs[k], p);
+            a[r | (1 << rb)] = shoup_mul(u - v + p2, w[r >> (rb + 1)], p);
         }
     }
 }
 
+// Shared-memory exchange between passes.  The swizzle is linear over GF(2) and
+// a row-base | place(t, 0) word has no bits in the register field, so the word
+// of register r is swz(base | place(t, 0)) ^ swz(r << lo): one XOR with a
+// compile-time constant per access.
+DM_HD uint32_t ntt_swz_base(uint32_t base, int L, int pass, uint32_t t) {
+    return ntt_swz(base | ntt_place(L, pass, t, 0));
+}
+DM_HD uint32_t ntt_swz_reg(int L, int pass, int r) { return ntt_swz((uint32_t)r << ntt_pass_lo(L, pass)); }
+
 // Whole transforms of one ring of size s = 2^L < 16 held in registers (one
 // thread per ring and prime): forward on [0, 4p), inverse on [0, 2p).
 template <int L>
-DM_HD void ntt_fwd_small(uint32_t* a, const uint32_t* zeta, const uint32_t* zetas, uint32_t p) {
+DM_HD void ntt_fwd_small(uint32_t* a, const Tw* tw, uint32_t p) {
     constexpr int s = 1 << L;
     const uint32_t p2 = 2 * p;
     DM_UNROLL
@@ -102,14 +119,14 @@ DM_HD void ntt_fwd_small(uint32_t* a, const uint32_t* zeta, const uint32_t* zeta
             if (j & len) continue;
             const uint32_t k = (1u << st) + (uint32_t)(j >> (L - st));
             const uint32_t u = red_below(a[j], p2);
-            const uint32_t v = shoup_mul(a[j + len], zeta[k], zetas[k], p);
+            const uint32_t v = shoup_mul(a[j + len], tw[k], p);
             a[j] = u + v;
             a[j + len] = u - v + p2;
         }
     }
 }
 template <int L>
-DM_HD void ntt_inv_small(uint32_t* a, const uint32_t* zinv, const uint32_t* zinvs, uint32_t p) {
+DM_HD void ntt_inv_small(uint32_t* a, const Tw* tw, uint32_t p) {
     constexpr int s = 1 << L;
     const uint32_t p2 = 2 * p;
     DM_UNROLL
@@ -121,7 +138,7 @@ DM_HD void ntt_inv_small(uint32_t* a, const uint32_t* zinv, const uint32_t* zinv
             const uint32_t k = (1u << st) + (uint32_t)(j >> (L - st));
             const uint32_t u = a[j], v = a[j + len];
             a[j] = red_below(u + v, p2);
-            a[j + len] = shoup_mul(u - v + p2, zinv[k], zinvs[k], p);
+            a[j + len] = shoup_mul(u - v + p2, tw[k], p);
         }
     }
 }

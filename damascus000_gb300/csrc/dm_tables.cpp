@@ -125,10 +125,8 @@ HostTables build() {
         if (p < (1u << 30) && is_prime_u32(p)) t.primes[found++] = p;
     }
     const size_t tab = (size_t)kPrimes * kMaxRing;
-    t.zeta.resize(tab);
-    t.zetas.resize(tab);
-    t.zinv.resize(tab);
-    t.zinvs.resize(tab);
+    t.fwd.resize(tab);
+    t.inv.resize(tab);
     for (int i = 0; i < kPrimes; ++i) {
         const uint32_t p = t.primes[i];
         PrimeConsts& c = t.pc;
@@ -146,10 +144,9 @@ HostTables build() {
         for (uint32_t k = 0; k < kMaxRing; ++k) {
             const uint32_t e = bitrev(k, kLogMaxRing);
             const size_t at = (size_t)i * kMaxRing + k;
-            t.zeta[at] = pow_mod(psi, e, p);
-            t.zetas[at] = shoup_const(t.zeta[at], p);
-            t.zinv[at] = pow_mod(psi_inv, e, p);
-            t.zinvs[at] = shoup_const(t.zinv[at], p);
+            const uint32_t z = pow_mod(psi, e, p), zi = pow_mod(psi_inv, e, p);
+            t.fwd[at] = Tw{z, shoup_const(z, p)};
+            t.inv[at] = Tw{zi, shoup_const(zi, p)};
         }
         const uint32_t inv4 = inv_mod(4, p);
         for (int L = 0; L <= kLogMaxRing; ++L) {

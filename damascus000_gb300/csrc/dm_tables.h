@@ -13,10 +13,10 @@ struct HostTables {
     uint32_t primes[kPrimes];  // the nine largest primes p < 2^30 with p = 1 mod 2^14
     PrimeConsts pc;
     CrtConsts cc;
-    // zeta[i * kMaxRing + k] = psi_i^brv13(k) mod p_i, psi_i a primitive
-    // 2*kMaxRing-th root of unity; zinv holds the inverses.  zetas / zinvs are
-    // the Shoup constants floor(z * 2^32 / p).
-    std::vector<uint32_t> zeta, zetas, zinv, zinvs;
+    // fwd[i * kMaxRing + k] = psi_i^brv13(k) mod p_i (psi_i a primitive
+    // 2*kMaxRing-th root of unity) with its Shoup constant floor(z * 2^32 / p);
+    // inv holds the inverses.
+    std::vector<Tw> fwd, inv;
     // Final scale of an inverse transform of size 2^L: n^-1, and n^-1 / 4 for
     // the even/odd cross terms (with Shoup constants).
     uint32_t ninv[kPrimes][kLogMaxRing + 1], ninvs[kPrimes][kLogMaxRing + 1];

@@ -68,7 +68,66 @@ __global__ void __launch_bounds__(kFoldThreads) fold_jobs_kernel(JobList<FoldJob
 constexpr int kGenThreads = 256;
 constexpr int kGenItems = 4;
 
-__global__ void __launch_bounds__(kGenThreads) gen_jobs_kernel(JobList<GenJob> J) {
+// 32-bit add issued on the FMA pipe (a * one + b with `one` a kernel argument
+// equal to 1, opaque to the compiler).  BLAKE3 is all adds, XORs and rotates;
+// moving the adds off the integer ALU pipe leaves that pipe only the XORs and
+// rotates.
+DM_D uint32_t fadd(uint32_t a, uint32_t b, uint32_t one) {
+    uint32_t r;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(one), "r"(b));
+    return r;
+}
+
+// BLAKE3 G on the generator message, whose words 7..15 are zero
+// (src/commitment/sis.rs:231-245: 25-byte "g" || i || k || c blocks).
+#define DM_GEN_G(a, b, c, d, X, Y)                        \
+    do {                                                   \
+        a = fadd(b, a, one);                               \
+        if ((X) < 7) a = fadd(m[(X) < 7 ? (X) : 0], a, one); \
+        d = b3_rotr(d ^ a, 16);                            \
+        c = fadd(d, c, one);                               \
+        b = b3_rotr(b ^ c, 12);                            \
+        a = fadd(b, a, one);                               \
+        if ((Y) < 7) a = fadd(m[(Y) < 7 ? (Y) : 0], a, one); \
+        d = b3_rotr(d ^ a, 8);                             \
+        c = fadd(d, c, one);                               \
+        b = b3_rotr(b ^ c, 7);                             \
+    } while (0)
+#define DM_GEN_ROUND(S0, S1, S2, S3, S4, S5, S6, S7, S8, S9, S10, S11, S12, S13, S14, S15) \
+    do {                                                                                   \
+        DM_GEN_G(v0, v4, v8, v12, S0, S1);                                                 \
+        DM_GEN_G(v1, v5, v9, v13, S2, S3);                                                 \
+        DM_GEN_G(v2, v6, v10, v14, S4, S5);                                                \
+        DM_GEN_G(v3, v7, v11, v15, S6, S7);                                                \
+        DM_GEN_G(v0, v5, v10, v15, S8, S9);                                                \
+        DM_GEN_G(v1, v6, v11, v12, S10, S11);                                              \
+        DM_GEN_G(v2, v7, v8, v13, S12, S13);                                               \
+        DM_GEN_G(v3, v4, v9, v14, S14, S15);                                               \
+    } while (0)
+
+// Keyed root compression of one 25-byte generator block: the first 8 output words.
+DM_D void gen_compress(const uint32_t key[8], const uint32_t m[7], uint32_t one, uint32_t out[8]) {
+    uint32_t v0 = key[0], v1 = key[1], v2 = key[2], v3 = key[3], v4 = key[4], v5 = key[5], v6 = key[6], v7 = key[7];
+    uint32_t v8 = DM_B3_IV0, v9 = DM_B3_IV1, v10 = DM_B3_IV2, v11 = DM_B3_IV3;
+    uint32_t v12 = 0, v13 = 0, v14 = 25, v15 = kB3ChunkStart | kB3ChunkEnd | kB3Root | kB3Keyed;
+    DM_GEN_ROUND(0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15);
+    DM_GEN_ROUND(2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8);
+    DM_GEN_ROUND(3, 4, 10, 12, 13, 2, 7, 14, 6, 5, 9, 0, 11, 15, 8, 1);
+    DM_GEN_ROUND(10, 7, 12, 9, 14, 3, 13, 15, 4, 0, 11, 2, 5, 8, 1, 6);
+    DM_GEN_ROUND(12, 13, 9, 11, 15, 10, 14, 8, 7, 2, 5, 3, 0, 1, 6, 4);
+    DM_GEN_ROUND(9, 14, 11, 5, 8, 12, 15, 1, 13, 3, 0, 10, 2, 6, 4, 7);
+    DM_GEN_ROUND(11, 15, 5, 0, 1, 9, 8, 6, 14, 10, 2, 12, 3, 4, 7, 13);
+    out[0] = v0 ^ v8;
+    out[1] = v1 ^ v9;
+    out[2] = v2 ^ v10;
+    out[3] = v3 ^ v11;
+    out[4] = v4 ^ v12;
+    out[5] = v5 ^ v13;
+    out[6] = v6 ^ v14;
+    out[7] = v7 ^ v15;
+}
+
+__global__ void __launch_bounds__(kGenThreads) gen_jobs_kernel(JobList<GenJob> J, uint32_t one) {
     const GenJob jb = J.j[find_job(J)];
     const uint64_t base = (uint64_t)(blockIdx.x - jb.cta0) * kGenThreads * kGenItems + threadIdx.x;
     for (int it = 0; it < kGenItems; ++it) {
@@ -77,10 +136,11 @@ __global__ void __launch_bounds__(kGenThreads) gen_jobs_kernel(JobList<GenJob> J
         const uint64_t c = e & ((1ull << jb.log_n) - 1);
         const uint64_t kk = (e >> jb.log_n) & 7u;
         const uint64_t i = e >> (jb.log_n + 3);
-        uint32_t m[16], out[16];
+        uint32_t m[16], out[8];
         b3_generator_block(i, kk, c, m);
-        b3_compress(jb.key, m, 0, 25, kB3ChunkStart | kB3ChunkEnd | kB3Root | kB3Keyed, out);
-        stq(jb.dst, e, fq_reduce8(out));
+        gen_compress(jb.key, m, one, out);
+        uint32_t r8[8] = {out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7]};
+        stq(jb.dst, e, fq_reduce8(r8));
     }
 }
 
@@ -192,7 +252,7 @@ cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st) {
         return (j.total + kGenThreads * kGenItems - 1) / (kGenThreads * kGenItems);
     });
     if (!ctas) return cudaSuccess;
-    gen_jobs_kernel<<<ctas, kGenThreads, 0, st>>>(JL);
+    gen_jobs_kernel<<<ctas, kGenThreads, 0, st>>>(JL, 1u);
     return cudaGetLastError();
 }
 

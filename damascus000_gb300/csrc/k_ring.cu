@@ -39,14 +39,15 @@ struct RowShape {
     static constexpr int THREADS = ROWS * T;
     static constexpr int PASSES = (L + 3) / 4;
     static constexpr size_t SMEM = PASSES > 1 ? (size_t)ROWS * (1u << L) * sizeof(uint32_t) : 0;
+    // resident blocks per SM the register budget is sized for (48 warps per SM)
+    static constexpr int MIN_BLOCKS = (48 * 32) / THREADS > 0 ? (48 * 32) / THREADS : 1;
 };
 
 // ================================================================ forward NTT
 
 template <int L>
-__global__ void __launch_bounds__(RowShape<L>::THREADS)
-    ntt_fwd_kernel(JobList<NttJob> J, PrimeConsts pc, const uint32_t* __restrict__ zeta,
-                   const uint32_t* __restrict__ zetas) {
+__global__ void __launch_bounds__(RowShape<L>::THREADS, RowShape<L>::MIN_BLOCKS)
+    ntt_fwd_kernel(JobList<NttJob> J, PrimeConsts pc, const Tw* __restrict__ fwd) {
     using S = RowShape<L>;
     extern __shared__ __align__(16) uint32_t sm[];
     const NttJob jb = J.j[find_job(J)];
@@ -58,8 +59,7 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
     const uint32_t pi = third * kPrimesPerBlock + row % kPrimesPerBlock;
     const bool active = poly < jb.npolys;
     const uint32_t p = pc.p[pi];
-    const uint32_t* zt = zeta + pi * kMaxRing;
-    const uint32_t* zs = zetas + pi * kMaxRing;
+    const Tw* tw = fwd + pi * kMaxRing;
     uint32_t a[kNttE];
     if (active) {
         const uint4* src = jb.src + (poly << L);
@@ -72,13 +72,15 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
     const uint32_t base = row << L;
 #pragma unroll
     for (int pass = 0; pass < S::PASSES; ++pass) {
-        ntt_fwd_pass(a, L, pass, t, zt, zs, p);
+        ntt_fwd_pass(a, L, pass, t, tw, p);
         if (pass + 1 < S::PASSES) {
+            const uint32_t ws = ntt_swz_base(base, L, pass, t);
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) sm[ntt_swz(base + ntt_place(L, pass, t, r))] = a[r];
+            for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[r];
             __syncthreads();
+            const uint32_t rs = ntt_swz_base(base, L, pass + 1, t);
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) a[r] = sm[ntt_swz(base + ntt_place(L, pass + 1, t, r))];
+            for (int r = 0; r < kNttE; ++r) a[r] = sm[rs ^ ntt_swz_reg(L, pass + 1, r)];
             __syncthreads();
         }
     }
@@ -98,8 +100,7 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
 // Rings smaller than 16: one thread per (polynomial, prime), all in registers.
 template <int L>
 __global__ void __launch_bounds__(128) ntt_fwd_small_kernel(JobList<NttJob> J, PrimeConsts pc,
-                                                            const uint32_t* __restrict__ zeta,
-                                                            const uint32_t* __restrict__ zetas) {
+                                                            const Tw* __restrict__ fwd) {
     constexpr int s = 1 << L;
     const NttJob jb = J.j[find_job(J)];
     const uint64_t item = (uint64_t)(blockIdx.x - jb.cta0) * blockDim.x + threadIdx.x;
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(128) ntt_fwd_small_kernel(JobList<NttJob> J, P
     uint32_t a[s];
 #pragma unroll
     for (int c = 0; c < s; ++c) a[c] = residue_lazy(ldq(jb.src + (poly << L), c), pc, pi);
-    ntt_fwd_small<L>(a, zeta + pi * kMaxRing, zetas + pi * kMaxRing, p);
+    ntt_fwd_small<L>(a, fwd + pi * kMaxRing, p);
 #pragma unroll
     for (int c = 0; c < s; ++c) jb.dst[((poly * kPrimes + pi) << L) + c] = red_below(red_below(a[c], 2 * p), p);
 }
@@ -168,48 +169,53 @@ __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> 
 
 // Triple MAC over h = count column pairs (i, i + h): one read of every generator
 // column gives the full sum (out0), L = sum G[i+h] M[i] (out1) and
-// R = sum G[i] M[i+h] (out2).
+// R = sum G[i] M[i+h] (out2).  Thread per slot pair (8-byte loads), L >= 1.
 __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
     const MacJobX jb = J.j[find_job(J)];
-    const uint32_t s = 1u << L;
-    const uint32_t nblk = slot_block_count(s);
+    const uint32_t sp = 1u << (L - 1);
+    const uint32_t nblk = slot_block_count(sp);
     uint32_t c = blockIdx.x - jb.cta0;
     const uint32_t blk = c % nblk;
     c /= nblk;
     const uint32_t kp = c % kRows;
     const uint32_t part = c / kRows;
-    const uint32_t slot = blk * kMacThreads + threadIdx.x;
-    if (slot >= s) return;
+    const uint32_t i2 = blk * kMacThreads + threadIdx.x;
+    if (i2 >= sp) return;
     const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
     const uint32_t h = jb.count;
     const uint32_t i0 = (uint32_t)((uint64_t)h * part / jb.parts);
     const uint32_t i1 = (uint32_t)((uint64_t)h * (part + 1) / jb.parts);
     const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
     const uint64_t mstride = (uint64_t)kPrimes << L;
-    const uint32_t* g = jb.G + ((((uint64_t)k) * kPrimes + pi) << L) + slot;
-    const uint32_t* m = jb.M + (((uint64_t)pi) << L) + slot;
+    const uint32_t* g = jb.G + ((((uint64_t)k) * kPrimes + pi) << L) + 2 * i2;
+    const uint32_t* m = jb.M + (((uint64_t)pi) << L) + 2 * i2;
     const uint64_t gh = (uint64_t)h * gstride, mh = (uint64_t)h * mstride;
-    uint64_t cl = 0, ll = 0, rl = 0;
-    uint32_t ch = 0, lh = 0, rh = 0;
+    uint64_t lo[6] = {0, 0, 0, 0, 0, 0};  // (full, L, R) x (even, odd slot)
+    uint32_t hi[6] = {0, 0, 0, 0, 0, 0};
     uint32_t i = i0;
     while (i < i1) {
         const uint32_t e = i + 8 < i1 ? i + 8 : i1;  // <= 16 products per block sum
-        uint64_t bc = 0, bl = 0, br = 0;
+        uint64_t b[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 4
         for (; i < e; ++i) {
-            const uint32_t gl = __ldg(g + i * gstride), gr = __ldg(g + i * gstride + gh);
-            const uint32_t ml = __ldg(m + i * mstride), mr = __ldg(m + i * mstride + mh);
-            bc += mul64(gl, ml) + mul64(gr, mr);
-            bl += mul64(gr, ml);
-            br += mul64(gl, mr);
+            const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
+            const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
+            const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
+            const uint2 mr = __ldg(reinterpret_cast<const uint2*>(m + i * mstride + mh));
+            b[0] += mul64(gl.x, ml.x) + mul64(gr.x, mr.x);
+            b[1] += mul64(gl.y, ml.y) + mul64(gr.y, mr.y);
+            b[2] += mul64(gr.x, ml.x);
+            b[3] += mul64(gr.y, ml.y);
+            b[4] += mul64(gl.x, mr.x);
+            b[5] += mul64(gl.y, mr.y);
         }
-        acc96(cl, ch, bc);
-        acc96(ll, lh, bl);
-        acc96(rl, rh, br);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) acc96(lo[q], hi[q], b[q]);
     }
-    const uint64_t o = (((uint64_t)part * kRows + kp) << L) + slot;
-    jb.out0[o] = red96(ch, cl, pc, pi);
-    jb.out1[o] = red96(lh, ll, pc, pi);
-    jb.out2[o] = red96(rh, rl, pc, pi);
+    const uint64_t o = (((uint64_t)part * kRows + kp) << L) + 2 * i2;
+    *reinterpret_cast<uint2*>(jb.out0 + o) = make_uint2(red96(hi[0], lo[0], pc, pi), red96(hi[1], lo[1], pc, pi));
+    *reinterpret_cast<uint2*>(jb.out1 + o) = make_uint2(red96(hi[2], lo[2], pc, pi), red96(hi[3], lo[3], pc, pi));
+    *reinterpret_cast<uint2*>(jb.out2 + o) = make_uint2(red96(hi[4], lo[4], pc, pi), red96(hi[5], lo[5], pc, pi));
 }
 
 // Split MAC: thread per slot pair (2 i2, 2 i2 + 1) of ring 2^L (L >= 1): the
@@ -240,6 +246,7 @@ __global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<Mac
     while (i < i1) {
         const uint32_t e = i + 16 < i1 ? i + 16 : i1;
         uint64_t b0 = 0, b1 = 0, bl = 0, br = 0;
+#pragma unroll 4
         for (; i < e; ++i) {
             const uint2 gv = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
             const uint2 mv = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
@@ -264,10 +271,9 @@ struct FinishConsts {
     uint32_t f[kPrimes], fs[kPrimes];  // final inverse-transform scale and its Shoup constant
 };
 
-DM_D uint32_t twist(uint32_t x, uint32_t mode, uint32_t idx, const uint32_t* zeta, const uint32_t* zetas,
-                    const uint32_t* zinv, const uint32_t* zinvs, uint32_t p) {
-    if (mode == kFinishSplitL) return shoup_mul(x, zeta[idx], zetas[idx], p);
-    if (mode == kFinishSplitR) return shoup_mul(x, zinv[idx], zinvs[idx], p);
+DM_D uint32_t twist(uint32_t x, uint32_t mode, uint32_t idx, const Tw* fwd, const Tw* inv, uint32_t p) {
+    if (mode == kFinishSplitL) return shoup_mul(x, fwd[idx], p);
+    if (mode == kFinishSplitR) return shoup_mul(x, inv[idx], p);
     return x;
 }
 
@@ -278,8 +284,7 @@ DM_D uint32_t twist(uint32_t x, uint32_t mode, uint32_t idx, const uint32_t* zet
 template <int L>
 __global__ void __launch_bounds__(RowShape<L>::THREADS)
     inv_rows_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
-                    const uint32_t* __restrict__ zeta, const uint32_t* __restrict__ zetas,
-                    const uint32_t* __restrict__ zinv, const uint32_t* __restrict__ zinvs) {
+                    const Tw* __restrict__ fwd, const Tw* __restrict__ inv) {
     using S = RowShape<L>;
     constexpr uint32_t s = 1u << L;
     extern __shared__ __align__(16) uint32_t sm[];
@@ -309,21 +314,22 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
         if (jb.mode != kFinishPlain) {
 #pragma unroll
             for (int r = 0; r < kNttE; ++r)
-                a[r] = twist(a[r], jb.mode, pi * kMaxRing + s + t * kNttE + r, zeta, zetas, zinv, zinvs, p);
+                a[r] = twist(a[r], jb.mode, pi * kMaxRing + s + t * kNttE + r, fwd, inv, p);
         }
     }
-    const uint32_t* zi = zinv + pi * kMaxRing;
-    const uint32_t* zis = zinvs + pi * kMaxRing;
+    const Tw* tw = inv + pi * kMaxRing;
     const uint32_t base = brow << L;
 #pragma unroll
     for (int pass = S::PASSES - 1; pass >= 0; --pass) {
-        ntt_inv_pass(a, L, pass, t, zi, zis, p);
+        ntt_inv_pass(a, L, pass, t, tw, p);
         if (pass > 0) {
+            const uint32_t ws = ntt_swz_base(base, L, pass, t);
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) sm[ntt_swz(base + ntt_place(L, pass, t, r))] = a[r];
+            for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[r];
             __syncthreads();
+            const uint32_t rs = ntt_swz_base(base, L, pass - 1, t);
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) a[r] = sm[ntt_swz(base + ntt_place(L, pass - 1, t, r))];
+            for (int r = 0; r < kNttE; ++r) a[r] = sm[rs ^ ntt_swz_reg(L, pass - 1, r)];
             __syncthreads();
         }
     }
@@ -340,8 +346,7 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
 template <int L>
 __global__ void __launch_bounds__(128)
     inv_rows_small_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
-                          const uint32_t* __restrict__ zeta, const uint32_t* __restrict__ zetas,
-                          const uint32_t* __restrict__ zinv, const uint32_t* __restrict__ zinvs) {
+                          const Tw* __restrict__ fwd, const Tw* __restrict__ inv) {
     constexpr uint32_t s = 1u << L;
     const FinishJobX jb = J.j[find_job(J)];
     const uint32_t row = (blockIdx.x - jb.cta0) * blockDim.x + threadIdx.x;
@@ -354,9 +359,9 @@ __global__ void __launch_bounds__(128)
         uint32_t acc = 0;
         for (uint32_t part = 0; part < jb.parts; ++part)
             acc = red_below(acc + jb.partials[(((uint64_t)part * jb.rows + row) << L) + c], p);
-        a[c] = twist(acc, jb.mode, pi * kMaxRing + s + c, zeta, zetas, zinv, zinvs, p);
+        a[c] = twist(acc, jb.mode, pi * kMaxRing + s + c, fwd, inv, p);
     }
-    ntt_inv_small<L>(a, zinv + pi * kMaxRing, zinvs + pi * kMaxRing, p);
+    ntt_inv_small<L>(a, inv + pi * kMaxRing, p);
     const FinishConsts& fc = (jb.mode == kFinishPlain) ? plain : split;
 #pragma unroll
     for (uint32_t c = 0; c < s; ++c)
@@ -403,14 +408,14 @@ cudaError_t ntt_launch_L(const DeviceTables& T, JobList<NttJob>& JL, NttJob* job
             return ((uint64_t)j.npolys * kPrimes + 127) / 128;
         });
         if (!ctas) return cudaSuccess;
-        ntt_fwd_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, T.zeta, T.zetas);
+        ntt_fwd_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, T.fwd);
     } else {
         using S = RowShape<L>;
         const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
             return ((uint64_t)(j.npolys + S::P - 1) / S::P) * kGroups;
         });
         if (!ctas) return cudaSuccess;
-        ntt_fwd_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.zeta, T.zetas);
+        ntt_fwd_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.fwd);
     }
     return cudaGetLastError();
 }
@@ -423,15 +428,14 @@ cudaError_t inv_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJ
             return ((uint64_t)j.rows + 127) / 128;
         });
         if (!ctas) return cudaSuccess;
-        inv_rows_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, plain, split, T.zeta, T.zetas, T.zinv, T.zinvs);
+        inv_rows_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, plain, split, T.fwd, T.inv);
     } else {
         using S = RowShape<L>;
         const uint32_t ctas = assign_ctas<FinishJobX>(jobs, n, JL, [](const FinishJobX& j) -> uint64_t {
             return ((uint64_t)j.rows + S::ROWS - 1) / S::ROWS;
         });
         if (!ctas) return cudaSuccess;
-        inv_rows_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, plain, split, T.zeta, T.zetas, T.zinv,
-                                                             T.zinvs);
+        inv_rows_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, plain, split, T.fwd, T.inv);
     }
     return cudaGetLastError();
 }
@@ -459,30 +463,28 @@ cudaError_t upload_tables(DeviceTables* out) {
     const HostTables& H = host_tables();
     out->pc = H.pc;
     out->cc = H.cc;
-    const size_t bytes = sizeof(uint32_t) * H.zeta.size();
-    const std::vector<uint32_t>* src[4] = {&H.zeta, &H.zetas, &H.zinv, &H.zinvs};
-    uint32_t* dst[4] = {nullptr, nullptr, nullptr, nullptr};
+    const size_t bytes = sizeof(Tw) * H.fwd.size();
+    const std::vector<Tw>* src[2] = {&H.fwd, &H.inv};
+    Tw* dst[2] = {nullptr, nullptr};
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
         e = cudaMalloc(&dst[i], bytes);
         if (e == cudaSuccess) e = cudaMemcpy(dst[i], src[i]->data(), bytes, cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) {
-        for (uint32_t* d : dst)
+        for (Tw* d : dst)
             if (d) cudaFree(d);
         return e;
     }
-    out->zeta = dst[0];
-    out->zetas = dst[1];
-    out->zinv = dst[2];
-    out->zinvs = dst[3];
+    out->fwd = dst[0];
+    out->inv = dst[1];
     return cudaSuccess;
 }
 
 void free_tables(DeviceTables* t) {
-    for (const uint32_t* d : {t->zeta, t->zetas, t->zinv, t->zinvs})
-        if (d) cudaFree(const_cast<uint32_t*>(d));
-    t->zeta = t->zetas = t->zinv = t->zinvs = nullptr;
+    for (const Tw* d : {t->fwd, t->inv})
+        if (d) cudaFree(const_cast<Tw*>(d));
+    t->fwd = t->inv = nullptr;
 }
 
 cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st) {
@@ -497,9 +499,9 @@ cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t
 
 cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (n > kMaxJobs) return cudaErrorInvalidValue;
+    if (n > kMaxJobs || L == 0) return cudaErrorInvalidValue;
     JobList<MacJobX> JL;
-    const uint32_t slots = 1u << L;
+    const uint32_t slots = 1u << (L - 1);  // slot pairs
     uint64_t total = 0;
     JL.n = n;
     for (int i = 0; i < n; ++i) {
