@@ -323,7 +323,7 @@ def run_gpu(args, wl):
         dev = [torch.frombuffer(bytearray(d), dtype=torch.uint8).cuda() for d, _, _ in files]
         pinned = [torch.frombuffer(bytearray(d), dtype=torch.uint8).pin_memory() for d, _, _ in files]
         torch.cuda.synchronize()
-        eng = D.Engine(ctx)
+        eng = D.Engine(ctx, max_waves=args.waves)
 
         def replay_device():
             ts = [eng.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]
@@ -429,6 +429,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="serve", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--waves", type=int, default=0, help="engine stage waves in flight (0: library default)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -15,11 +15,15 @@ constexpr size_t kTail = 128;  // pinned tail: [0,32) file id, [32,40) flags, [4
 
 constexpr uint32_t kRows = kRank * kPrimes;  // MAC rows per job: (coordinate, prime)
 
-uint32_t mac_parts(uint32_t slots, int njobs, uint32_t count) {
-    const uint32_t ctas = ((slots + 127) / 128) * kRows * (uint32_t)njobs;
-    uint32_t parts = (1216u + ctas - 1) / ctas;
+// Column splits of a MAC: as many parts as fit one full wave of blocks (152 SMs
+// x 8 resident blocks), at most kMaxParts and at least one column per part.
+// Long column runs per thread keep more loads in flight than extra parts, and a
+// single wave has no tail.
+uint32_t mac_parts(uint32_t threads_per_row, uint32_t count) {
+    const uint32_t per_part = ((threads_per_row + 127) / 128) * kRows;
+    uint32_t parts = (152u * 8u) / per_part;
     if (parts > kMaxParts) parts = kMaxParts;
-    if (parts > count) parts = count ? count : 1;
+    if (parts > count) parts = count;
     return parts ? parts : 1;
 }
 
@@ -311,10 +315,10 @@ void ProofState::plan_stage(Plan& P) {
         g.total = 8 * S2;
         g.log_n = L;
         P.gen.push_back(g);
-        P.ntt[L].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), S, 0});
-        P.ntt[L].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * S, 0});
+        P.ntt[L].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), S, 0, 0});
+        P.ntt[L].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * S, 0, 1});
         const int nj = S >= 2 ? 3 : 1;
-        parts_ = mac_parts(S, 1, S / 2 ? S / 2 : 1);
+        parts_ = nj == 3 ? mac_parts(S / 2, S / 2) : mac_parts(S, S);
         const size_t pstride = (size_t)parts_ * kRows * S;
         if (nj == 3) {
             P.triple[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
@@ -341,9 +345,9 @@ void ProofState::plan_stage(Plan& P) {
         P.fold.push_back(FoldJob{g_b_.as<uint4>(), g_a_.as<uint4>(), g_a_.as<uint4>() + 4 * s2, nullptr, xi_, fq_zero(),
                                  4 * s2, kFoldVec, 0, 0});
         P.fold.push_back(FoldJob{cs(kCt), cs(kC), cs(kL), cs(kR), xi_, x_, (uint64_t)kRank * s, kCombine, 0, 0});
-        P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
-        P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
-        parts_ = mac_parts(h, 1, h);
+        P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), h, 0, 0});
+        P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0, 1});
+        parts_ = mac_parts(h, h);
         uint32_t* pchk = part;
         uint32_t* plp = part + (size_t)parts_ * kRows * s;
         uint32_t* prp = plp + (size_t)parts_ * kRows * h;
@@ -364,10 +368,10 @@ void ProofState::plan_stage(Plan& P) {
         P.fold.push_back(FoldJob{g_a_.as<uint4>(), g_b_.as<uint4>(), nullptr, nullptr, yi_, fq_zero(), 8 * h2, kFoldPolyX,
                                  Ln, 0});
         P.fold.push_back(FoldJob{cs(kC), cs(kCt), cs(kLp), cs(kRp), yi_, y_, (uint64_t)kRank * h, kCombineEven, Ln, 0});
-        P.ntt[Ln].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
-        P.ntt[Ln].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
+        P.ntt[Ln].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), h, 0, 0});
+        P.ntt[Ln].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0, 1});
         const int nj = h >= 2 ? 3 : 1;
-        parts_ = mac_parts(h, 1, h / 2 ? h / 2 : 1);
+        parts_ = nj == 3 ? mac_parts(h / 2, h / 2) : mac_parts(h, h);
         const size_t pstride = (size_t)parts_ * kRows * h;
         if (nj == 3) {
             P.triple[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
