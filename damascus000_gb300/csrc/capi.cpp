@@ -253,8 +253,8 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
         out.alloc(C, kRank * n * 16))
         return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
     cudaStream_t s = C->stream();
-    NttJob nj[2] = {{m.m.as<uint4>(), mh.m.as<uint32_t>(), (uint32_t)N, 0, 0},
-                    {gg.m.as<uint4>(), gh.m.as<uint32_t>(), (uint32_t)(N * kRank), 0, 1}};
+    NttJob nj[2] = {{m.m.as<uint4>(), mh.m.as<uint32_t>(), (uint32_t)N, 0},
+                    {gg.m.as<uint4>(), gh.m.as<uint32_t>(), (uint32_t)(N * kRank), 0}};
     MacJobX mj{gh.m.as<uint32_t>(), mh.m.as<uint32_t>(), part.m.as<uint32_t>(), nullptr, nullptr, 0, 0, (uint32_t)N,
                parts, 0};
     FinishJobX fj{part.m.as<uint32_t>(), out.m.as<uint4>(), nullptr, nullptr, parts, kFinishPlain, rows, 0};
@@ -337,8 +337,8 @@ int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const voi
         e0 = C->take_event();
         cudaEventRecord(e0, s);
     }
-    NttJob nj[2] = {{static_cast<const uint4*>(d_a), ra.m.as<uint32_t>(), (uint32_t)count, 0, 0},
-                    {static_cast<const uint4*>(d_b), rb.m.as<uint32_t>(), (uint32_t)count, 0, 0}};
+    NttJob nj[2] = {{static_cast<const uint4*>(d_a), ra.m.as<uint32_t>(), (uint32_t)count, 0},
+                    {static_cast<const uint4*>(d_b), rb.m.as<uint32_t>(), (uint32_t)count, 0}};
     cudaError_t e = launch_ntt_jobs(T, nj, 2, L, s);
     if (e0) {
         e1 = C->take_event();

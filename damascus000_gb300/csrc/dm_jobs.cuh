@@ -12,18 +12,14 @@ namespace dm {
 constexpr int kMaxJobs = 48;
 
 // ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][9][2^L] ----
-// lazy = 1 leaves the residues in [0, 4p) for a consumer that reduces them
-// (the generator transforms, read once by a memory-bound MAC); otherwise [0, p).
 struct NttJob {
     const uint4* src;
     uint32_t* dst;
     uint32_t npolys;
     uint32_t cta0;  // filled by the launcher
-    uint32_t lazy;
 };
 
 // ---- multiply-accumulate over columns (all jobs of a launch share L) ----
-// G residues may be lazy ([0, 4p)); M residues are reduced.
 // plain: partials[part][k*9+p][slot] = sum_{i<count} G[g_base+i][k][p][slot] * M[m_base+i][p][slot]
 // split: chk over 2^L slots, lp / rp over 2^(L-1) (even/odd cross terms)
 struct MacJobX {

@@ -85,11 +85,9 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS, RowShape<L>::MIN_BLOCKS)
         }
     }
     if (active) {
-        if (!jb.lazy) {
-            const uint32_t p2 = 2 * p;
+        const uint32_t p2 = 2 * p;
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) a[r] = red_below(red_below(a[r], p2), p);
-        }
+        for (int r = 0; r < kNttE; ++r) a[r] = red_below(red_below(a[r], p2), p);
         // the last pass holds slots 16 t .. 16 t + 15
         uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * kNttE);
         dst[0] = make_uint4(a[0], a[1], a[2], a[3]);
@@ -130,8 +128,7 @@ DM_D void acc96(uint64_t& lo, uint32_t& hi, uint64_t v) {
     hi += lo < v ? 1u : 0u;
 }
 DM_D uint64_t mul64(uint32_t a, uint32_t b) { return (uint64_t)a * b; }
-// a generator residue from [0, 4p) to [0, p)
-DM_D uint32_t gnorm(uint32_t x, uint32_t p) { return red_below(red_below(x, 2 * p), p); }
+
 
 // grid: per job, nblk * 72 * parts blocks; block -> (part, row, slot block).
 __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
@@ -146,7 +143,6 @@ __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> 
     const uint32_t slot = blk * kMacThreads + threadIdx.x;
     if (slot >= s) return;
     const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
-    const uint32_t p = pc.p[pi];
     const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
     const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
     const uint64_t gstride = (uint64_t)kRank * kPrimes << L;  // one generator vector
@@ -160,14 +156,14 @@ __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> 
         uint64_t b0 = 0, b1 = 0;
 #pragma unroll
         for (int u = 0; u < 8; u += 2) {
-            b0 += mul64(gnorm(__ldg(g + (i + u) * gstride), p), __ldg(m + (i + u) * mstride));
-            b1 += mul64(gnorm(__ldg(g + (i + u + 1) * gstride), p), __ldg(m + (i + u + 1) * mstride));
+            b0 += mul64(__ldg(g + (i + u) * gstride), __ldg(m + (i + u) * mstride));
+            b1 += mul64(__ldg(g + (i + u + 1) * gstride), __ldg(m + (i + u + 1) * mstride));
         }
         acc96(lo, hi, b0);
         acc96(lo, hi, b1);
     }
     uint64_t b = 0;
-    for (; i < i1; ++i) b += mul64(gnorm(__ldg(g + i * gstride), p), __ldg(m + i * mstride));
+    for (; i < i1; ++i) b += mul64(__ldg(g + i * gstride), __ldg(m + i * mstride));
     acc96(lo, hi, b);
     jb.out0[(((uint64_t)part * kRows + kp) << L) + slot] = red96(hi, lo, pc, pi);
 }
@@ -187,7 +183,6 @@ __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<Ma
     const uint32_t i2 = blk * kMacThreads + threadIdx.x;
     if (i2 >= sp) return;
     const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
-    const uint32_t p = pc.p[pi];
     const uint32_t h = jb.count;
     const uint32_t i0 = (uint32_t)((uint64_t)h * part / jb.parts);
     const uint32_t i1 = (uint32_t)((uint64_t)h * (part + 1) / jb.parts);
@@ -204,10 +199,8 @@ __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<Ma
         uint64_t b[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 4
         for (; i < e; ++i) {
-            uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
-            uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
-            gl = make_uint2(gnorm(gl.x, p), gnorm(gl.y, p));
-            gr = make_uint2(gnorm(gr.x, p), gnorm(gr.y, p));
+            const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
+            const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
             const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
             const uint2 mr = __ldg(reinterpret_cast<const uint2*>(m + i * mstride + mh));
             b[0] += mul64(gl.x, ml.x) + mul64(gr.x, mr.x);
@@ -256,8 +249,7 @@ __global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<Mac
         uint64_t b0 = 0, b1 = 0, bl = 0, br = 0;
 #pragma unroll 4
         for (; i < e; ++i) {
-            uint2 gv = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
-            gv = make_uint2(gnorm(gv.x, p), gnorm(gv.y, p));
+            const uint2 gv = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
             const uint2 mv = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
             b0 += mul64(gv.x, mv.x);
             b1 += mul64(gv.y, mv.y);

@@ -315,8 +315,8 @@ void ProofState::plan_stage(Plan& P) {
         g.total = 8 * S2;
         g.log_n = L;
         P.gen.push_back(g);
-        P.ntt[L].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), S, 0, 0});
-        P.ntt[L].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * S, 0, 1});
+        P.ntt[L].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), S, 0});
+        P.ntt[L].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * S, 0});
         const int nj = S >= 2 ? 3 : 1;
         parts_ = nj == 3 ? mac_parts(S / 2, S / 2) : mac_parts(S, S);
         const size_t pstride = (size_t)parts_ * kRows * S;
@@ -341,12 +341,12 @@ void ProofState::plan_stage(Plan& P) {
     const uint64_t s2 = (uint64_t)s * s;
     if (stage_ == Stage::Vec) {
         P.fold.push_back(FoldJob{m_b_.as<uint4>(), m_a_.as<uint4>(), m_a_.as<uint4>() + (uint64_t)h * s, nullptr, x_,
-                                 fq_zero(), (uint64_t)h * s, kFoldVec, 0, 0});
+                                 fq_zero(), (uint64_t)h * s, kFoldVec, 0});
         P.fold.push_back(FoldJob{g_b_.as<uint4>(), g_a_.as<uint4>(), g_a_.as<uint4>() + 4 * s2, nullptr, xi_, fq_zero(),
-                                 4 * s2, kFoldVec, 0, 0});
-        P.fold.push_back(FoldJob{cs(kCt), cs(kC), cs(kL), cs(kR), xi_, x_, (uint64_t)kRank * s, kCombine, 0, 0});
-        P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), h, 0, 0});
-        P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0, 1});
+                                 4 * s2, kFoldVec, 0});
+        P.fold.push_back(FoldJob{cs(kCt), cs(kC), cs(kL), cs(kR), xi_, x_, (uint64_t)kRank * s, kCombine, 0});
+        P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
+        P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
         parts_ = mac_parts(h, h);
         uint32_t* pchk = part;
         uint32_t* plp = part + (size_t)parts_ * kRows * s;
@@ -368,8 +368,8 @@ void ProofState::plan_stage(Plan& P) {
         P.fold.push_back(FoldJob{g_a_.as<uint4>(), g_b_.as<uint4>(), nullptr, nullptr, yi_, fq_zero(), 8 * h2, kFoldPolyX,
                                  Ln, 0});
         P.fold.push_back(FoldJob{cs(kC), cs(kCt), cs(kLp), cs(kRp), yi_, y_, (uint64_t)kRank * h, kCombineEven, Ln, 0});
-        P.ntt[Ln].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), h, 0, 0});
-        P.ntt[Ln].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0, 1});
+        P.ntt[Ln].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
+        P.ntt[Ln].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
         const int nj = h >= 2 ? 3 : 1;
         parts_ = nj == 3 ? mac_parts(h / 2, h / 2) : mac_parts(h, h);
         const size_t pstride = (size_t)parts_ * kRows * h;
