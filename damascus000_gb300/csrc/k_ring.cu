@@ -43,6 +43,28 @@ struct RowShape {
     static constexpr int MIN_BLOCKS = (48 * 32) / THREADS > 0 ? (48 * 32) / THREADS : 1;
 };
 
+// Exchange barrier of one row: the row's 2^(L-4) threads are consecutive, so rows
+// of up to 32 threads sit inside one warp (a warp barrier suffices) and larger
+// rows own whole warps and a named barrier (id row + 1, counted in threads).
+// Rows then move through their passes independently instead of the whole block
+// waiting at each exchange.  Every thread of a row, active or not, runs the same
+// passes and so the same barriers.
+template <int L>
+DM_D void row_sync(uint32_t row) {
+    if constexpr ((1 << (L - 4)) <= 32) {
+        __syncwarp();
+    } else {
+        // immediate barrier ids, so the block reserves four barriers, not sixteen
+        static_assert(RowShape<L>::ROWS == 3, "three rows per block at L >= 10");
+        if (row == 0)
+            asm volatile("bar.sync 1, %0;" ::"n"(1 << (L - 4)) : "memory");
+        else if (row == 1)
+            asm volatile("bar.sync 2, %0;" ::"n"(1 << (L - 4)) : "memory");
+        else
+            asm volatile("bar.sync 3, %0;" ::"n"(1 << (L - 4)) : "memory");
+    }
+}
+
 // ================================================================ forward NTT
 
 template <int L>
@@ -77,11 +99,11 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS, RowShape<L>::MIN_BLOCKS)
             const uint32_t ws = ntt_swz_base(base, L, pass, t);
 #pragma unroll
             for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[r];
-            __syncthreads();
+            row_sync<L>(row);
             const uint32_t rs = ntt_swz_base(base, L, pass + 1, t);
 #pragma unroll
             for (int r = 0; r < kNttE; ++r) a[r] = sm[rs ^ ntt_swz_reg(L, pass + 1, r)];
-            __syncthreads();
+            row_sync<L>(row);
         }
     }
     if (active) {
@@ -327,11 +349,11 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
             const uint32_t ws = ntt_swz_base(base, L, pass, t);
 #pragma unroll
             for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[r];
-            __syncthreads();
+            row_sync<L>(brow);
             const uint32_t rs = ntt_swz_base(base, L, pass - 1, t);
 #pragma unroll
             for (int r = 0; r < kNttE; ++r) a[r] = sm[rs ^ ntt_swz_reg(L, pass - 1, r)];
-            __syncthreads();
+            row_sync<L>(brow);
         }
     }
     if (active) {
