@@ -53,6 +53,8 @@ WORKLOADS = {
     "d6": dict(kind="plain", file_bytes=53_248, desc="plain full flow d=6: 53,248 random bytes, 64x64 witness"),
     "d9": dict(kind="plain", file_bytes=1 << 20, desc="plain full flow d=9: 1 MiB random file, 512x512 witness"),
     "d11": dict(kind="plain", file_bytes=16 << 20, desc="plain full flow d=11: 16 MiB random file, 2048x2048 witness"),
+    "ringmul": dict(kind="ringmul", pairs=4096, n=512,
+                    desc="ring-mult microbench: 4,096 random degree-512 R_q pairs per step"),
 }
 KERNELS = ["file_hash", "unpack_witness", "gen_generators", "fold", "ntt_fwd", "mac", "mac_split", "finish"]
 
@@ -120,6 +122,20 @@ def workload_files(wl, rank: int = 0):
     return None
 
 
+def ring_pairs(wl, rank: int = 0):
+    """Two byte strings of pairs * n random Z_q elements (16-byte LE, below 2^112)."""
+    import numpy as np
+    from damascus000_gb300 import synth
+    nbytes = wl["pairs"] * wl["n"] * 16
+    out = []
+    for which in range(2):
+        raw, _ = synth.random_file(MASTER_SEED + 7919 * rank, nbytes, 30_000 + which)
+        w = np.frombuffer(raw, dtype=np.uint32).reshape(-1, 4).copy()
+        w[:, 3] &= 0xFFFF
+        out.append(w.tobytes())
+    return out[0], out[1]
+
+
 class ClockSampler:
     """Samples nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -184,6 +200,22 @@ def cpu_baseline(wl, budget_s: float = 15.0, threads: int = 0):
     from damascus000_gb300 import synth
     O.build()
     threads = threads or (os.cpu_count() or 1)
+    if wl["kind"] == "ringmul":
+        import concurrent.futures as cf
+        a, b = ring_pairs(wl, 0)
+        sz = wl["n"] * 16
+        done = 0
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            while time.perf_counter() - t0 < budget_s and done < wl["pairs"]:
+                k = min(threads * 4, wl["pairs"] - done)
+                list(ex.map(lambda i: O.negacyclic_multiply_bytes(a[i * sz:(i + 1) * sz], b[i * sz:(i + 1) * sz],
+                                                                  wl["n"]), range(done, done + k)))
+                done += k
+        el = time.perf_counter() - t0
+        return {"value": done / el, "unit": "products/s", "cores": threads, "kind": "port",
+                "sample": f"{done} degree-{wl['n']} negacyclic products by the oracle restatement (2n-point NTT "
+                          f"over 8 CRT primes + Garner CRT per product) on {threads} threads in {el:.1f} s"}
     if wl["kind"] == "plain":
         items = ((synth.random_file(MASTER_SEED, wl["file_bytes"], 1000 + i)) for i in range(64))
         what = f"full commit+prove of {wl['file_bytes']}-byte files"
@@ -231,6 +263,13 @@ def run_reference(args, wl):
 
 
 # ------------------------------------------------------------------ GPU
+# DRAM bytes per algorithmic byte of the forward transform: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum over 600 transform launches of the
+# serving stream (0.95-1.03 for the rings that dominate its time, below 1 for
+# small rings that stay in L2).
+NTT_TRAFFIC_RATIO = 0.988
+
+
 def roofline(stats):
     peak, src = read_peaks()
     live = {k: v for k, v in stats.items() if v}
@@ -240,8 +279,10 @@ def roofline(stats):
     n, ms, byts, ops = live[dom]
     achieved = byts / n / (ms / n / 1000.0) / 1e9
     total_ms = sum(v[1] for v in live.values())
+    traffic = byts / n * NTT_TRAFFIC_RATIO if dom == "ntt_fwd" else None
     return {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": src, "traffic": None,
+            "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+            "traffic_source": "ncu DRAM bytes / algorithmic bytes of this kernel" if traffic else None,
             "algo_bytes_per_launch": byts / n, "avg_launch_ms": ms / n, "share_of_kernel_time": ms / total_ms,
             "kernels": {k: {"launches": v[0], "ms": round(v[1], 4), "algo_bytes": v[2], "algo_ops": v[3]}
                         for k, v in live.items()}}
@@ -274,7 +315,60 @@ def run_gpu(args, wl):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/u128 integer",
             "data": "synthetic (seeded ChaCha20 files)"}
 
-    if wl["kind"] == "plain":
+    if wl["kind"] == "ringmul":
+        n, pairs = wl["n"], wl["pairs"]
+        a, b = ring_pairs(wl, rank)
+        da = torch.frombuffer(bytearray(a), dtype=torch.uint8).cuda()
+        db = torch.frombuffer(bytearray(b), dtype=torch.uint8).cuda()
+        dout = torch.empty_like(da)
+        pa = torch.frombuffer(bytearray(a), dtype=torch.uint8).pin_memory()
+        pb = torch.frombuffer(bytearray(b), dtype=torch.uint8).pin_memory()
+        po = torch.empty(len(a), dtype=torch.uint8).pin_memory()
+        torch.cuda.synchronize()
+        for _ in range(args.warmup):
+            ctx.ring_mul_batch_device(da.data_ptr(), db.data_ptr(), dout.data_ptr(), n, pairs)
+        ctx.set_profiling(True)
+        ctx.reset_stats()
+        clocks = ClockSampler(local)
+        clocks.start()
+        barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        ev0.record()
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            ctx.ring_mul_batch_device(da.data_ptr(), db.data_ptr(), dout.data_ptr(), n, pairs)
+        ev1.record()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        stats = {k: ctx.kernel_stat(k) for k in KERNELS + ["ring_mul"]}
+        ctx.set_profiling(False)
+        # device time of the products themselves (the per-step L2 flush excluded)
+        dev_ms = sum(v[1] for k, v in stats.items() if v and k in ("ntt_fwd", "ring_mul"))
+        total_ms = max_over_ranks(dev_ms)
+        value = world * args.steps * pairs / (total_ms / 1000.0)
+        lib = D.load()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.check(lib.damascus_ring_mul_batch(ctx.handle, ctypes.cast(pa.data_ptr(), ctypes.c_char_p),
+                                                  ctypes.cast(pb.data_ptr(), ctypes.c_char_p),
+                                                  ctypes.c_void_p(po.data_ptr()), n, pairs), "ring_mul_batch")
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+        ok = bytes(po.numpy()) == bytes(dout.cpu().numpy())
+        line.update({"metric": "ring-mults/s", "unit": "products/s", "value": value,
+                     "ms_per_step": total_ms / args.steps,
+                     "config": {"workload": wl["desc"], "pairs": pairs, "ring_degree": n,
+                                "parallelism": f"replicas x{world}",
+                                "l2": "flushed (256 MiB write) between timed steps", "host_and_device_agree": ok},
+                     "e2e": {"value": world * args.steps * pairs / e2e_s, "unit": "products/s",
+                             "h2d_bytes_per_step": 2 * len(a), "d2h_bytes_per_step": len(a)},
+                     "gpu_launches": int(sum(s[0] for s in stats.values() if s)),
+                     "roofline": roofline({k: v for k, v in stats.items() if k != "ring_mul"}), "clocks": clk})
+    elif wl["kind"] == "plain":
         file_bytes = wl["file_bytes"]
         nsteps = args.warmup + args.steps
         from damascus000_gb300 import synth

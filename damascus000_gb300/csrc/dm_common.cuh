@@ -39,7 +39,7 @@ constexpr int kLogMaxProverRing = 12;
 constexpr uint32_t kMaxRing = 1u << kLogMaxRing;
 // Deepest fold the prover accepts: the ring of degree 2^d must fit the transform
 // kernels (2^12) and N * n * q^2 < P / 2 must hold (2^248 < 2^268 at d = 12).
-constexpr int kMaxDepth = 11;
+constexpr int kMaxDepth = 12;
 // Minimum fold depth (src/utils/config.rs:5).
 constexpr int kMinDepth = 6;
 constexpr int kBytesPerCoeff = 13;

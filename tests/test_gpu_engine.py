@@ -71,8 +71,8 @@ def test_engine_failure_is_isolated(ctx):
     good = _files(92, [40_000, 70_000])
     with D.Engine(ctx) as eng:
         t0 = eng.submit(*good[0], EPOCH)
-        # 54.5 MB + 1 byte lands on depth 12, above the supported maximum
-        bad = eng.submit(bytes(2048 * 2048 * 13 + 1), bytes(32), EPOCH)
+        # 218 MB + 1 byte lands on depth 13, above the supported maximum (12)
+        bad = eng.submit(bytes(4096 * 4096 * 13 + 1), bytes(32), EPOCH)
         t1 = eng.submit(*good[1], EPOCH)
         p0 = eng.wait(t0)[0]
         with pytest.raises(D.DamascusError) as e:

@@ -272,6 +272,18 @@ def test_d11_prove_verifies_on_gpu(ctx):
     assert not ctx.verify(bytes(bad), EPOCH)
 
 
+@pytest.mark.slow
+def test_d12_prove_verifies_on_gpu(ctx):
+    """Depth 12 (4096 x 4096 witness, the largest ring the transform kernels take):
+    the commitment sums reach 2^248 in magnitude, inside the nine-prime CRT range."""
+    nbytes = 2048 * 2048 * 13 + 4096 * 1024  # just above the depth-11 capacity
+    data, seed = synth.random_file(12, nbytes, 0)
+    assert D.layout_for_byte_len(nbytes)[0] == 12
+    proof = ctx.prove(data, seed, EPOCH)
+    assert len(proof) == D.proof_size(nbytes)
+    assert ctx.verify(proof, EPOCH)
+
+
 # ------------------------------------------------------------------ reference FFI drop-ins
 def test_cuda_fold_batch_dropin():
     rng = random.Random(3)
