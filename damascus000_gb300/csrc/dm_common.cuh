@@ -22,8 +22,8 @@ namespace dm {
 
 // Module rank K of R_q^K (src/utils/config.rs:7).
 constexpr int kRank = 8;
-// NTT primes carrying the ring products: nine primes p < 2^30 with p = 1 mod 2^14
-// (their product P > 2^269 bounds every commitment sum up to depth 12).
+// NTT primes carrying the ring products: nine primes p < 2^28 with p = 1 mod 2^14
+// (their product P > 2^251 bounds every commitment sum, |X| < 2^248, up to depth 12).
 constexpr int kPrimes = 9;
 // Primes per thread block of the transforms (kPrimes / 3 blocks per polynomial).
 constexpr int kPrimesPerBlock = 3;
@@ -38,7 +38,7 @@ constexpr int kLogMaxRing = 13;
 constexpr int kLogMaxProverRing = 12;
 constexpr uint32_t kMaxRing = 1u << kLogMaxRing;
 // Deepest fold the prover accepts: the ring of degree 2^d must fit the transform
-// kernels (2^12) and N * n * q^2 < P / 2 must hold (2^248 < 2^268 at d = 12).
+// kernels (2^12) and N * n * q^2 < P / 2 must hold (2^248 < 2^250.9 at d = 12).
 constexpr int kMaxDepth = 12;
 // Minimum fold depth (src/utils/config.rs:5).
 constexpr int kMinDepth = 6;

@@ -4,13 +4,13 @@
 //    serde form of src/algebra/field.rs:112-129).  Multiplication is a 4x4 limb
 //    schoolbook product reduced with 2^112 = 75 (mod q), the same pseudo-Mersenne
 //    identity as field.rs:229-258.
-//  * Arithmetic modulo the nine NTT primes p < 2^30 (p = 1 mod 2^14) that carry
+//  * Arithmetic modulo the nine NTT primes p < 2^28 (p = 1 mod 2^14) that carry
 //    every ring product: Shoup products by constants give [0, 2p), so the
-//    transforms keep values in [0, 4p) < 2^32 between butterflies (Harvey's lazy
-//    butterflies), and products of two reduced residues fit 60 bits.
+//    transforms run four stages on values below 12p < 2^32 without reducing
+//    (lazy Harvey butterflies), and products of two reduced residues fit 56 bits.
 //  * Garner recombination of the nine residues into Z_q with a centred lift
-//    (the integer result of src/algebra/ntt.rs:372-427; P > 2^269 leaves room for
-//    any commitment sum up to depth 12).
+//    (the integer result of src/algebra/ntt.rs:372-427; P > 2^251 leaves room for
+//    any commitment sum, |X| < 2^248, up to depth 12).
 #pragma once
 
 #include "dm_common.cuh"
@@ -190,7 +190,7 @@ DM_HD uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
 // x mod p in [0, m) for x in [0, 2m): min(x, x - m) (x - m wraps when x < m).
 DM_HD uint32_t red_below(uint32_t x, uint32_t m) { return umin32(x, x - m); }
 
-// Shoup product x * w mod p in [0, 2p) for any x < 2^32, with w < p < 2^30 and
+// Shoup product x * w mod p in [0, 2p) for any x < 2^32, with w < p < 2^31 and
 // ws = floor(w * 2^32 / p): q = floor(x * ws / 2^32) is floor(x w / p) or one less.
 DM_HD uint32_t shoup_mul(uint32_t x, uint32_t w, uint32_t ws, uint32_t p) {
     const uint32_t q = mulhi32(x, ws);
@@ -275,7 +275,7 @@ DM_HD fq crt_to_fq(const uint32_t r[kPrimes], const PrimeConsts& pc, const CrtCo
         uint32_t t = r[i];  // [0, p), then [0, 2p) after each step
         DM_UNROLL
         for (int j = 0; j < i; ++j) {
-            // v_j < p_j < 2^30 < 2 p_i: one conditional subtraction gives v_j mod p_i
+            // v_j < p_j < 2^28 < 2 p_i: one conditional subtraction gives v_j mod p_i
             const uint32_t vj = red_below(v[j], p);
             const uint32_t tr = red_below(t, p);
             t = shoup_mul(tr + p - vj, cc.inv[j][i], cc.invs[j][i], p);

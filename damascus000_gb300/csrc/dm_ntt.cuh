@@ -37,7 +37,13 @@ DM_HD uint32_t ntt_place(int L, int pass, uint32_t t, uint32_t r) {
 // threads per row).
 DM_HD uint32_t ntt_swz(uint32_t i) { return i ^ ((i >> 4) & 31u); }
 
-// ---- Harvey butterflies on [0, 4p) (p < 2^30) ----
+// ---- lazy Harvey butterflies (p < 2^28) ----
+//
+// A forward butterfly with u < B and v = Shoup(x) < 2p gives u + v < B + 2p
+// and u - v + 2p < B + 2p, so values grow by 2p per stage.  Passes start from
+// [0, 4p) (the first: residues) or [0, 2p) (after one Shoup product by 1 per
+// register), so four stages stay below 12p < 2^32 for p < 2^28: no reduction
+// inside a pass, 5 instructions per butterfly (3 of them on the FMA pipe).
 //
 // Twiddle of the butterfly on register r in stage st of a pass:
 // k = 2^st + (j >> (bb + 1)) with j = place(t, r) and bb = L - 1 - st.  The
@@ -45,35 +51,65 @@ DM_HD uint32_t ntt_swz(uint32_t i) { return i ^ ((i >> 4) & 31u); }
 // k = 2^st + ((t >> lo) << (3 - rb)) + (r >> (rb + 1)): a stage needs only
 // 8 >> rb distinct twiddles per thread (15 per four-stage pass, not 32).
 
+// The 8 >> rb twiddles tw[kb ..] of a stage.  kb is a multiple of their count
+// (2^st >= 8 >> rb), so pairs are 16-byte aligned and load as one 16-byte word.
+DM_HD void ntt_load_twiddles(Tw w[8], const Tw* tw, uint32_t kb, int rb) {
+    const int ng = 8 >> rb;
+    if (ng == 1) {
+        w[0] = tw[kb];
+        return;
+    }
+#if defined(__CUDA_ARCH__)
+    const uint4* q = reinterpret_cast<const uint4*>(tw + kb);
+    DM_UNROLL
+    for (int g = 0; g < ng / 2; ++g) {
+        const uint4 v = q[g];
+        w[2 * g] = Tw{v.x, v.y};
+        w[2 * g + 1] = Tw{v.z, v.w};
+    }
+#else
+    for (int g = 0; g < ng; ++g) w[g] = tw[kb + g];
+#endif
+}
+
+// x mod p in [0, 2p) for any x < 2^32: Shoup product by 1 (one_s = floor(2^32 / p)).
+DM_HD uint32_t shoup_one(uint32_t x, uint32_t one_s, uint32_t p) { return x - mulhi32(x, one_s) * p; }
+
 // Forward (Cooley-Tukey) stages [4*pass, min(4*pass+4, L)) on the 16 registers
-// of thread t; inputs and outputs in [0, 4p).  tw: this prime's bit-reversed
+// of thread t; inputs below 4p (first pass) or any 32-bit values (later passes,
+// which reduce first), outputs below 12p.  tw: this prime's bit-reversed
 // twiddles psi^brv(k) with Shoup constants.
-DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p) {
+DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p, uint32_t one_s) {
     const int lo = ntt_pass_lo(L, pass);
     const int st_end = (4 * pass + 4 < L) ? 4 * pass + 4 : L;
     const uint32_t p2 = 2 * p;
     const uint32_t th = t >> lo;
+    if (pass > 0) {
+        DM_UNROLL
+        for (int r = 0; r < kNttE; ++r) a[r] = shoup_one(a[r], one_s, p);  // [0, 2p)
+    }
     DM_UNROLL
     for (int st = 4 * pass; st < st_end; ++st) {
         const int rb = L - 1 - st - lo;  // bit of the butterfly distance within r
         const uint32_t kb = (1u << st) + (th << (3 - rb));
         Tw w[8];
-        DM_UNROLL
-        for (int g = 0; g < (8 >> rb); ++g) w[g] = tw[kb + g];
+        ntt_load_twiddles(w, tw, kb, rb);
         DM_UNROLL
         for (int r = 0; r < kNttE; ++r) {
             if (r & (1 << rb)) continue;
-            const uint32_t u = red_below(a[r], p2);                           // [0, 2p)
+            const uint32_t u = a[r];
             const uint32_t v = shoup_mul(a[r | (1 << rb)], w[r >> (rb + 1)], p);  // [0, 2p)
-            a[r] = u + v;                                                    // [0, 4p)
-            a[r | (1 << rb)] = u - v + p2;                                   // (0, 4p)
+            a[r] = u + v;
+            a[r | (1 << rb)] = u - v + p2;
         }
     }
 }
+// Forward output (below 12p) to [0, p).
+DM_HD uint32_t ntt_fwd_final(uint32_t x, uint32_t one_s, uint32_t p) { return red_below(shoup_one(x, one_s, p), p); }
 
 // Inverse (Gentleman-Sande) stages of the same pass in reverse order (passes
 // from last to first, stages within a pass from the deepest up); inputs and
-// outputs in [0, 2p).
+// outputs in [0, 2p) (a sum doubles the bound, so it is reduced every stage).
 DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p) {
     const int lo = ntt_pass_lo(L, pass);
     const int st_end = (4 * pass + 4 < L) ? 4 * pass + 4 : L;
@@ -84,8 +120,7 @@ DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw
         const int rb = L - 1 - st - lo;
         const uint32_t kb = (1u << st) + (th << (3 - rb));
         Tw w[8];
-        DM_UNROLL
-        for (int g = 0; g < (8 >> rb); ++g) w[g] = tw[kb + g];
+        ntt_load_twiddles(w, tw, kb, rb);
         DM_UNROLL
         for (int r = 0; r < kNttE; ++r) {
             if (r & (1 << rb)) continue;
@@ -106,7 +141,8 @@ DM_HD uint32_t ntt_swz_base(uint32_t base, int L, int pass, uint32_t t) {
 DM_HD uint32_t ntt_swz_reg(int L, int pass, int r) { return ntt_swz((uint32_t)r << ntt_pass_lo(L, pass)); }
 
 // Whole transforms of one ring of size s = 2^L < 16 held in registers (one
-// thread per ring and prime): forward on [0, 4p), inverse on [0, 2p).
+// thread per ring and prime): forward from [0, 4p) (outputs below 10p), inverse
+// on [0, 2p).
 template <int L>
 DM_HD void ntt_fwd_small(uint32_t* a, const Tw* tw, uint32_t p) {
     constexpr int s = 1 << L;
@@ -118,7 +154,7 @@ DM_HD void ntt_fwd_small(uint32_t* a, const Tw* tw, uint32_t p) {
         for (int j = 0; j < s; ++j) {
             if (j & len) continue;
             const uint32_t k = (1u << st) + (uint32_t)(j >> (L - st));
-            const uint32_t u = red_below(a[j], p2);
+            const uint32_t u = a[j];  // below 4p + 2p st < 10p
             const uint32_t v = shoup_mul(a[j + len], tw[k], p);
             a[j] = u + v;
             a[j + len] = u - v + p2;

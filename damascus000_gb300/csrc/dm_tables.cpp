@@ -74,7 +74,7 @@ uint32_t generator_of(uint32_t p) {
 uint32_t inv_mod(uint32_t a, uint32_t p) { return pow_mod(a, p - 2, p); }
 uint32_t to_mont(uint32_t a, uint32_t p) { return (uint32_t)((((uint64_t)a) << 32) % p); }
 
-// Minimal little-endian 384-bit integer for the CRT constants (P < 2^270).
+// Minimal little-endian 384-bit integer for the CRT constants (P < 2^252).
 struct U384 {
     uint64_t w[6] = {0, 0, 0, 0, 0, 0};
 };
@@ -118,11 +118,11 @@ fq mod_q(const U384& a) {
 
 HostTables build() {
     HostTables t;
-    // the nine largest primes below 2^30 of the form k * 2^14 + 1
+    // the nine largest primes below 2^28 of the form k * 2^14 + 1
     int found = 0;
-    for (uint32_t k = ((1u << 30) - 1) >> 14; found < kPrimes && k > 0; --k) {
+    for (uint32_t k = ((1u << 28) - 1) >> 14; found < kPrimes && k > 0; --k) {
         const uint32_t p = (k << 14) + 1;
-        if (p < (1u << 30) && is_prime_u32(p)) t.primes[found++] = p;
+        if (p < (1u << 28) && is_prime_u32(p)) t.primes[found++] = p;
     }
     const size_t tab = (size_t)kPrimes * kMaxRing;
     t.fwd.resize(tab);

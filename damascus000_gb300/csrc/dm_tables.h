@@ -10,7 +10,7 @@
 namespace dm {
 
 struct HostTables {
-    uint32_t primes[kPrimes];  // the nine largest primes p < 2^30 with p = 1 mod 2^14
+    uint32_t primes[kPrimes];  // the nine largest primes p < 2^28 with p = 1 mod 2^14
     PrimeConsts pc;
     CrtConsts cc;
     // fwd[i * kMaxRing + k] = psi_i^brv13(k) mod p_i (psi_i a primitive

@@ -39,8 +39,10 @@ struct RowShape {
     static constexpr int THREADS = ROWS * T;
     static constexpr int PASSES = (L + 3) / 4;
     static constexpr size_t SMEM = PASSES > 1 ? (size_t)ROWS * (1u << L) * sizeof(uint32_t) : 0;
-    // resident blocks per SM the register budget is sized for (48 warps per SM)
-    static constexpr int MIN_BLOCKS = (48 * 32) / THREADS > 0 ? (48 * 32) / THREADS : 1;
+    // resident blocks per SM the register budget is sized for (32 warps per SM:
+    // measured faster than 48 or 64, the transform is latency-bound and uses the
+    // registers for loads in flight)
+    static constexpr int MIN_BLOCKS = (32 * 32) / THREADS > 0 ? (32 * 32) / THREADS : 1;
 };
 
 // Exchange barrier of one row: the row's 2^(L-4) threads are consecutive, so rows
@@ -94,7 +96,7 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS, RowShape<L>::MIN_BLOCKS)
     const uint32_t base = row << L;
 #pragma unroll
     for (int pass = 0; pass < S::PASSES; ++pass) {
-        ntt_fwd_pass(a, L, pass, t, tw, p);
+        ntt_fwd_pass(a, L, pass, t, tw, p, pc.one_s[pi]);
         if (pass + 1 < S::PASSES) {
             const uint32_t ws = ntt_swz_base(base, L, pass, t);
 #pragma unroll
@@ -107,9 +109,9 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS, RowShape<L>::MIN_BLOCKS)
         }
     }
     if (active) {
-        const uint32_t p2 = 2 * p;
+        const uint32_t one_s = pc.one_s[pi];
 #pragma unroll
-        for (int r = 0; r < kNttE; ++r) a[r] = red_below(red_below(a[r], p2), p);
+        for (int r = 0; r < kNttE; ++r) a[r] = ntt_fwd_final(a[r], one_s, p);
         // the last pass holds slots 16 t .. 16 t + 15
         uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * kNttE);
         dst[0] = make_uint4(a[0], a[1], a[2], a[3]);
@@ -135,12 +137,12 @@ __global__ void __launch_bounds__(128) ntt_fwd_small_kernel(JobList<NttJob> J, P
     for (int c = 0; c < s; ++c) a[c] = residue_lazy(ldq(jb.src + (poly << L), c), pc, pi);
     ntt_fwd_small<L>(a, fwd + pi * kMaxRing, p);
 #pragma unroll
-    for (int c = 0; c < s; ++c) jb.dst[((poly * kPrimes + pi) << L) + c] = red_below(red_below(a[c], 2 * p), p);
+    for (int c = 0; c < s; ++c) jb.dst[((poly * kPrimes + pi) << L) + c] = ntt_fwd_final(a[c], pc.one_s[pi], p);
 }
 
 // ================================================================ MAC
-// Residues are < p < 2^30, so a product fits 60 bits and 16 of them fit a
-// 64-bit word; block sums go into a 96-bit accumulator (64-bit low word + carry
+// Residues are < p < 2^28, so a product fits 56 bits and 16 of them fit a
+// 64-bit word with room to spare; block sums go into a 96-bit accumulator (64-bit low word + carry
 // count) reduced once per output.
 constexpr int kMacThreads = 128;
 
