@@ -45,7 +45,7 @@ EXPORTED_SYMBOLS = (
     "damascus_transcript_challenge", "damascus_coeff_count_for_byte_len", "damascus_layout_for_byte_len",
     "damascus_proof_size", "damascus_record_size", "damascus_statement_size", "damascus_prover_footprint",
     "damascus_file_id", "damascus_derive_generators", "damascus_commit_with_generators", "damascus_commit",
-    "damascus_ring_mul_batch", "damascus_ring_mul_batch_device",
+    "damascus_ring_mul_batch", "damascus_ring_mul_batch_device", "damascus_engine_profile",
     "damascus_prover_new", "damascus_prover_free", "damascus_prover_rounds_total",
     "damascus_prover_current_round", "damascus_prover_dimensions", "damascus_prover_statement",
     "damascus_prover_current_commitment", "damascus_prover_fold_round", "damascus_prover_final_opening",
@@ -162,6 +162,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_take", i32, vp, u64, vp, sz)
     sig("damascus_engine_drain", i32, vp)
     sig("damascus_engine_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64))
+    sig("damascus_engine_profile", i32, vp, P(ctypes.c_double), P(ctypes.c_double))
 
 
 # ------------------------------------------------------------------ encoding helpers
@@ -595,7 +596,11 @@ class Engine:
     def stats(self) -> dict:
         v = [ctypes.c_uint64() for _ in range(5)]
         self._ctx.check(self._lib.damascus_engine_stats(self._h, *[ctypes.byref(x) for x in v]), "engine stats")
-        return dict(zip(("completed", "failed", "waves", "launches", "peak_reserved"), (x.value for x in v)))
+        out = dict(zip(("completed", "failed", "waves", "launches", "peak_reserved"), (x.value for x in v)))
+        h, i = ctypes.c_double(), ctypes.c_double()
+        self._ctx.check(self._lib.damascus_engine_profile(self._h, ctypes.byref(h), ctypes.byref(i)), "engine profile")
+        out.update(host_stage_ms=h.value, gpu_idle_ms=i.value)
+        return out
 
     def prove_batch(self, items) -> list:
         """items: iterable of (data, seed_generators, epoch_seed); returns the proofs in order."""

@@ -605,6 +605,14 @@ int damascus_engine_stats(damascus_engine* e, uint64_t* completed, uint64_t* fai
     return DAMASCUS_OK;
 }
 
+int damascus_engine_profile(damascus_engine* e, double* host_stage_ms, double* gpu_idle_ms) {
+    if (!e) return DAMASCUS_EINVAL;
+    const EngineStats s = e->e->stats();
+    if (host_stage_ms) *host_stage_ms = s.host_stage_ms;
+    if (gpu_idle_ms) *gpu_idle_ms = s.gpu_idle_ms;
+    return DAMASCUS_OK;
+}
+
 // ------------------------------------------------------------------ reference FFI
 namespace {
 damascus_ctx* default_ctx() {

@@ -31,10 +31,18 @@ using namespace jobkit;
 constexpr int kGroups = kPrimes / kPrimesPerBlock;  // blocks per polynomial group
 constexpr int kRows = kRank * kPrimes;              // MAC rows per job (coordinate, prime)
 
+#ifndef DM_ROW_GROUP_THREADS
+#define DM_ROW_GROUP_THREADS 64  // threads per prime of a block for small rings (32 or 64)
+#endif
+static_assert(DM_ROW_GROUP_THREADS == 32 || DM_ROW_GROUP_THREADS == 64, "row barriers assume this");
+#ifndef DM_RESIDENT_WARPS
+#define DM_RESIDENT_WARPS 32
+#endif
+
 template <int L>
 struct RowShape {
     static constexpr int T = 1 << (L - 4);                   // threads per row
-    static constexpr int P = T >= 64 ? 1 : 64 / T;            // polynomials per block
+    static constexpr int P = T >= DM_ROW_GROUP_THREADS ? 1 : DM_ROW_GROUP_THREADS / T;  // polynomials per block
     static constexpr int ROWS = P * kPrimesPerBlock;          // rows per block
     static constexpr int THREADS = ROWS * T;
     static constexpr int PASSES = (L + 3) / 4;
@@ -42,7 +50,8 @@ struct RowShape {
     // resident blocks per SM the register budget is sized for (32 warps per SM:
     // measured faster than 48 or 64, the transform is latency-bound and uses the
     // registers for loads in flight)
-    static constexpr int MIN_BLOCKS = (32 * 32) / THREADS > 0 ? (32 * 32) / THREADS : 1;
+    static constexpr int MIN_BLOCKS =
+        (DM_RESIDENT_WARPS * 32) / THREADS > 0 ? (DM_RESIDENT_WARPS * 32) / THREADS : 1;
 };
 
 // Exchange barrier of one row: the row's 2^(L-4) threads are consecutive, so rows
@@ -57,7 +66,7 @@ DM_D void row_sync(uint32_t row) {
         __syncwarp();
     } else {
         // immediate barrier ids, so the block reserves four barriers, not sixteen
-        static_assert(RowShape<L>::ROWS == 3, "three rows per block at L >= 10");
+        static_assert(RowShape<L>::ROWS == 3, "rows above a warp: one polynomial (three rows) per block");
         if (row == 0)
             asm volatile("bar.sync 1, %0;" ::"n"(1 << (L - 4)) : "memory");
         else if (row == 1)

@@ -117,7 +117,7 @@ void CUDART_CB Engine::on_wave_done(void* arg) {
     {
         std::lock_guard<std::mutex> g(e->mu_);
         for (Request* r : w->reqs) e->host_q_.push_back(r);
-        e->inflight_waves_--;
+        if (--e->inflight_waves_ == 0) e->idle_since_ = Clock::now();
         e->wave_stream_busy_[w->stream_idx] = false;
     }
     e->work_cv_.notify_all();
@@ -160,6 +160,7 @@ void Engine::scheduler() {
                 continue;
             }
             r->state = Request::Active;
+            if (active_++ == 0) active_since_ = Clock::now();
             ready_.push_back(r);
             if (ctx_->reserved() > stats_.peak_reserved) stats_.peak_reserved = ctx_->reserved();
         }
@@ -168,7 +169,11 @@ void Engine::scheduler() {
         if (si < 0) continue;
         Wave* w = new Wave{this, {}, si};
         w->reqs.swap(ready_);
-        inflight_waves_++;
+        if (inflight_waves_++ == 0) {
+            const Clock::time_point now = Clock::now();
+            const Clock::time_point from = idle_since_ > active_since_ ? idle_since_ : active_since_;
+            if (now > from) stats_.gpu_idle_ms += std::chrono::duration<double, std::milli>(now - from).count();
+        }
         lk.unlock();
         cudaStream_t ws = wave_streams_[si];
         // admissions (allocations, file copies) on stream_ precede the wave's kernels
@@ -182,7 +187,7 @@ void Engine::scheduler() {
         if (n >= 0) e = cudaLaunchHostFunc(ws, on_wave_done, w);
         lk.lock();
         if (n < 0 || e != cudaSuccess) {
-            inflight_waves_--;
+            if (--inflight_waves_ == 0) idle_since_ = Clock::now();
             wave_stream_busy_[si] = false;
             std::vector<Request*> reqs = w->reqs;
             delete w;
@@ -211,20 +216,25 @@ void Engine::worker() {
             r = host_q_.front();
             host_q_.pop_front();
         }
+        const Clock::time_point t0 = Clock::now();
         const int rc = r->ps->complete_stage();
-        if (rc != kOk) {
-            r->err = r->ps->error();
-            r->err_code = rc;
-            finish_request(r);
-            continue;
-        }
-        if (r->ps->stage() == Stage::Done) {
-            r->ps->encode_proof(&r->proof);
+        if (rc == kOk && r->ps->stage() == Stage::Done) r->ps->encode_proof(&r->proof);
+        const double host_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+        if (rc != kOk || r->ps->stage() == Stage::Done) {
+            if (rc != kOk) {
+                r->err = r->ps->error();
+                r->err_code = rc;
+            }
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                stats_.host_stage_ms += host_ms;
+            }
             finish_request(r);
             continue;
         }
         {
             std::lock_guard<std::mutex> g(mu_);
+            stats_.host_stage_ms += host_ms;
             ready_.push_back(r);
         }
         sched_cv_.notify_one();
@@ -239,6 +249,7 @@ void Engine::finish_request(Request* r) {
         std::lock_guard<std::mutex> g(mu_);
         if (r->pinned_file) ctx_->put_pinned(r->pinned_file, r->pinned_bytes);
         r->pinned_file = nullptr;
+        if (r->state == Request::Active) --active_;
         r->state = ok ? Request::Done : Request::Failed;
         admit_blocked_ = false;
         if (ok) {

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -31,6 +32,8 @@ struct EngineStats {
     uint64_t submitted = 0, completed = 0, failed = 0, waves = 0, launches = 0;
     uint64_t bytes_done = 0;
     uint64_t peak_reserved = 0;
+    double host_stage_ms = 0;  // summed time of the host part of stages (all workers)
+    double gpu_idle_ms = 0;    // wall time with no wave in flight while requests were admitted
 };
 
 class Engine {
@@ -73,6 +76,8 @@ class Engine {
     std::map<uint64_t, std::unique_ptr<Request>> all_;
     uint64_t next_ticket_ = 1;
     int inflight_waves_ = 0;
+    int active_ = 0;  // admitted, not finished
+    std::chrono::steady_clock::time_point idle_since_{}, active_since_{};
     bool admit_blocked_ = false;  // the queue head waits for memory; cleared when a request finishes
     bool stop_ = false;
     EngineStats stats_;

@@ -188,6 +188,10 @@ int damascus_engine_take(damascus_engine* e, uint64_t ticket, uint8_t* proof_out
 int damascus_engine_drain(damascus_engine* e);
 int damascus_engine_stats(damascus_engine* e, uint64_t* completed, uint64_t* failed, uint64_t* waves,
                           uint64_t* launches, uint64_t* peak_reserved_bytes);
+/* Where the engine's time went: summed host time of the Fiat-Shamir stage parts
+ * (all workers), and wall time with no stage wave on the GPU while admitted
+ * requests were unfinished. */
+int damascus_engine_profile(damascus_engine* e, double* host_stage_ms, double* gpu_idle_ms);
 
 /* ------------------------------------------------------------------ reference FFI */
 /* Drop-in for the reference's own CUDA hooks, same signatures and argument
