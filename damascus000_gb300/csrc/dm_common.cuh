@@ -25,8 +25,14 @@ constexpr int kRank = 8;
 // NTT primes carrying the ring products: nine primes p < 2^28 with p = 1 mod 2^14
 // (their product P > 2^251 bounds every commitment sum, |X| < 2^248, up to depth 12).
 constexpr int kPrimes = 9;
-// Primes per thread block of the transforms (kPrimes / 3 blocks per polynomial).
-constexpr int kPrimesPerBlock = 3;
+// Primes per thread block of the transforms (kPrimes / kPrimesPerBlock blocks
+// per polynomial): 1 or 3.  One prime per block measured faster (smaller blocks,
+// more of them resident, their load phases overlap better).
+#ifndef DM_PRIMES_PER_BLOCK
+#define DM_PRIMES_PER_BLOCK 1
+#endif
+constexpr int kPrimesPerBlock = DM_PRIMES_PER_BLOCK;
+static_assert(kPrimesPerBlock == 1 || kPrimesPerBlock == 3, "transform block shapes");
 // The reference's eight CRT primes (src/utils/config.rs:9-18), used only by the
 // reference-compatible FFI convolution hook, whose caller passes them in.
 constexpr int kRefPrimes = 8;

@@ -13,9 +13,9 @@
 // Gentleman-Sande with zeta^-1 and a final n^-1.
 //
 // Block shape of the transforms: rows of 2^L residues (one polynomial under one
-// prime), 2^(L-4) threads per row holding 16 residues each in registers, three
-// primes of a polynomial per block (three blocks per polynomial), and for small
-// rings several polynomials per block (192 threads for L <= 10).
+// prime), 2^(L-4) threads per row holding 16 residues each in registers, one
+// prime per block (nine blocks per polynomial), and for small rings several
+// polynomials per block (64 threads up to L = 10, one row of 2^(L-4) above).
 #include <cuda_runtime.h>
 
 #include "dm_jobkit.cuh"
@@ -64,6 +64,8 @@ template <int L>
 DM_D void row_sync(uint32_t row) {
     if constexpr ((1 << (L - 4)) <= 32) {
         __syncwarp();
+    } else if constexpr (RowShape<L>::ROWS == 1) {
+        __syncthreads();
     } else {
         // immediate barrier ids, so the block reserves four barriers, not sixteen
         static_assert(RowShape<L>::ROWS == 3, "rows above a warp: one polynomial (three rows) per block");
