@@ -264,10 +264,10 @@ def run_reference(args, wl):
 
 # ------------------------------------------------------------------ GPU
 # DRAM bytes per algorithmic byte of the forward transform: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum over 600 transform launches of the
+# dram__bytes_read.sum + dram__bytes_write.sum over 1200 transform launches of the
 # serving stream (0.95-1.03 for the rings that dominate its time, below 1 for
 # small rings that stay in L2).
-NTT_TRAFFIC_RATIO = 0.988
+NTT_TRAFFIC_RATIO = 0.964
 
 
 def roofline(stats, measured_on="the timed steps"):

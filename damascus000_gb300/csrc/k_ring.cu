@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<Mac
     while (i < i1) {
         const uint32_t e = i + 16 < i1 ? i + 16 : i1;
         uint64_t b0 = 0, b1 = 0, bl = 0, br = 0;
-#pragma unroll 4
+#pragma unroll 8
         for (; i < e; ++i) {
             const uint2 gv = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
             const uint2 mv = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
