@@ -93,3 +93,21 @@ def test_engine_device_resident_submission(ctx):
         proofs = [eng.wait(t)[0] for t in ts]
     for (d, s), p in zip(files, proofs):
         assert p == ctx.prove(d, s, EPOCH)
+
+
+def test_engine_many_small_requests_and_profile(ctx):
+    """Many small requests (depths 6-8) in flight at once: every proof verifies,
+    sampled ones equal the plain path, and the engine accounts its time."""
+    rng = random.Random(17)
+    files = _files(94, [rng.randrange(1, 200_000) for _ in range(120)])
+    with D.Engine(ctx, max_waves=6) as eng:
+        tickets = [eng.submit(d, s, EPOCH) for d, s in files]
+        proofs = [eng.wait(t)[0] for t in tickets]
+        st = eng.stats()
+    assert st["completed"] == 120 and st["failed"] == 0
+    assert st["host_stage_ms"] > 0 and st["gpu_idle_ms"] >= 0
+    assert st["launches"] > st["waves"] > 0
+    for p in proofs:
+        assert ctx.verify(p, EPOCH)
+    for (d, s), p in list(zip(files, proofs))[::17]:
+        assert p == ctx.prove(d, s, EPOCH)
