@@ -25,14 +25,15 @@ constexpr int kRank = 8;
 // NTT primes carrying the ring products: nine primes p < 2^28 with p = 1 mod 2^14
 // (their product P > 2^251 bounds every commitment sum, |X| < 2^248, up to depth 12).
 constexpr int kPrimes = 9;
-// Primes per thread block of the transforms (kPrimes / kPrimesPerBlock blocks
-// per polynomial): 1 or 3.  One prime per block measured faster (smaller blocks,
-// more of them resident, their load phases overlap better).
-#ifndef DM_PRIMES_PER_BLOCK
-#define DM_PRIMES_PER_BLOCK 1
+// Primes per thread of the forward transforms (kPrimes / kPrimesPerThread blocks
+// per polynomial): 1 or 3.  Three read each 16-byte coefficient once for three
+// residue rows (a third of the load traffic through L1) but triple the unrolled
+// code; one measured faster (the larger kernel stalls on instruction fetch).
+#ifndef DM_PRIMES_PER_THREAD
+#define DM_PRIMES_PER_THREAD 1
 #endif
-constexpr int kPrimesPerBlock = DM_PRIMES_PER_BLOCK;
-static_assert(kPrimesPerBlock == 1 || kPrimesPerBlock == 3, "transform block shapes");
+constexpr int kPrimesPerThread = DM_PRIMES_PER_THREAD;
+static_assert(kPrimesPerThread == 1 || kPrimesPerThread == 3, "transform block shapes");
 // The reference's eight CRT primes (src/utils/config.rs:9-18), used only by the
 // reference-compatible FFI convolution hook, whose caller passes them in.
 constexpr int kRefPrimes = 8;
@@ -43,6 +44,9 @@ constexpr int kLogMaxRing = 13;
 // Largest ring degree of the commitment / fold kernels.
 constexpr int kLogMaxProverRing = 12;
 constexpr uint32_t kMaxRing = 1u << kLogMaxRing;
+// Last-pass twiddle tables: one block of 2^L entries per ring size 2^L, L = 4..12,
+// at offset 2^L - 16 within a prime's span.
+constexpr uint32_t kLastSpan = (2u << kLogMaxProverRing) - 16u;
 // Deepest fold the prover accepts: the ring of degree 2^d must fit the transform
 // kernels (2^12) and N * n * q^2 < P / 2 must hold (2^248 < 2^250.9 at d = 12).
 constexpr int kMaxDepth = 12;

@@ -248,6 +248,15 @@ DM_HD uint32_t residue_lazy(const fq& x, const PrimeConsts& c, int i) {
                        (uint64_t)x.w[3] * c.c3[i];
     return red64_lazy(t, c, i);
 }
+// The same residue below 8p with one multiply fewer, as a forward transform
+// input: the low word (< 2^32 < 16.01p) is brought below 4.01p by two
+// conditional subtractions instead of a Shoup product by 1.
+DM_HD uint32_t residue_fwd(const fq& x, const PrimeConsts& c, int i) {
+    const uint32_t p = c.p[i];
+    const uint64_t t = (uint64_t)x.w[0] + (uint64_t)x.w[1] * c.c1[i] + (uint64_t)x.w[2] * c.c2[i] +
+                       (uint64_t)x.w[3] * c.c3[i];
+    return shoup_mul((uint32_t)(t >> 32), c.c1[i], c.c1s[i], p) + red_below(red_below((uint32_t)t, 8 * p), 4 * p);
+}
 DM_HD uint32_t residue(const fq& x, const PrimeConsts& c, int i) {
     const uint32_t p = c.p[i];
     return red_below(red_below(residue_lazy(x, c, i), 2 * p), p);

@@ -19,6 +19,8 @@ struct DeviceTables {
     CrtConsts cc;
     const Tw* fwd = nullptr;  // [prime][kMaxRing]: psi^brv(k) with Shoup constants
     const Tw* inv = nullptr;  // inverses
+    const Tw* fwd_last = nullptr;  // [prime][kLastSpan]: last-pass order per ring size
+    const Tw* inv_last = nullptr;
 };
 
 // Uploads the tables to the current device and sets the kernels' shared-memory

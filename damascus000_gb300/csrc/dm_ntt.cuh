@@ -40,10 +40,12 @@ DM_HD uint32_t ntt_swz(uint32_t i) { return i ^ ((i >> 4) & 31u); }
 // ---- lazy Harvey butterflies (p < 2^28) ----
 //
 // A forward butterfly with u < B and v = Shoup(x) < 2p gives u + v < B + 2p
-// and u - v + 2p < B + 2p, so values grow by 2p per stage.  Passes start from
-// [0, 4p) (the first: residues) or [0, 2p) (after one Shoup product by 1 per
-// register), so four stages stay below 12p < 2^32 for p < 2^28: no reduction
-// inside a pass, 5 instructions per butterfly (3 of them on the FMA pipe).
+// and u - v + 2p < B + 2p, so values grow by 2p per stage.  Every pass starts
+// below 8p (the first from the lazy residues, later ones after one conditional
+// subtraction of 8p per register), so four stages stay below 16p < 2^32 for
+// p < 2^28: no reduction inside a pass, 5 instructions per butterfly (3 of them
+// multiplies), and the reduction between passes is an add and a min on the
+// integer ALU, leaving the multiplier pipe to the butterflies.
 //
 // Twiddle of the butterfly on register r in stage st of a pass:
 // k = 2^st + (j >> (bb + 1)) with j = place(t, r) and bb = L - 1 - st.  The
@@ -72,28 +74,63 @@ DM_HD void ntt_load_twiddles(Tw w[8], const Tw* tw, uint32_t kb, int rb) {
 #endif
 }
 
+// The last pass (lo = 0) gives every thread its own 8 >> rb twiddles per stage,
+// so in the natural order a warp's 16-byte loads stride 16 * (ng / 2) bytes and
+// touch twice or four times the sectors they use.  The last-pass table of ring
+// 2^L stores stage st's entries k = 2^st + th * ng + g at
+// 2^st + 2 * ((g >> 1) * 2^st / ng + th) + (g & 1): the pair (g, g + 1) of
+// consecutive threads th sits in consecutive 16-byte words.
+DM_HD uint32_t ntt_last_pos(int L, int st, uint32_t th, int g) {
+    const int ng = 8 >> (L - 1 - st);
+    if (ng == 1) return (1u << st) + th;
+    return (1u << st) + 2u * ((uint32_t)(g >> 1) * ((1u << st) / (uint32_t)ng) + th) + (uint32_t)(g & 1);
+}
+DM_HD void ntt_load_twiddles_last(Tw w[8], const Tw* twl, int L, int st, uint32_t th) {
+    const int ng = 8 >> (L - 1 - st);
+    if (ng == 1) {
+        w[0] = twl[(1u << st) + th];
+        return;
+    }
+#if defined(__CUDA_ARCH__)
+    const uint4* q = reinterpret_cast<const uint4*>(twl + (1u << st));
+    const uint32_t m = (1u << st) / (uint32_t)ng;
+    DM_UNROLL
+    for (int g = 0; g < ng / 2; ++g) {
+        const uint4 v = q[g * m + th];
+        w[2 * g] = Tw{v.x, v.y};
+        w[2 * g + 1] = Tw{v.z, v.w};
+    }
+#else
+    for (int g = 0; g < ng; ++g) w[g] = twl[ntt_last_pos(L, st, th, g)];
+#endif
+}
+
 // x mod p in [0, 2p) for any x < 2^32: Shoup product by 1 (one_s = floor(2^32 / p)).
 DM_HD uint32_t shoup_one(uint32_t x, uint32_t one_s, uint32_t p) { return x - mulhi32(x, one_s) * p; }
 
 // Forward (Cooley-Tukey) stages [4*pass, min(4*pass+4, L)) on the 16 registers
-// of thread t; inputs below 4p (first pass) or any 32-bit values (later passes,
-// which reduce first), outputs below 12p.  tw: this prime's bit-reversed
-// twiddles psi^brv(k) with Shoup constants.
-DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p, uint32_t one_s) {
+// of thread t; inputs below 8p (first pass) or below 16p (later passes, which
+// subtract 8p first), outputs below 16p.  tw: this prime's bit-reversed twiddles
+// psi^brv(k) with Shoup constants; twl: the same in the last-pass order of ring
+// 2^L (used by the pass with lo = 0).
+DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, const Tw* twl, uint32_t p) {
     const int lo = ntt_pass_lo(L, pass);
     const int st_end = (4 * pass + 4 < L) ? 4 * pass + 4 : L;
     const uint32_t p2 = 2 * p;
     const uint32_t th = t >> lo;
     if (pass > 0) {
+        const uint32_t p8 = 8 * p;
         DM_UNROLL
-        for (int r = 0; r < kNttE; ++r) a[r] = shoup_one(a[r], one_s, p);  // [0, 2p)
+        for (int r = 0; r < kNttE; ++r) a[r] = red_below(a[r], p8);  // [0, 8p)
     }
     DM_UNROLL
     for (int st = 4 * pass; st < st_end; ++st) {
         const int rb = L - 1 - st - lo;  // bit of the butterfly distance within r
-        const uint32_t kb = (1u << st) + (th << (3 - rb));
         Tw w[8];
-        ntt_load_twiddles(w, tw, kb, rb);
+        if (lo == 0)
+            ntt_load_twiddles_last(w, twl, L, st, th);
+        else
+            ntt_load_twiddles(w, tw, (1u << st) + (th << (3 - rb)), rb);
         DM_UNROLL
         for (int r = 0; r < kNttE; ++r) {
             if (r & (1 << rb)) continue;
@@ -104,13 +141,14 @@ DM_HD void ntt_fwd_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw
         }
     }
 }
-// Forward output (below 12p) to [0, p).
+// Forward output (any 32-bit value, in practice below 16p) to [0, p).
 DM_HD uint32_t ntt_fwd_final(uint32_t x, uint32_t one_s, uint32_t p) { return red_below(shoup_one(x, one_s, p), p); }
 
 // Inverse (Gentleman-Sande) stages of the same pass in reverse order (passes
 // from last to first, stages within a pass from the deepest up); inputs and
 // outputs in [0, 2p) (a sum doubles the bound, so it is reduced every stage).
-DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p) {
+// tw / twl: the inverse twiddles in natural and last-pass order.
+DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw* tw, const Tw* twl, uint32_t p) {
     const int lo = ntt_pass_lo(L, pass);
     const int st_end = (4 * pass + 4 < L) ? 4 * pass + 4 : L;
     const uint32_t p2 = 2 * p;
@@ -118,9 +156,11 @@ DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw
     DM_UNROLL
     for (int st = st_end - 1; st >= 4 * pass; --st) {
         const int rb = L - 1 - st - lo;
-        const uint32_t kb = (1u << st) + (th << (3 - rb));
         Tw w[8];
-        ntt_load_twiddles(w, tw, kb, rb);
+        if (lo == 0)
+            ntt_load_twiddles_last(w, twl, L, st, th);
+        else
+            ntt_load_twiddles(w, tw, (1u << st) + (th << (3 - rb)), rb);
         DM_UNROLL
         for (int r = 0; r < kNttE; ++r) {
             if (r & (1 << rb)) continue;
@@ -141,7 +181,7 @@ DM_HD uint32_t ntt_swz_base(uint32_t base, int L, int pass, uint32_t t) {
 DM_HD uint32_t ntt_swz_reg(int L, int pass, int r) { return ntt_swz((uint32_t)r << ntt_pass_lo(L, pass)); }
 
 // Whole transforms of one ring of size s = 2^L < 16 held in registers (one
-// thread per ring and prime): forward from [0, 4p) (outputs below 10p), inverse
+// thread per ring and prime): forward from [0, 8p) (outputs below 14p), inverse
 // on [0, 2p).
 template <int L>
 DM_HD void ntt_fwd_small(uint32_t* a, const Tw* tw, uint32_t p) {
@@ -154,7 +194,7 @@ DM_HD void ntt_fwd_small(uint32_t* a, const Tw* tw, uint32_t p) {
         for (int j = 0; j < s; ++j) {
             if (j & len) continue;
             const uint32_t k = (1u << st) + (uint32_t)(j >> (L - st));
-            const uint32_t u = a[j];  // below 4p + 2p st < 10p
+            const uint32_t u = a[j];  // below 8p + 2p st < 14p
             const uint32_t v = shoup_mul(a[j + len], tw[k], p);
             a[j] = u + v;
             a[j + len] = u - v + p2;

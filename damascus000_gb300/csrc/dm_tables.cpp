@@ -1,5 +1,7 @@
 #include "dm_tables.h"
 
+#include "dm_ntt.cuh"
+
 #include <mutex>
 
 namespace dm {
@@ -127,6 +129,8 @@ HostTables build() {
     const size_t tab = (size_t)kPrimes * kMaxRing;
     t.fwd.resize(tab);
     t.inv.resize(tab);
+    t.fwd_last.resize((size_t)kPrimes * kLastSpan);
+    t.inv_last.resize((size_t)kPrimes * kLastSpan);
     for (int i = 0; i < kPrimes; ++i) {
         const uint32_t p = t.primes[i];
         PrimeConsts& c = t.pc;
@@ -147,6 +151,17 @@ HostTables build() {
             const uint32_t z = pow_mod(psi, e, p), zi = pow_mod(psi_inv, e, p);
             t.fwd[at] = Tw{z, shoup_const(z, p)};
             t.inv[at] = Tw{zi, shoup_const(zi, p)};
+        }
+        for (int L = 4; L <= kLogMaxProverRing; ++L) {
+            const size_t off = (size_t)i * kLastSpan + (1u << L) - 16u;
+            for (int st = 4 * (ntt_pass_count(L) - 1); st < L; ++st) {
+                const uint32_t ng = 8u >> (L - 1 - st);
+                for (uint32_t j = 0; j < (1u << st); ++j) {
+                    const uint32_t pos = ntt_last_pos(L, st, j / ng, (int)(j % ng));
+                    t.fwd_last[off + pos] = t.fwd[(size_t)i * kMaxRing + (1u << st) + j];
+                    t.inv_last[off + pos] = t.inv[(size_t)i * kMaxRing + (1u << st) + j];
+                }
+            }
         }
         const uint32_t inv4 = inv_mod(4, p);
         for (int L = 0; L <= kLogMaxRing; ++L) {

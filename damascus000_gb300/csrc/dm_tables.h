@@ -17,6 +17,9 @@ struct HostTables {
     // 2*kMaxRing-th root of unity) with its Shoup constant floor(z * 2^32 / p);
     // inv holds the inverses.
     std::vector<Tw> fwd, inv;
+    // [prime][kLastSpan]: the same twiddles in the last-pass order of each ring
+    // size 2^L (L = 4..12, block at 2^L - 16; see ntt_last_pos).
+    std::vector<Tw> fwd_last, inv_last;
     // Final scale of an inverse transform of size 2^L: n^-1, and n^-1 / 4 for
     // the even/odd cross terms (with Shoup constants).
     uint32_t ninv[kPrimes][kLogMaxRing + 1], ninvs[kPrimes][kLogMaxRing + 1];

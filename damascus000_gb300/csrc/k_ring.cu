@@ -13,9 +13,11 @@
 // Gentleman-Sande with zeta^-1 and a final n^-1.
 //
 // Block shape of the transforms: rows of 2^L residues (one polynomial under one
-// prime), 2^(L-4) threads per row holding 16 residues each in registers, one
-// prime per block (nine blocks per polynomial), and for small rings several
-// polynomials per block (64 threads up to L = 10, one row of 2^(L-4) above).
+// prime), 2^(L-4) threads per polynomial holding 16 residues of each row in
+// registers.  A forward-transform thread carries three primes (three blocks per
+// polynomial: every coefficient is read once per three residues); an inverse
+// thread one.  Small rings put several polynomials in a block (64 threads up to
+// L = 10, 2^(L-4) above).
 #include <cuda_runtime.h>
 
 #include "dm_jobkit.cuh"
@@ -28,107 +30,130 @@ namespace {
 
 using namespace jobkit;
 
-constexpr int kGroups = kPrimes / kPrimesPerBlock;  // blocks per polynomial group
-constexpr int kRows = kRank * kPrimes;              // MAC rows per job (coordinate, prime)
+constexpr int kGroups = kPrimes / kPrimesPerThread;  // forward-transform blocks per polynomial group
+constexpr int kRows = kRank * kPrimes;               // MAC rows per job (coordinate, prime)
 
 #ifndef DM_ROW_GROUP_THREADS
-#define DM_ROW_GROUP_THREADS 64  // threads per prime of a block for small rings (32 or 64)
+#define DM_ROW_GROUP_THREADS 64  // threads per block for small rings (32 or 64)
 #endif
 static_assert(DM_ROW_GROUP_THREADS == 32 || DM_ROW_GROUP_THREADS == 64, "row barriers assume this");
 #ifndef DM_RESIDENT_WARPS
 #define DM_RESIDENT_WARPS 32
 #endif
+#ifndef DM_FWD_RESIDENT_WARPS
+#define DM_FWD_RESIDENT_WARPS (DM_RESIDENT_WARPS / kPrimesPerThread > 16 ? DM_RESIDENT_WARPS / kPrimesPerThread : 16)
+#endif
 
+// Block shape of the inverse transforms: one row (polynomial under one prime)
+// of 2^(L-4) threads, several rows per block for small rings.
 template <int L>
 struct RowShape {
     static constexpr int T = 1 << (L - 4);                   // threads per row
-    static constexpr int P = T >= DM_ROW_GROUP_THREADS ? 1 : DM_ROW_GROUP_THREADS / T;  // polynomials per block
-    static constexpr int ROWS = P * kPrimesPerBlock;          // rows per block
+    static constexpr int P = T >= DM_ROW_GROUP_THREADS ? 1 : DM_ROW_GROUP_THREADS / T;  // rows per block
+    static constexpr int ROWS = P;
     static constexpr int THREADS = ROWS * T;
     static constexpr int PASSES = (L + 3) / 4;
     static constexpr size_t SMEM = PASSES > 1 ? (size_t)ROWS * (1u << L) * sizeof(uint32_t) : 0;
-    // resident blocks per SM the register budget is sized for (32 warps per SM:
-    // measured faster than 48 or 64, the transform is latency-bound and uses the
-    // registers for loads in flight)
-    static constexpr int MIN_BLOCKS =
-        (DM_RESIDENT_WARPS * 32) / THREADS > 0 ? (DM_RESIDENT_WARPS * 32) / THREADS : 1;
 };
 
-// Exchange barrier of one row: the row's 2^(L-4) threads are consecutive, so rows
-// of up to 32 threads sit inside one warp (a warp barrier suffices) and larger
-// rows own whole warps and a named barrier (id row + 1, counted in threads).
-// Rows then move through their passes independently instead of the whole block
-// waiting at each exchange.  Every thread of a row, active or not, runs the same
-// passes and so the same barriers.
+// Block shape of the forward transforms: P polynomials, each held by 2^(L-4)
+// threads with kPrimesPerThread residue rows per thread; shared memory holds
+// kPrimesPerThread x P rows, prime-major, so each prime's rows sit together as
+// in a one-prime block.
 template <int L>
-DM_D void row_sync(uint32_t row) {
+struct FwdShape {
+    static constexpr int T = 1 << (L - 4);
+    static constexpr int P = T >= DM_ROW_GROUP_THREADS ? 1 : DM_ROW_GROUP_THREADS / T;
+    static constexpr int THREADS = P * T;
+    static constexpr int PASSES = (L + 3) / 4;
+    static constexpr size_t SMEM = PASSES > 1 ? (size_t)kPrimesPerThread * P * (1u << L) * sizeof(uint32_t) : 0;
+    // resident blocks per SM the register budget is sized for (32 warps per SM
+    // with one prime per thread: measured faster than 48 or 64; the registers
+    // hold loads in flight)
+    static constexpr int MIN_BLOCKS =
+        (DM_FWD_RESIDENT_WARPS * 32) / THREADS > 0 ? (DM_FWD_RESIDENT_WARPS * 32) / THREADS : 1;
+};
+
+// Exchange barrier of one row group: a group of 2^(L-4) consecutive threads that
+// fits one warp needs only a warp barrier; larger groups are the whole block.
+// Every thread of a group, active or not, runs the same passes and so the same
+// barriers.
+template <int L>
+DM_D void row_sync() {
     if constexpr ((1 << (L - 4)) <= 32) {
         __syncwarp();
-    } else if constexpr (RowShape<L>::ROWS == 1) {
-        __syncthreads();
     } else {
-        // immediate barrier ids, so the block reserves four barriers, not sixteen
-        static_assert(RowShape<L>::ROWS == 3, "rows above a warp: one polynomial (three rows) per block");
-        if (row == 0)
-            asm volatile("bar.sync 1, %0;" ::"n"(1 << (L - 4)) : "memory");
-        else if (row == 1)
-            asm volatile("bar.sync 2, %0;" ::"n"(1 << (L - 4)) : "memory");
-        else
-            asm volatile("bar.sync 3, %0;" ::"n"(1 << (L - 4)) : "memory");
+        static_assert(RowShape<L>::P == 1 && FwdShape<L>::P == 1, "groups above a warp fill their block");
+        __syncthreads();
     }
 }
 
 // ================================================================ forward NTT
 
 template <int L>
-__global__ void __launch_bounds__(RowShape<L>::THREADS, RowShape<L>::MIN_BLOCKS)
-    ntt_fwd_kernel(JobList<NttJob> J, PrimeConsts pc, const Tw* __restrict__ fwd) {
-    using S = RowShape<L>;
+__global__ void __launch_bounds__(FwdShape<L>::THREADS, FwdShape<L>::MIN_BLOCKS)
+    ntt_fwd_kernel(JobList<NttJob> J, PrimeConsts pc, const Tw* __restrict__ fwd, const Tw* __restrict__ fwd_last) {
+    using S = FwdShape<L>;
+    constexpr int K = kPrimesPerThread;
     extern __shared__ __align__(16) uint32_t sm[];
     const NttJob jb = J.j[find_job(J)];
     const uint32_t lcta = blockIdx.x - jb.cta0;
-    const uint32_t grp = lcta / kGroups, third = lcta % kGroups;
-    const uint32_t row = threadIdx.x / S::T;
+    const uint32_t grp = lcta / kGroups, pi0 = (lcta % kGroups) * K;
+    const uint32_t prow = threadIdx.x / S::T;  // polynomial within the block
     const uint32_t t = threadIdx.x % S::T;
-    const uint64_t poly = (uint64_t)grp * S::P + row / kPrimesPerBlock;
-    const uint32_t pi = third * kPrimesPerBlock + row % kPrimesPerBlock;
+    const uint64_t poly = (uint64_t)grp * S::P + prow;
     const bool active = poly < jb.npolys;
-    const uint32_t p = pc.p[pi];
-    const Tw* tw = fwd + pi * kMaxRing;
-    uint32_t a[kNttE];
+    uint32_t a[K][kNttE];
     if (active) {
         const uint4* src = jb.src + (poly << L);
 #pragma unroll
-        for (int r = 0; r < kNttE; ++r) a[r] = residue_lazy(ldq(src, ntt_place(L, 0, t, r)), pc, pi);
+        for (int r = 0; r < kNttE; ++r) {
+            const fq x = ldq(src, ntt_place(L, 0, t, r));
+#pragma unroll
+            for (int k = 0; k < K; ++k) a[k][r] = residue_fwd(x, pc, pi0 + k);
+        }
     } else {
 #pragma unroll
-        for (int r = 0; r < kNttE; ++r) a[r] = 0;
+        for (int k = 0; k < K; ++k)
+#pragma unroll
+            for (int r = 0; r < kNttE; ++r) a[k][r] = 0;
     }
-    const uint32_t base = row << L;
 #pragma unroll
     for (int pass = 0; pass < S::PASSES; ++pass) {
-        ntt_fwd_pass(a, L, pass, t, tw, p, pc.one_s[pi]);
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            ntt_fwd_pass(a[k], L, pass, t, fwd + (pi0 + k) * kMaxRing,
+                         fwd_last + (pi0 + k) * kLastSpan + (1u << L) - 16u, pc.p[pi0 + k]);
         if (pass + 1 < S::PASSES) {
-            const uint32_t ws = ntt_swz_base(base, L, pass, t);
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[r];
-            row_sync<L>(row);
-            const uint32_t rs = ntt_swz_base(base, L, pass + 1, t);
+            for (int k = 0; k < K; ++k) {
+                const uint32_t ws = ntt_swz_base((uint32_t)(k * S::P + prow) << L, L, pass, t);
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) a[r] = sm[rs ^ ntt_swz_reg(L, pass + 1, r)];
-            row_sync<L>(row);
+                for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[k][r];
+            }
+            row_sync<L>();
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const uint32_t rs = ntt_swz_base((uint32_t)(k * S::P + prow) << L, L, pass + 1, t);
+#pragma unroll
+                for (int r = 0; r < kNttE; ++r) a[k][r] = sm[rs ^ ntt_swz_reg(L, pass + 1, r)];
+            }
+            row_sync<L>();
         }
     }
     if (active) {
-        const uint32_t one_s = pc.one_s[pi];
 #pragma unroll
-        for (int r = 0; r < kNttE; ++r) a[r] = ntt_fwd_final(a[r], one_s, p);
-        // the last pass holds slots 16 t .. 16 t + 15
-        uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * kNttE);
-        dst[0] = make_uint4(a[0], a[1], a[2], a[3]);
-        dst[1] = make_uint4(a[4], a[5], a[6], a[7]);
-        dst[2] = make_uint4(a[8], a[9], a[10], a[11]);
-        dst[3] = make_uint4(a[12], a[13], a[14], a[15]);
+        for (int k = 0; k < K; ++k) {
+            const uint32_t pi = pi0 + k, p = pc.p[pi], one_s = pc.one_s[pi];
+#pragma unroll
+            for (int r = 0; r < kNttE; ++r) a[k][r] = ntt_fwd_final(a[k][r], one_s, p);
+            // the last pass holds slots 16 t .. 16 t + 15
+            uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * kNttE);
+            dst[0] = make_uint4(a[k][0], a[k][1], a[k][2], a[k][3]);
+            dst[1] = make_uint4(a[k][4], a[k][5], a[k][6], a[k][7]);
+            dst[2] = make_uint4(a[k][8], a[k][9], a[k][10], a[k][11]);
+            dst[3] = make_uint4(a[k][12], a[k][13], a[k][14], a[k][15]);
+        }
     }
 }
 
@@ -145,7 +170,7 @@ __global__ void __launch_bounds__(128) ntt_fwd_small_kernel(JobList<NttJob> J, P
     const uint32_t p = pc.p[pi];
     uint32_t a[s];
 #pragma unroll
-    for (int c = 0; c < s; ++c) a[c] = residue_lazy(ldq(jb.src + (poly << L), c), pc, pi);
+    for (int c = 0; c < s; ++c) a[c] = residue_fwd(ldq(jb.src + (poly << L), c), pc, pi);
     ntt_fwd_small<L>(a, fwd + pi * kMaxRing, p);
 #pragma unroll
     for (int c = 0; c < s; ++c) jb.dst[((poly * kPrimes + pi) << L) + c] = ntt_fwd_final(a[c], pc.one_s[pi], p);
@@ -302,6 +327,56 @@ __global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<Mac
     jb.out2[(((uint64_t)part * kRows + kp) << (L - 1)) + i2] = red96(hr, lr, pc, pi);
 }
 
+// The same with two slot pairs per thread (16-byte loads of four slots), L >= 3.
+__global__ void __launch_bounds__(kMacThreads, 8) mac_split4_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+    const MacJobX jb = J.j[find_job(J)];
+    const uint32_t hq = 1u << (L - 2);  // slot quads
+    const uint32_t nblk = slot_block_count(hq);
+    uint32_t c = blockIdx.x - jb.cta0;
+    const uint32_t blk = c % nblk;
+    c /= nblk;
+    const uint32_t kp = c % kRows;
+    const uint32_t part = c / kRows;
+    const uint32_t i4 = blk * kMacThreads + threadIdx.x;
+    if (i4 >= hq) return;
+    const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
+    const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
+    const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
+    const uint32_t p = pc.p[pi];
+    const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
+    const uint64_t mstride = (uint64_t)kPrimes << L;
+    const uint32_t* g = jb.G + ((((uint64_t)jb.g_base * kRank + k) * kPrimes + pi) << L) + 4 * i4;
+    const uint32_t* m = jb.M + (((uint64_t)jb.m_base * kPrimes + pi) << L) + 4 * i4;
+    uint64_t lo[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // slots 0..3, then L and R of pairs 0, 1
+    uint32_t hi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t i = i0;
+    while (i < i1) {
+        const uint32_t e = i + 16 < i1 ? i + 16 : i1;
+        uint64_t b[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll 4
+        for (; i < e; ++i) {
+            const uint4 gv = __ldg(reinterpret_cast<const uint4*>(g + i * gstride));
+            const uint4 mv = __ldg(reinterpret_cast<const uint4*>(m + i * mstride));
+            b[0] += mul64(gv.x, mv.x);
+            b[1] += mul64(gv.y, mv.y);
+            b[2] += mul64(gv.z, mv.z);
+            b[3] += mul64(gv.w, mv.w);
+            b[4] += mul64(red_below(gv.x + p - gv.y, p), red_below(mv.x + mv.y, p));
+            b[5] += mul64(red_below(gv.x + gv.y, p), red_below(mv.x + p - mv.y, p));
+            b[6] += mul64(red_below(gv.z + p - gv.w, p), red_below(mv.z + mv.w, p));
+            b[7] += mul64(red_below(gv.z + gv.w, p), red_below(mv.z + p - mv.w, p));
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc96(lo[q], hi[q], b[q]);
+    }
+    *reinterpret_cast<uint4*>(jb.out0 + (((uint64_t)part * kRows + kp) << L) + 4 * i4) =
+        make_uint4(red96(hi[0], lo[0], pc, pi), red96(hi[1], lo[1], pc, pi), red96(hi[2], lo[2], pc, pi),
+                   red96(hi[3], lo[3], pc, pi));
+    const uint64_t oh = (((uint64_t)part * kRows + kp) << (L - 1)) + 2 * i4;
+    *reinterpret_cast<uint2*>(jb.out1 + oh) = make_uint2(red96(hi[4], lo[4], pc, pi), red96(hi[6], lo[6], pc, pi));
+    *reinterpret_cast<uint2*>(jb.out2 + oh) = make_uint2(red96(hi[5], lo[5], pc, pi), red96(hi[7], lo[7], pc, pi));
+}
+
 // ================================================================ finish
 struct FinishConsts {
     uint32_t f[kPrimes], fs[kPrimes];  // final inverse-transform scale and its Shoup constant
@@ -320,7 +395,7 @@ DM_D uint32_t twist(uint32_t x, uint32_t mode, uint32_t idx, const Tw* fwd, cons
 template <int L>
 __global__ void __launch_bounds__(RowShape<L>::THREADS)
     inv_rows_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
-                    const Tw* __restrict__ fwd, const Tw* __restrict__ inv) {
+                    const Tw* __restrict__ fwd, const Tw* __restrict__ inv, const Tw* __restrict__ inv_last) {
     using S = RowShape<L>;
     constexpr uint32_t s = 1u << L;
     extern __shared__ __align__(16) uint32_t sm[];
@@ -354,19 +429,20 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
         }
     }
     const Tw* tw = inv + pi * kMaxRing;
+    const Tw* twl = inv_last + pi * kLastSpan + (1u << L) - 16u;
     const uint32_t base = brow << L;
 #pragma unroll
     for (int pass = S::PASSES - 1; pass >= 0; --pass) {
-        ntt_inv_pass(a, L, pass, t, tw, p);
+        ntt_inv_pass(a, L, pass, t, tw, twl, p);
         if (pass > 0) {
             const uint32_t ws = ntt_swz_base(base, L, pass, t);
 #pragma unroll
             for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[r];
-            row_sync<L>(brow);
+            row_sync<L>();
             const uint32_t rs = ntt_swz_base(base, L, pass - 1, t);
 #pragma unroll
             for (int r = 0; r < kNttE; ++r) a[r] = sm[rs ^ ntt_swz_reg(L, pass - 1, r)];
-            row_sync<L>(brow);
+            row_sync<L>();
         }
     }
     if (active) {
@@ -446,12 +522,12 @@ cudaError_t ntt_launch_L(const DeviceTables& T, JobList<NttJob>& JL, NttJob* job
         if (!ctas) return cudaSuccess;
         ntt_fwd_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, T.fwd);
     } else {
-        using S = RowShape<L>;
+        using S = FwdShape<L>;
         const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
             return ((uint64_t)(j.npolys + S::P - 1) / S::P) * kGroups;
         });
         if (!ctas) return cudaSuccess;
-        ntt_fwd_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.fwd);
+        ntt_fwd_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.fwd, T.fwd_last);
     }
     return cudaGetLastError();
 }
@@ -471,7 +547,7 @@ cudaError_t inv_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJ
             return ((uint64_t)j.rows + S::ROWS - 1) / S::ROWS;
         });
         if (!ctas) return cudaSuccess;
-        inv_rows_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, plain, split, T.fwd, T.inv);
+        inv_rows_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, plain, split, T.fwd, T.inv, T.inv_last);
     }
     return cudaGetLastError();
 }
@@ -499,11 +575,11 @@ cudaError_t upload_tables(DeviceTables* out) {
     const HostTables& H = host_tables();
     out->pc = H.pc;
     out->cc = H.cc;
-    const size_t bytes = sizeof(Tw) * H.fwd.size();
-    const std::vector<Tw>* src[2] = {&H.fwd, &H.inv};
-    Tw* dst[2] = {nullptr, nullptr};
+    const std::vector<Tw>* src[4] = {&H.fwd, &H.inv, &H.fwd_last, &H.inv_last};
+    Tw* dst[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
+        const size_t bytes = sizeof(Tw) * src[i]->size();
         e = cudaMalloc(&dst[i], bytes);
         if (e == cudaSuccess) e = cudaMemcpy(dst[i], src[i]->data(), bytes, cudaMemcpyHostToDevice);
     }
@@ -514,13 +590,15 @@ cudaError_t upload_tables(DeviceTables* out) {
     }
     out->fwd = dst[0];
     out->inv = dst[1];
+    out->fwd_last = dst[2];
+    out->inv_last = dst[3];
     return cudaSuccess;
 }
 
 void free_tables(DeviceTables* t) {
-    for (const Tw* d : {t->fwd, t->inv})
+    for (const Tw* d : {t->fwd, t->inv, t->fwd_last, t->inv_last})
         if (d) cudaFree(const_cast<Tw*>(d));
-    t->fwd = t->inv = nullptr;
+    t->fwd = t->inv = t->fwd_last = t->inv_last = nullptr;
 }
 
 cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st) {
@@ -550,9 +628,12 @@ cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, 
     return cudaGetLastError();
 }
 
+cudaError_t launch_mac_split4(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st);
+
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs || (split && L == 0)) return cudaErrorInvalidValue;
+    if (split && L >= 3) return launch_mac_split4(T, jobs, n, L, st);
     JobList<MacJobX> JL;
     const uint32_t slots = split ? (1u << (L - 1)) : (1u << L);
     uint64_t total = 0;
@@ -567,6 +648,22 @@ cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_
         mac_split_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
     else
         mac_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+    return cudaGetLastError();
+}
+
+// Split MAC with four slots per thread (L >= 3).
+cudaError_t launch_mac_split4(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st) {
+    JobList<MacJobX> JL;
+    const uint32_t quads = 1u << (L - 2);
+    uint64_t total = 0;
+    JL.n = n;
+    for (int i = 0; i < n; ++i) {
+        jobs[i].cta0 = (uint32_t)total;
+        JL.j[i] = jobs[i];
+        total += (uint64_t)((quads + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
+    }
+    const unsigned bx = quads < (uint32_t)kMacThreads ? quads : kMacThreads;
+    mac_split4_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
     return cudaGetLastError();
 }
 

@@ -347,7 +347,7 @@ void ProofState::plan_stage(Plan& P) {
         P.fold.push_back(FoldJob{cs(kCt), cs(kC), cs(kL), cs(kR), xi_, x_, (uint64_t)kRank * s, kCombine, 0});
         P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
         P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
-        parts_ = mac_parts(h, h);
+        parts_ = mac_parts(L >= 3 ? h / 2 : h, h);  // the split MAC runs four slots per thread from L = 3
         uint32_t* pchk = part;
         uint32_t* plp = part + (size_t)parts_ * kRows * s;
         uint32_t* prp = plp + (size_t)parts_ * kRows * h;
