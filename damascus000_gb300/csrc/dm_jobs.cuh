@@ -30,6 +30,10 @@ struct MacJobX {
     uint32_t* out2;  // split: rp partials
     uint32_t g_base, m_base, count, parts;
     uint32_t cta0;
+    // Triple MAC only: 0 = column pairs (i, i + count); otherwise pairs
+    // (i, i + pair) for i < count <= pair with every witness column from `pair`
+    // on zero, so the witness is read at i only and R is zero.
+    uint32_t pair;
 };
 
 // ---- sum partials, inverse NTT, CRT to Z_q, optional compare (all jobs share L) ----

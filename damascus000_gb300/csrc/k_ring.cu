@@ -228,9 +228,11 @@ __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> 
     jb.out0[(((uint64_t)part * kRows + kp) << L) + slot] = red96(hi, lo, pc, pi);
 }
 
-// Triple MAC over h = count column pairs (i, i + h): one read of every generator
-// column gives the full sum (out0), L = sum G[i+h] M[i] (out1) and
-// R = sum G[i] M[i+h] (out2).  Thread per slot pair (8-byte loads), L >= 1.
+// Triple MAC over column pairs (i, i + h): one read of every generator column
+// gives the full sum (out0), L = sum G[i+h] M[i] (out1) and R = sum G[i] M[i+h]
+// (out2).  h = count, or h = pair when the witness columns from h on are known
+// zero: then i runs over the count < h leading columns only, the witness is read
+// at i alone and R is zero.  Thread per slot pair (8-byte loads), L >= 1.
 __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
     const MacJobX jb = J.j[find_job(J)];
     const uint32_t sp = 1u << (L - 1);
@@ -243,9 +245,9 @@ __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<Ma
     const uint32_t i2 = blk * kMacThreads + threadIdx.x;
     if (i2 >= sp) return;
     const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
-    const uint32_t h = jb.count;
-    const uint32_t i0 = (uint32_t)((uint64_t)h * part / jb.parts);
-    const uint32_t i1 = (uint32_t)((uint64_t)h * (part + 1) / jb.parts);
+    const uint32_t h = jb.pair ? jb.pair : jb.count;
+    const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
+    const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
     const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
     const uint64_t mstride = (uint64_t)kPrimes << L;
     const uint32_t* g = jb.G + ((((uint64_t)k) * kPrimes + pi) << L) + 2 * i2;
@@ -254,24 +256,43 @@ __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<Ma
     uint64_t lo[6] = {0, 0, 0, 0, 0, 0};  // (full, L, R) x (even, odd slot)
     uint32_t hi[6] = {0, 0, 0, 0, 0, 0};
     uint32_t i = i0;
-    while (i < i1) {
-        const uint32_t e = i + 8 < i1 ? i + 8 : i1;  // <= 16 products per block sum
-        uint64_t b[6] = {0, 0, 0, 0, 0, 0};
+    if (jb.pair) {
+        while (i < i1) {
+            const uint32_t e = i + 16 < i1 ? i + 16 : i1;  // <= 16 products per block sum
+            uint64_t b[4] = {0, 0, 0, 0};
 #pragma unroll 4
-        for (; i < e; ++i) {
-            const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
-            const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
-            const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
-            const uint2 mr = __ldg(reinterpret_cast<const uint2*>(m + i * mstride + mh));
-            b[0] += mul64(gl.x, ml.x) + mul64(gr.x, mr.x);
-            b[1] += mul64(gl.y, ml.y) + mul64(gr.y, mr.y);
-            b[2] += mul64(gr.x, ml.x);
-            b[3] += mul64(gr.y, ml.y);
-            b[4] += mul64(gl.x, mr.x);
-            b[5] += mul64(gl.y, mr.y);
-        }
+            for (; i < e; ++i) {
+                const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
+                const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
+                const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
+                b[0] += mul64(gl.x, ml.x);
+                b[1] += mul64(gl.y, ml.y);
+                b[2] += mul64(gr.x, ml.x);
+                b[3] += mul64(gr.y, ml.y);
+            }
 #pragma unroll
-        for (int q = 0; q < 6; ++q) acc96(lo[q], hi[q], b[q]);
+            for (int q = 0; q < 4; ++q) acc96(lo[q], hi[q], b[q]);
+        }
+    } else {
+        while (i < i1) {
+            const uint32_t e = i + 8 < i1 ? i + 8 : i1;  // <= 16 products per block sum
+            uint64_t b[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 4
+            for (; i < e; ++i) {
+                const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
+                const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
+                const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
+                const uint2 mr = __ldg(reinterpret_cast<const uint2*>(m + i * mstride + mh));
+                b[0] += mul64(gl.x, ml.x) + mul64(gr.x, mr.x);
+                b[1] += mul64(gl.y, ml.y) + mul64(gr.y, mr.y);
+                b[2] += mul64(gr.x, ml.x);
+                b[3] += mul64(gr.y, ml.y);
+                b[4] += mul64(gl.x, mr.x);
+                b[5] += mul64(gl.y, mr.y);
+            }
+#pragma unroll
+            for (int q = 0; q < 6; ++q) acc96(lo[q], hi[q], b[q]);
+        }
     }
     const uint64_t o = (((uint64_t)part * kRows + kp) << L) + 2 * i2;
     *reinterpret_cast<uint2*>(jb.out0 + o) = make_uint2(red96(hi[0], lo[0], pc, pi), red96(hi[1], lo[1], pc, pi));
@@ -325,56 +346,6 @@ __global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<Mac
         make_uint2(red96(h0, l0, pc, pi), red96(h1, l1, pc, pi));
     jb.out1[(((uint64_t)part * kRows + kp) << (L - 1)) + i2] = red96(hl, ll, pc, pi);
     jb.out2[(((uint64_t)part * kRows + kp) << (L - 1)) + i2] = red96(hr, lr, pc, pi);
-}
-
-// The same with two slot pairs per thread (16-byte loads of four slots), L >= 3.
-__global__ void __launch_bounds__(kMacThreads, 8) mac_split4_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
-    const MacJobX jb = J.j[find_job(J)];
-    const uint32_t hq = 1u << (L - 2);  // slot quads
-    const uint32_t nblk = slot_block_count(hq);
-    uint32_t c = blockIdx.x - jb.cta0;
-    const uint32_t blk = c % nblk;
-    c /= nblk;
-    const uint32_t kp = c % kRows;
-    const uint32_t part = c / kRows;
-    const uint32_t i4 = blk * kMacThreads + threadIdx.x;
-    if (i4 >= hq) return;
-    const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
-    const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
-    const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
-    const uint32_t p = pc.p[pi];
-    const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
-    const uint64_t mstride = (uint64_t)kPrimes << L;
-    const uint32_t* g = jb.G + ((((uint64_t)jb.g_base * kRank + k) * kPrimes + pi) << L) + 4 * i4;
-    const uint32_t* m = jb.M + (((uint64_t)jb.m_base * kPrimes + pi) << L) + 4 * i4;
-    uint64_t lo[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // slots 0..3, then L and R of pairs 0, 1
-    uint32_t hi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    uint32_t i = i0;
-    while (i < i1) {
-        const uint32_t e = i + 16 < i1 ? i + 16 : i1;
-        uint64_t b[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-#pragma unroll 4
-        for (; i < e; ++i) {
-            const uint4 gv = __ldg(reinterpret_cast<const uint4*>(g + i * gstride));
-            const uint4 mv = __ldg(reinterpret_cast<const uint4*>(m + i * mstride));
-            b[0] += mul64(gv.x, mv.x);
-            b[1] += mul64(gv.y, mv.y);
-            b[2] += mul64(gv.z, mv.z);
-            b[3] += mul64(gv.w, mv.w);
-            b[4] += mul64(red_below(gv.x + p - gv.y, p), red_below(mv.x + mv.y, p));
-            b[5] += mul64(red_below(gv.x + gv.y, p), red_below(mv.x + p - mv.y, p));
-            b[6] += mul64(red_below(gv.z + p - gv.w, p), red_below(mv.z + mv.w, p));
-            b[7] += mul64(red_below(gv.z + gv.w, p), red_below(mv.z + p - mv.w, p));
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) acc96(lo[q], hi[q], b[q]);
-    }
-    *reinterpret_cast<uint4*>(jb.out0 + (((uint64_t)part * kRows + kp) << L) + 4 * i4) =
-        make_uint4(red96(hi[0], lo[0], pc, pi), red96(hi[1], lo[1], pc, pi), red96(hi[2], lo[2], pc, pi),
-                   red96(hi[3], lo[3], pc, pi));
-    const uint64_t oh = (((uint64_t)part * kRows + kp) << (L - 1)) + 2 * i4;
-    *reinterpret_cast<uint2*>(jb.out1 + oh) = make_uint2(red96(hi[4], lo[4], pc, pi), red96(hi[6], lo[6], pc, pi));
-    *reinterpret_cast<uint2*>(jb.out2 + oh) = make_uint2(red96(hi[5], lo[5], pc, pi), red96(hi[7], lo[7], pc, pi));
 }
 
 // ================================================================ finish
@@ -628,12 +599,9 @@ cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_mac_split4(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st);
-
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs || (split && L == 0)) return cudaErrorInvalidValue;
-    if (split && L >= 3) return launch_mac_split4(T, jobs, n, L, st);
     JobList<MacJobX> JL;
     const uint32_t slots = split ? (1u << (L - 1)) : (1u << L);
     uint64_t total = 0;
@@ -648,22 +616,6 @@ cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_
         mac_split_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
     else
         mac_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
-    return cudaGetLastError();
-}
-
-// Split MAC with four slots per thread (L >= 3).
-cudaError_t launch_mac_split4(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st) {
-    JobList<MacJobX> JL;
-    const uint32_t quads = 1u << (L - 2);
-    uint64_t total = 0;
-    JL.n = n;
-    for (int i = 0; i < n; ++i) {
-        jobs[i].cta0 = (uint32_t)total;
-        JL.j[i] = jobs[i];
-        total += (uint64_t)((quads + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
-    }
-    const unsigned bx = quads < (uint32_t)kMacThreads ? quads : kMacThreads;
-    mac_split4_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
     return cudaGetLastError();
 }
 

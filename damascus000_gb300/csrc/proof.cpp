@@ -257,6 +257,7 @@ int ProofState::setup(const uint8_t* file, uint64_t len, bool on_device, const u
     d_ = d;
     S_ = N_ = n_ = (uint32_t)S;
     len_ = len;
+    mcols_ = (uint32_t)((coeff_count_for_byte_len(len) + S - 1) / S);
     alloc_stream_ = stream;
     std::memcpy(seed_, seed, 32);
     const uint64_t S2 = S * S;
@@ -294,6 +295,46 @@ int ProofState::setup(const uint8_t* file, uint64_t len, bool on_device, const u
     return kOk;
 }
 
+// Transforms and the multiply-accumulate of a commitment stage over `cols`
+// columns of ring 2^L of which the first `c` can be nonzero: the full sum into
+// `part`, and for cols >= 2 the cross terms L (pairs (i, i + cols/2)) and R.
+// With c <= cols/2 the witness half from cols/2 on is zero: only c witness
+// columns and the generator columns [0, c) and [cols/2, cols/2 + c) are
+// transformed and read, and R is zero.  Returns whether the cross terms exist.
+bool ProofState::plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, const uint4* m_src, const uint4* g_src,
+                             uint32_t* part) {
+    const uint64_t s = 1ull << L;
+    uint32_t* mh = mhat_.as<uint32_t>();
+    uint32_t* gh = ghat_.as<uint32_t>();
+    const uint64_t gcol_in = 8 * s, gcol_out = 8 * (uint64_t)kPrimes * s;  // one generator column
+    auto ntt = [&](const uint4* src, uint32_t* dst, uint64_t polys) {
+        if (polys) P.ntt[L].push_back(NttJob{src, dst, polys, 0});
+    };
+    if (cols < 2) {
+        ntt(m_src, mh, c);
+        ntt(g_src, gh, 8ull * c);
+        parts_ = mac_parts((uint32_t)s, c);
+        P.mac[L].push_back(MacJobX{gh, mh, part, nullptr, nullptr, 0, 0, c, parts_, 0, 0});
+        return false;
+    }
+    const uint32_t half = cols / 2;
+    if (c <= half) {
+        ntt(m_src, mh, c);
+        ntt(g_src, gh, 8ull * c);
+        ntt(g_src + half * gcol_in, gh + half * gcol_out, 8ull * c);
+        parts_ = mac_parts(s / 2, c);
+        const size_t ps = (size_t)parts_ * kRows * s;
+        P.triple[L].push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, c, parts_, 0, half});
+    } else {
+        ntt(m_src, mh, cols);
+        ntt(g_src, gh, 8ull * cols);
+        parts_ = mac_parts(s / 2, half);
+        const size_t ps = (size_t)parts_ * kRows * s;
+        P.triple[L].push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, half, parts_, 0, 0});
+    }
+    return true;
+}
+
 void ProofState::plan_stage(Plan& P) {
     const uint32_t S = S_;
     const size_t slot = (size_t)kRank * S;
@@ -315,23 +356,16 @@ void ProofState::plan_stage(Plan& P) {
         g.total = 8 * S2;
         g.log_n = L;
         P.gen.push_back(g);
-        P.ntt[L].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), S, 0});
-        P.ntt[L].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * S, 0});
-        const int nj = S >= 2 ? 3 : 1;
-        parts_ = nj == 3 ? mac_parts(S / 2, S / 2) : mac_parts(S, S);
-        const size_t pstride = (size_t)parts_ * kRows * S;
-        if (nj == 3) {
-            P.triple[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
-                                          part + 2 * pstride, 0, 0, S / 2, parts_, 0});
+        const bool nj = plan_commit(P, L, S, mcols_ < S ? mcols_ : S, m_a_.as<uint4>(), g_a_.as<uint4>(), part);
+        if (nj) {
+            const size_t pstride = (size_t)parts_ * kRows * S;
             P.finish[L].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
             P.finish[L].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
-        } else {
-            P.mac[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, S, parts_, 0});
         }
         P.finish[L].push_back(FinishJobX{part, cs(kC), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
         P.d2h.push_back(Copy{tail, misc_.as<uint8_t>(), 32});
         P.d2h.push_back(Copy{pinned_, cs(kC), slot * 16});
-        if (nj == 3) {
+        if (nj) {
             P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kL), slot * 16});
             P.d2h.push_back(Copy{pinned_ + 2 * slot * 16, cs(kR), slot * 16});
         }
@@ -345,13 +379,18 @@ void ProofState::plan_stage(Plan& P) {
         P.fold.push_back(FoldJob{g_b_.as<uint4>(), g_a_.as<uint4>(), g_a_.as<uint4>() + 4 * s2, nullptr, xi_, fq_zero(),
                                  4 * s2, kFoldVec, 0});
         P.fold.push_back(FoldJob{cs(kCt), cs(kC), cs(kL), cs(kR), xi_, x_, (uint64_t)kRank * s, kCombine, 0});
-        P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
-        P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
-        parts_ = mac_parts(L >= 3 ? h / 2 : h, h);  // the split MAC runs four slots per thread from L = 3
+        // the folded witness has h columns, of which the first c can be nonzero:
+        // the check and both cross terms only need those columns
+        const uint32_t c = mcols_ < h ? mcols_ : h;
+        if (c) {
+            P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), c, 0});
+            P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8ull * c, 0});
+        }
+        parts_ = mac_parts(h, c);
         uint32_t* pchk = part;
         uint32_t* plp = part + (size_t)parts_ * kRows * s;
         uint32_t* prp = plp + (size_t)parts_ * kRows * h;
-        P.split[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, h, parts_, 0});
+        P.split[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, c, parts_, 0, 0});
         P.finish[L].push_back(FinishJobX{pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain, kRows, 0});
         P.finish[L - 1].push_back(FinishJobX{plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL, kRows, 0});
         P.finish[L - 1].push_back(FinishJobX{prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR, kRows, 0});
@@ -368,22 +407,15 @@ void ProofState::plan_stage(Plan& P) {
         P.fold.push_back(FoldJob{g_a_.as<uint4>(), g_b_.as<uint4>(), nullptr, nullptr, yi_, fq_zero(), 8 * h2, kFoldPolyX,
                                  Ln, 0});
         P.fold.push_back(FoldJob{cs(kC), cs(kCt), cs(kLp), cs(kRp), yi_, y_, (uint64_t)kRank * h, kCombineEven, Ln, 0});
-        P.ntt[Ln].push_back(NttJob{m_a_.as<uint4>(), mhat_.as<uint32_t>(), h, 0});
-        P.ntt[Ln].push_back(NttJob{g_a_.as<uint4>(), ghat_.as<uint32_t>(), 8 * h, 0});
-        const int nj = h >= 2 ? 3 : 1;
-        parts_ = nj == 3 ? mac_parts(h / 2, h / 2) : mac_parts(h, h);
-        const size_t pstride = (size_t)parts_ * kRows * h;
-        if (nj == 3) {
-            P.triple[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, part + pstride,
-                                           part + 2 * pstride, 0, 0, h / 2, parts_, 0});
+        const bool nj = plan_commit(P, Ln, h, mcols_ < h ? mcols_ : h, m_a_.as<uint4>(), g_a_.as<uint4>(), part);
+        if (nj) {
+            const size_t pstride = (size_t)parts_ * kRows * h;
             P.finish[Ln].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
             P.finish[Ln].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
-        } else {
-            P.mac[Ln].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), part, nullptr, nullptr, 0, 0, h, parts_, 0});
         }
         P.finish[Ln].push_back(FinishJobX{part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain, kRows, 0});
         P.d2h.push_back(Copy{pinned_, cs(kC), (size_t)kRank * h * 16});
-        if (nj == 3) {
+        if (nj) {
             P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kL), (size_t)kRank * h * 16});
             P.d2h.push_back(Copy{pinned_ + 2 * slot * 16, cs(kR), (size_t)kRank * h * 16});
         }

@@ -81,6 +81,8 @@ class ProofState {
 
    private:
     int fail(int code, const std::string& msg);
+    bool plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, const uint4* m_src, const uint4* g_src,
+                     uint32_t* part);
     Context* ctx_;
     cudaStream_t alloc_stream_ = nullptr;
     Stage stage_ = Stage::Init;
@@ -100,6 +102,11 @@ class ProofState {
     uint8_t* pinned_ = nullptr;
     size_t pinned_bytes_ = 0;
     uint32_t parts_ = 1;
+    // Witness columns that can be nonzero: the file fills the coefficients in
+    // order and the square layout pads with zeros, and folds keep zero columns
+    // zero, so a stage's columns from min(mcols_, columns) on are zero.  Their
+    // transforms and the generator columns that only meet them are skipped.
+    uint32_t mcols_ = 0;
     uint8_t seed_[32];
     uint8_t epoch_copy_[32];
 };

@@ -155,6 +155,21 @@ def test_prover_rounds_bit_exact_with_oracle(ctx, oracle_lib, nbytes, tweak):
     assert gp.final_opening() == op.final_opening()
 
 
+# File sizes around the witness fill boundaries: the padding columns are zero and
+# the device skips their transforms and the generator columns that only meet
+# them (fill <= 1/2 of a stage's columns, exactly 1/2, just above, one column,
+# the empty file), so every round must still match the oracle bit for bit.
+@pytest.mark.parametrize("nbytes", [0, 832, 6656, 13_317, 26_624, 26_625, 106_496])
+def test_zero_witness_columns_bit_exact_with_oracle(ctx, oracle_lib, nbytes):
+    data, seed = synth.random_file(23, nbytes, 0)
+    op = oracle_lib.Prover(data, seed, EPOCH)
+    gp = D.DamascusProver(ctx, data, seed, EPOCH)
+    assert gp.statement() == op.statement()
+    for r in range(op.rounds_total):
+        assert gp.fold_round(r) == op.fold_round(r), r
+    assert gp.final_opening() == op.final_opening()
+
+
 def test_full_proof_golden_d6(ctx):
     g = json.loads((GOLDEN / "golden.json").read_text())
     c = g["d6"]
