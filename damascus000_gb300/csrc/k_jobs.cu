@@ -77,69 +77,100 @@ DM_D uint32_t fadd(uint32_t a, uint32_t b, uint32_t one) {
     asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(one), "r"(b));
     return r;
 }
+// Rotation right by 7 on the FMA pipe: x * 2^25 + floor(x * 2^25 / 2^32), with
+// r7 = 2^25 a kernel argument so the compiler keeps the multiplies (the two
+// parts have disjoint bits, so their sum is the rotation).  Used for part of
+// the rotations to balance the two pipes: the ALU pipe bounds the expansion.
+DM_D uint32_t frotr7(uint32_t x, uint32_t r7) {
+    uint32_t r;
+    asm("{\n\t.reg .u32 h;\n\tmul.hi.u32 h, %1, %2;\n\tmad.lo.u32 %0, %1, %2, h;\n\t}" : "=r"(r) : "r"(x), "r"(r7));
+    return r;
+}
 
-// BLAKE3 G on the generator message, whose words 7..15 are zero
-// (src/commitment/sis.rs:231-245: 25-byte "g" || i || k || c blocks).
-#define DM_GEN_G(a, b, c, d, X, Y)                        \
-    do {                                                   \
-        a = fadd(b, a, one);                               \
-        if ((X) < 7) a = fadd(m[(X) < 7 ? (X) : 0], a, one); \
-        d = b3_rotr(d ^ a, 16);                            \
-        c = fadd(d, c, one);                               \
-        b = b3_rotr(b ^ c, 12);                            \
-        a = fadd(b, a, one);                               \
-        if ((Y) < 7) a = fadd(m[(Y) < 7 ? (Y) : 0], a, one); \
-        d = b3_rotr(d ^ a, 8);                             \
-        c = fadd(d, c, one);                               \
-        b = b3_rotr(b ^ c, 7);                             \
+// The generator message (src/commitment/sis.rs:231-245): the 25-byte block
+// "g" || i || k || c (u64 LE each) as words m0 = 0x67 | i << 8, m1 = i >> 24,
+// m2 = k << 8, m4 = c << 8; words 3, 5 .. 15 are zero for k < 8 and c < 2^24
+// (the launcher checks the ring size), so their adds are left out.
+#define DM_GEN_NZ(X) ((X) == 0 || (X) == 1 || (X) == 2 || (X) == 4)
+#define DM_GEN_G(a, b, c, d, X, Y, ROT7)                     \
+    do {                                                      \
+        a = fadd(b, a, one);                                  \
+        if (DM_GEN_NZ(X)) a = fadd(m[DM_GEN_NZ(X) ? (X) : 0], a, one); \
+        d = b3_rotr(d ^ a, 16);                               \
+        c = fadd(d, c, one);                                  \
+        b = b3_rotr(b ^ c, 12);                               \
+        a = fadd(b, a, one);                                  \
+        if (DM_GEN_NZ(Y)) a = fadd(m[DM_GEN_NZ(Y) ? (Y) : 0], a, one); \
+        d = b3_rotr(d ^ a, 8);                                \
+        c = fadd(d, c, one);                                  \
+        b = ROT7(b ^ c);                                      \
+    } while (0)
+#define DM_ROT7_ALU(x) b3_rotr((x), 7)
+#define DM_ROT7_FMA(x) frotr7((x), r7)
+// Column steps on the ALU rotation, diagonal steps on the FMA-pipe rotation.
+#define DM_GEN_COLUMNS(S0, S1, S2, S3, S4, S5, S6, S7)      \
+    do {                                                    \
+        DM_GEN_G(v0, v4, v8, v12, S0, S1, DM_ROT7_ALU);     \
+        DM_GEN_G(v1, v5, v9, v13, S2, S3, DM_ROT7_ALU);     \
+        DM_GEN_G(v2, v6, v10, v14, S4, S5, DM_ROT7_ALU);    \
+        DM_GEN_G(v3, v7, v11, v15, S6, S7, DM_ROT7_ALU);    \
+    } while (0)
+#define DM_GEN_DIAGONALS(S8, S9, S10, S11, S12, S13, S14, S15) \
+    do {                                                       \
+        DM_GEN_G(v0, v5, v10, v15, S8, S9, DM_ROT7_FMA);       \
+        DM_GEN_G(v1, v6, v11, v12, S10, S11, DM_ROT7_FMA);     \
+        DM_GEN_G(v2, v7, v8, v13, S12, S13, DM_ROT7_FMA);      \
+        DM_GEN_G(v3, v4, v9, v14, S14, S15, DM_ROT7_FMA);      \
     } while (0)
 #define DM_GEN_ROUND(S0, S1, S2, S3, S4, S5, S6, S7, S8, S9, S10, S11, S12, S13, S14, S15) \
     do {                                                                                   \
-        DM_GEN_G(v0, v4, v8, v12, S0, S1);                                                 \
-        DM_GEN_G(v1, v5, v9, v13, S2, S3);                                                 \
-        DM_GEN_G(v2, v6, v10, v14, S4, S5);                                                \
-        DM_GEN_G(v3, v7, v11, v15, S6, S7);                                                \
-        DM_GEN_G(v0, v5, v10, v15, S8, S9);                                                \
-        DM_GEN_G(v1, v6, v11, v12, S10, S11);                                              \
-        DM_GEN_G(v2, v7, v8, v13, S12, S13);                                               \
-        DM_GEN_G(v3, v4, v9, v14, S14, S15);                                               \
+        DM_GEN_COLUMNS(S0, S1, S2, S3, S4, S5, S6, S7);                                    \
+        DM_GEN_DIAGONALS(S8, S9, S10, S11, S12, S13, S14, S15);                            \
     } while (0)
 
-// Keyed root compression of one 25-byte generator block: the first 8 output words.
-DM_D void gen_compress(const uint32_t key[8], const uint32_t m[7], uint32_t one, uint32_t out[8]) {
-    uint32_t v0 = key[0], v1 = key[1], v2 = key[2], v3 = key[3], v4 = key[4], v5 = key[5], v6 = key[6], v7 = key[7];
-    uint32_t v8 = DM_B3_IV0, v9 = DM_B3_IV1, v10 = DM_B3_IV2, v11 = DM_B3_IV3;
-    uint32_t v12 = 0, v13 = 0, v14 = 25, v15 = kB3ChunkStart | kB3ChunkEnd | kB3Root | kB3Keyed;
-    DM_GEN_ROUND(0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15);
-    DM_GEN_ROUND(2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8);
-    DM_GEN_ROUND(3, 4, 10, 12, 13, 2, 7, 14, 6, 5, 9, 0, 11, 15, 8, 1);
-    DM_GEN_ROUND(10, 7, 12, 9, 14, 3, 13, 15, 4, 0, 11, 2, 5, 8, 1, 6);
-    DM_GEN_ROUND(12, 13, 9, 11, 15, 10, 14, 8, 7, 2, 5, 3, 0, 1, 6, 4);
-    DM_GEN_ROUND(9, 14, 11, 5, 8, 12, 15, 1, 13, 3, 0, 10, 2, 6, 4, 7);
-    DM_GEN_ROUND(11, 15, 5, 0, 1, 9, 8, 6, 14, 10, 2, 12, 3, 4, 7, 13);
-    out[0] = v0 ^ v8;
-    out[1] = v1 ^ v9;
-    out[2] = v2 ^ v10;
-    out[3] = v3 ^ v11;
-    out[4] = v4 ^ v12;
-    out[5] = v5 ^ v13;
-    out[6] = v6 ^ v14;
-    out[7] = v7 ^ v15;
-}
-
-__global__ void __launch_bounds__(kGenThreads) gen_jobs_kernel(JobList<GenJob> J, uint32_t one) {
+__global__ void __launch_bounds__(kGenThreads) gen_jobs_kernel(JobList<GenJob> J, uint32_t one, uint32_t r7) {
     const GenJob jb = J.j[find_job(J)];
     const uint64_t base = (uint64_t)(blockIdx.x - jb.cta0) * kGenThreads * kGenItems + threadIdx.x;
+    const uint32_t* key = jb.key;
+    // Round 1's column steps on words (0, 1), (2, 3), (4, 5), (6, 7) depend on
+    // i, k, c and nothing respectively: the last once per thread, the first two
+    // again only when the item's (i, k) changes (never within a thread once a
+    // ring has 1024 coefficients).
+    uint32_t m[5] = {0, 0, 0, 0, 0};
+    uint32_t c3a = key[3], c3b = key[7], c3c = DM_B3_IV3, c3d = kB3ChunkStart | kB3ChunkEnd | kB3Root | kB3Keyed;
+    DM_GEN_G(c3a, c3b, c3c, c3d, 6, 7, DM_ROT7_ALU);
+    uint32_t c0a = 0, c0b = 0, c0c = 0, c0d = 0, c1a = 0, c1b = 0, c1c = 0, c1d = 0;
+    uint64_t last_ik = ~0ull;
     for (int it = 0; it < kGenItems; ++it) {
         const uint64_t e = base + (uint64_t)it * kGenThreads;
         if (e >= jb.total) return;
-        const uint64_t c = e & ((1ull << jb.log_n) - 1);
-        const uint64_t kk = (e >> jb.log_n) & 7u;
-        const uint64_t i = e >> (jb.log_n + 3);
-        uint32_t m[16], out[8];
-        b3_generator_block(i, kk, c, m);
-        gen_compress(jb.key, m, one, out);
-        uint32_t r8[8] = {out[0], out[1], out[2], out[3], out[4], out[5], out[6], out[7]};
+        const uint32_t c = (uint32_t)(e & ((1ull << jb.log_n) - 1));
+        const uint64_t ik = e >> jb.log_n;  // i * 8 + k
+        if (ik != last_ik) {
+            last_ik = ik;
+            const uint64_t i = ik >> 3;
+            m[0] = 0x67u | ((uint32_t)i << 8);
+            m[1] = (uint32_t)(i >> 24);
+            m[2] = ((uint32_t)ik & 7u) << 8;
+            c0a = key[0], c0b = key[4], c0c = DM_B3_IV0, c0d = 0;
+            DM_GEN_G(c0a, c0b, c0c, c0d, 0, 1, DM_ROT7_ALU);
+            c1a = key[1], c1b = key[5], c1c = DM_B3_IV1, c1d = 0;
+            DM_GEN_G(c1a, c1b, c1c, c1d, 2, 3, DM_ROT7_ALU);
+        }
+        m[4] = c << 8;
+        uint32_t v0 = c0a, v4 = c0b, v8 = c0c, v12 = c0d;
+        uint32_t v1 = c1a, v5 = c1b, v9 = c1c, v13 = c1d;
+        uint32_t v2 = key[2], v6 = key[6], v10 = DM_B3_IV2, v14 = 25;
+        uint32_t v3 = c3a, v7 = c3b, v11 = c3c, v15 = c3d;
+        DM_GEN_G(v2, v6, v10, v14, 4, 5, DM_ROT7_ALU);
+        DM_GEN_DIAGONALS(8, 9, 10, 11, 12, 13, 14, 15);
+        DM_GEN_ROUND(2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8);
+        DM_GEN_ROUND(3, 4, 10, 12, 13, 2, 7, 14, 6, 5, 9, 0, 11, 15, 8, 1);
+        DM_GEN_ROUND(10, 7, 12, 9, 14, 3, 13, 15, 4, 0, 11, 2, 5, 8, 1, 6);
+        DM_GEN_ROUND(12, 13, 9, 11, 15, 10, 14, 8, 7, 2, 5, 3, 0, 1, 6, 4);
+        DM_GEN_ROUND(9, 14, 11, 5, 8, 12, 15, 1, 13, 3, 0, 10, 2, 6, 4, 7);
+        DM_GEN_ROUND(11, 15, 5, 0, 1, 9, 8, 6, 14, 10, 2, 12, 3, 4, 7, 13);
+        uint32_t r8[8] = {v0 ^ v8, v1 ^ v9, v2 ^ v10, v3 ^ v11, v4 ^ v12, v5 ^ v13, v6 ^ v14, v7 ^ v15};
         stq(jb.dst, e, fq_reduce8(r8));
     }
 }
@@ -247,12 +278,14 @@ cudaError_t launch_fold_jobs(FoldJob* jobs, int n, cudaStream_t st) {
 cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs) return cudaErrorInvalidValue;
+    for (int i = 0; i < n; ++i)  // message words 5 and 6 are zero for c < 2^24
+        if (jobs[i].log_n > 24) return cudaErrorInvalidValue;
     JobList<GenJob> JL;
     const uint32_t ctas = assign_ctas<GenJob>(jobs, n, JL, [](const GenJob& j) -> uint64_t {
         return (j.total + kGenThreads * kGenItems - 1) / (kGenThreads * kGenItems);
     });
     if (!ctas) return cudaSuccess;
-    gen_jobs_kernel<<<ctas, kGenThreads, 0, st>>>(JL, 1u);
+    gen_jobs_kernel<<<ctas, kGenThreads, 0, st>>>(JL, 1u, 1u << 25);
     return cudaGetLastError();
 }
 
