@@ -265,9 +265,18 @@ def run_reference(args, wl):
 # ------------------------------------------------------------------ GPU
 # DRAM bytes per algorithmic byte of the forward transform: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum over 1200 transform launches of the
-# serving stream (0.95-1.03 for the rings that dominate its time, below 1 for
+# serving stream (0.94-0.99 for the rings that dominate its time, below 1 for
 # small rings that stay in L2).
-NTT_TRAFFIC_RATIO = 0.964
+NTT_TRAFFIC_RATIO = 0.950
+# The transform and the generator expansion are integer-bound: the busy fraction
+# of the pipe that limits each, from ncu --set full on a d = 11 proof (FMA-heavy,
+# which runs the integer multiplies, for the transform; the ALU for BLAKE3).
+INT_PIPE = {
+    "ntt_fwd": {"pipe": "FMA-heavy (integer multiply)", "ncu_frac": 0.698,
+                "unit_rate": "butterflies/s"},
+    "gen_generators": {"pipe": "ALU (XOR / rotate)", "ncu_frac": 0.885, "unit_rate": "BLAKE3 compressions/s"},
+}
+INT_PIPE_SOURCE = "profiles/kernels_d11_full.md"
 
 
 def roofline(stats, measured_on="the timed steps"):
@@ -280,13 +289,18 @@ def roofline(stats, measured_on="the timed steps"):
     achieved = byts / n / (ms / n / 1000.0) / 1e9
     total_ms = sum(v[1] for v in live.values())
     traffic = byts / n * NTT_TRAFFIC_RATIO if dom == "ntt_fwd" else None
-    return {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": src, "traffic": traffic,
-            "traffic_source": "ncu DRAM bytes / algorithmic bytes of this kernel" if traffic else None,
-            "algo_bytes_per_launch": byts / n, "avg_launch_ms": ms / n, "share_of_kernel_time": ms / total_ms,
-            "measured_on": measured_on,
-            "kernels": {k: {"launches": v[0], "ms": round(v[1], 4), "algo_bytes": v[2], "algo_ops": v[3]}
-                        for k, v in live.items()}}
+    out = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+           "traffic_source": "ncu DRAM bytes / algorithmic bytes of this kernel" if traffic else None,
+           "algo_bytes_per_launch": byts / n, "avg_launch_ms": ms / n, "share_of_kernel_time": ms / total_ms,
+           "measured_on": measured_on,
+           "kernels": {k: {"launches": v[0], "ms": round(v[1], 4), "algo_bytes": v[2], "algo_ops": v[3]}
+                       for k, v in live.items()}}
+    if dom in INT_PIPE:
+        # the kernel's own limit is an integer pipe; the HBM fraction above is the share of
+        # the copy bandwidth it uses, the pipe fraction below how close it runs to its limit
+        out["int_pipe"] = dict(INT_PIPE[dom], achieved_rate=ops / (ms / 1000.0), source=INT_PIPE_SOURCE)
+    return out
 
 
 def percentile(xs, q):
