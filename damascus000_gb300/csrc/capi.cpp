@@ -245,7 +245,7 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
     const uint32_t L = log2u(n);
     const uint32_t rows = kRank * kPrimes;
     uint32_t parts = (uint32_t)((1216 + ((n + 127) / 128) * rows - 1) / (((n + 127) / 128) * rows));
-    if (parts > 16) parts = 16;
+    if (parts > kMaxMacParts) parts = kMaxMacParts;
     if (parts > N) parts = (uint32_t)N;
     Scratch m, gg, mh, gh, part, out;
     if (m.alloc(C, N * n * 16) || gg.alloc(C, N * kRank * n * 16) || mh.alloc(C, N * kPrimes * n * 4) ||

@@ -10,6 +10,10 @@
 namespace dm {
 
 constexpr int kMaxJobs = 48;
+// Column splits of one multiply-accumulate.  The finish sums a row's parts with
+// plain 32-bit adds: 16 residues below 2^28 cannot overflow.
+constexpr uint32_t kMaxMacParts = 16;
+static_assert((uint64_t)kMaxMacParts * ((1u << 28) - 1) < (1ull << 32), "part sums fit 32 bits");
 
 // ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][9][2^L] ----
 struct NttJob {

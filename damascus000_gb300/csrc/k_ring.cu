@@ -381,23 +381,27 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
 #pragma unroll
     for (int r = 0; r < kNttE; ++r) a[r] = 0;
     if (active) {
+        // plain 32-bit sums (at most kMaxMacParts residues below 2^28), loads of
+        // several parts in flight, one reduction at the end
+        const uint4* src = reinterpret_cast<const uint4*>(jb.partials + ((uint64_t)row << L) + t * kNttE);
+        const uint64_t pstep = ((uint64_t)jb.rows << L) / 4;  // one part, in uint4
+#pragma unroll 4
         for (uint32_t part = 0; part < jb.parts; ++part) {
-            const uint4* src =
-                reinterpret_cast<const uint4*>(jb.partials + (((uint64_t)part * jb.rows + row) << L) + t * kNttE);
 #pragma unroll
             for (int q4 = 0; q4 < 4; ++q4) {
-                const uint4 v = src[q4];
-                a[4 * q4] = red_below(a[4 * q4] + v.x, p);
-                a[4 * q4 + 1] = red_below(a[4 * q4 + 1] + v.y, p);
-                a[4 * q4 + 2] = red_below(a[4 * q4 + 2] + v.z, p);
-                a[4 * q4 + 3] = red_below(a[4 * q4 + 3] + v.w, p);
+                const uint4 v = src[part * pstep + q4];
+                a[4 * q4] += v.x;
+                a[4 * q4 + 1] += v.y;
+                a[4 * q4 + 2] += v.z;
+                a[4 * q4 + 3] += v.w;
             }
         }
-        if (jb.mode != kFinishPlain) {
+        // to [0, 2p): the twist's Shoup product takes any 32-bit value
+        const uint32_t one_s = pc.one_s[pi];
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r)
-                a[r] = twist(a[r], jb.mode, pi * kMaxRing + s + t * kNttE + r, fwd, inv, p);
-        }
+        for (int r = 0; r < kNttE; ++r)
+            a[r] = jb.mode == kFinishPlain ? shoup_one(a[r], one_s, p)
+                                           : twist(a[r], jb.mode, pi * kMaxRing + s + t * kNttE + r, fwd, inv, p);
     }
     const Tw* tw = inv + pi * kMaxRing;
     const Tw* twl = inv_last + pi * kLastSpan + (1u << L) - 16u;
@@ -438,12 +442,14 @@ __global__ void __launch_bounds__(128)
     const uint32_t p = pc.p[pi];
     uint32_t a[s];
 #pragma unroll
-    for (uint32_t c = 0; c < s; ++c) {
-        uint32_t acc = 0;
-        for (uint32_t part = 0; part < jb.parts; ++part)
-            acc = red_below(acc + jb.partials[(((uint64_t)part * jb.rows + row) << L) + c], p);
-        a[c] = twist(acc, jb.mode, pi * kMaxRing + s + c, fwd, inv, p);
-    }
+    for (uint32_t c = 0; c < s; ++c) a[c] = 0;
+    for (uint32_t part = 0; part < jb.parts; ++part)  // at most kMaxMacParts residues: no overflow
+#pragma unroll
+        for (uint32_t c = 0; c < s; ++c) a[c] += jb.partials[(((uint64_t)part * jb.rows + row) << L) + c];
+#pragma unroll
+    for (uint32_t c = 0; c < s; ++c)
+        a[c] = jb.mode == kFinishPlain ? shoup_one(a[c], pc.one_s[pi], p)
+                                       : twist(a[c], jb.mode, pi * kMaxRing + s + c, fwd, inv, p);
     ntt_inv_small<L>(a, inv + pi * kMaxRing, p);
     const FinishConsts& fc = (jb.mode == kFinishPlain) ? plain : split;
 #pragma unroll
@@ -622,6 +628,8 @@ cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_
 cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
+    for (int i = 0; i < n; ++i)
+        if (jobs[i].parts == 0 || jobs[i].parts > kMaxMacParts) return cudaErrorInvalidValue;
     const HostTables& H = host_tables();
     FinishConsts plain, split;
     for (int i = 0; i < kPrimes; ++i) {

@@ -10,7 +10,7 @@ namespace {
 
 // Commitment slots in comm_ (each 8 * S elements).
 enum Slot { kC = 0, kL = 1, kR = 2, kCt = 3, kV = 4, kLp = 5, kRp = 6, kChk = 7, kSlots = 8 };
-constexpr uint32_t kMaxParts = 16;
+constexpr uint32_t kMaxParts = kMaxMacParts;
 constexpr size_t kTail = 128;  // pinned tail: [0,32) file id, [32,40) flags, [48,64) m*
 
 constexpr uint32_t kRows = kRank * kPrimes;  // MAC rows per job: (coordinate, prime)
