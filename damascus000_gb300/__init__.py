@@ -58,6 +58,7 @@ EXPORTED_SYMBOLS = (
     "damascus_engine_create", "damascus_engine_destroy", "damascus_engine_submit", "damascus_engine_submit_device",
     "damascus_engine_poll",
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
+    "damascus_tuning_set", "damascus_tuning_get", "damascus_tuning_measure",
 )
 
 
@@ -163,6 +164,9 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_drain", i32, vp)
     sig("damascus_engine_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64))
     sig("damascus_engine_profile", i32, vp, P(ctypes.c_double), P(ctypes.c_double))
+    sig("damascus_tuning_set", i32, vp, i32, u32, i32)
+    sig("damascus_tuning_get", i32, vp, i32, u32, P(i32))
+    sig("damascus_tuning_measure", i32, vp, i32, u32, i32, u32, i32, P(ctypes.c_double))
 
 
 # ------------------------------------------------------------------ encoding helpers
@@ -270,7 +274,9 @@ def depth_j(d: int, j: int) -> Tuple[int, int]:
 class Context:
     """A GPU context: device, stream, twiddle/CRT tables and an HBM budget."""
 
-    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, tuning="auto"):
+        """tuning: "auto" applies the packaged autotuner table (tuning_gb300.json) when
+        present, None keeps the built-in launch shapes, a dict applies that table."""
         L = load()
         h = ctypes.c_void_p()
         rc = L.damascus_ctx_create(device, hbm_budget_bytes, ctypes.byref(h))
@@ -278,6 +284,9 @@ class Context:
             raise DamascusError(rc, L.damascus_create_error().decode())
         self._h = h
         self._lib = L
+        if tuning is not None:
+            from . import autotune
+            autotune.apply(self, table=None if tuning == "auto" else tuning)
 
     @property
     def handle(self) -> ctypes.c_void_p:
@@ -314,6 +323,22 @@ class Context:
     @property
     def reserved(self) -> int:
         return self._lib.damascus_ctx_reserved(self._h)
+
+    # -- launch-shape tuning (damascus_tuning_*; autotune.py measures and sets them)
+    def tuning_set(self, knob: int, log_ring: int, value: int) -> None:
+        self.check(self._lib.damascus_tuning_set(self._h, knob, log_ring, value), "tuning_set")
+
+    def tuning_get(self, knob: int, log_ring: int) -> int:
+        v = ctypes.c_int()
+        self.check(self._lib.damascus_tuning_get(self._h, knob, log_ring, ctypes.byref(v)), "tuning_get")
+        return v.value
+
+    def tuning_measure(self, knob: int, log_ring: int, value: int, count: int, reps: int = 5) -> float:
+        """Mean ms per launch of the knob's kernel with `value` on synthetic device data."""
+        ms = ctypes.c_double()
+        self.check(self._lib.damascus_tuning_measure(self._h, knob, log_ring, value, count, reps, ctypes.byref(ms)),
+                   "tuning_measure")
+        return ms.value
 
     # -- profiling
     def set_profiling(self, on: bool) -> None:

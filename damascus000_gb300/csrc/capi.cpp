@@ -5,6 +5,7 @@
 #include <unistd.h>
 
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <map>
 #include <mutex>
@@ -235,7 +236,7 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
                                     uint64_t n, uint8_t* com_out) {
     if (!ctx || !witness || !generators || !com_out || N == 0 || !pow2(n) || n > (1u << kLogMaxProverRing))
         return set_err(ctx, DAMASCUS_EINVAL, "bad commitment shape");
-    // CRT headroom of the single NTT-domain sum: N * n * q^2 < P / 2 (P > 2^269).
+    // CRT headroom of the single NTT-domain sum: N * n * q^2 < P / 2 (P > 2^251).
     if (N * n > (1ull << 24)) return set_err(ctx, DAMASCUS_EUNSUPPORTED, "N * n above 2^24 exceeds the CRT range");
     if (N > 0xFFFFFFFFull / kRank) return set_err(ctx, DAMASCUS_EINVAL, "too many columns");
     Context* C = ctx->ctx;
@@ -244,9 +245,7 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
     const DeviceTables& T = C->tables();
     const uint32_t L = log2u(n);
     const uint32_t rows = kRank * kPrimes;
-    uint32_t parts = (uint32_t)((1216 + ((n + 127) / 128) * rows - 1) / (((n + 127) / 128) * rows));
-    if (parts > kMaxMacParts) parts = kMaxMacParts;
-    if (parts > N) parts = (uint32_t)N;
+    const uint32_t parts = C->mac_parts(kTuneMacPlain, L, (uint32_t)n, (uint32_t)N);
     Scratch m, gg, mh, gh, part, out;
     if (m.alloc(C, N * n * 16) || gg.alloc(C, N * kRank * n * 16) || mh.alloc(C, N * kPrimes * n * 4) ||
         gh.alloc(C, N * kRank * kPrimes * n * 4) || part.alloc(C, (size_t)parts * rows * n * 4) ||
@@ -263,7 +262,7 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
     // inputs may be any 128-bit words: reduce them mod q first
     if (e == cudaSuccess) e = launch_canon(m.m.as<uint4>(), N * n, s);
     if (e == cudaSuccess) e = launch_canon(gg.m.as<uint4>(), N * kRank * n, s);
-    if (e == cudaSuccess) e = launch_ntt_jobs(T, nj, 2, L, s);
+    if (e == cudaSuccess) e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L));
     if (e == cudaSuccess) e = launch_mac_jobs(T, &mj, 1, L, false, s);
     if (e == cudaSuccess) e = launch_finish_jobs(T, &fj, 1, L, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(com_out, out.m.as<uint8_t>(), kRank * n * 16, cudaMemcpyDeviceToHost, s);
@@ -339,7 +338,7 @@ int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const voi
     }
     NttJob nj[2] = {{static_cast<const uint4*>(d_a), ra.m.as<uint32_t>(), (uint32_t)count, 0},
                     {static_cast<const uint4*>(d_b), rb.m.as<uint32_t>(), (uint32_t)count, 0}};
-    cudaError_t e = launch_ntt_jobs(T, nj, 2, L, s);
+    cudaError_t e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L));
     if (e0) {
         e1 = C->take_event();
         cudaEventRecord(e1, s);
@@ -468,6 +467,82 @@ int damascus_prove_device_timed(damascus_ctx* ctx, const void* d_file, size_t le
 int damascus_ctx_flush_l2(damascus_ctx* ctx) {
     if (!ctx) return DAMASCUS_EINVAL;
     return ctx->ctx->flush_l2();
+}
+
+// ------------------------------------------------------------------ tuning
+int damascus_tuning_set(damascus_ctx* ctx, int knob, uint32_t log_ring, int value) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    if (ctx->ctx->set_tuning(knob, log_ring, value) != kOk)
+        return set_err(ctx, DAMASCUS_EINVAL, "tuning knob, ring size or value out of range");
+    return DAMASCUS_OK;
+}
+
+int damascus_tuning_get(damascus_ctx* ctx, int knob, uint32_t log_ring, int* value) {
+    if (!ctx || !value || knob < 0 || knob >= kTuneKnobs || log_ring > (uint32_t)kLogMaxProverRing)
+        return DAMASCUS_EINVAL;
+    *value = ctx->ctx->tuning(knob, log_ring);
+    return DAMASCUS_OK;
+}
+
+int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int value, uint32_t count, int reps,
+                            double* ms_per_launch) {
+    if (!ctx || !ms_per_launch || count == 0 || reps <= 0 || log_ring > (uint32_t)kLogMaxProverRing)
+        return DAMASCUS_EINVAL;
+    const uint32_t L = log_ring;
+    const uint64_t s = 1ull << L;
+    if (knob == kTuneNttGroup ? (L < 4 || (value != 32 && value != 64)) : (knob <= 0 || knob >= kTuneKnobs || L < 1 ||
+                                                                         value < 1 || value > 32))
+        return set_err(ctx, DAMASCUS_EINVAL, "tuning knob, ring size or value out of range");
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    const DeviceTables& T = C->tables();
+    cudaStream_t st = C->stream();
+    const uint32_t rows = kRank * kPrimes;
+    Scratch a, b, part;
+    std::function<cudaError_t()> launch;
+    NttJob nj{};
+    MacJobX mj{};
+    if (knob == kTuneNttGroup) {
+        // count polynomials of arbitrary 128-bit words -> nine residue rows each
+        if (a.alloc(C, count * s * 16) || b.alloc(C, count * kPrimes * s * 4))
+            return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+        cudaMemsetAsync(a.m.as<uint8_t>(), 0x5A, count * s * 16, st);
+        nj = NttJob{a.m.as<uint4>(), b.m.as<uint32_t>(), count, 0};
+        launch = [&] { return launch_ntt_jobs(T, &nj, 1, L, st, value); };
+    } else {
+        // generator / witness residues (all 0x01010101 < p) over `count` columns (pairs for the triple MAC)
+        const uint64_t cols = knob == kTuneMacTriple ? 2ull * count : count;
+        const uint32_t tpr = knob == kTuneMacPlain ? (uint32_t)s : (uint32_t)(s / 2);
+        const uint32_t parts = C->mac_parts_for(value, tpr, count);
+        if (a.alloc(C, cols * rows * s * 4) || b.alloc(C, cols * kPrimes * s * 4) ||
+            part.alloc(C, 3ull * parts * rows * s * 4))
+            return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+        cudaMemsetAsync(a.m.as<uint8_t>(), 0x01, cols * rows * s * 4, st);
+        cudaMemsetAsync(b.m.as<uint8_t>(), 0x01, cols * kPrimes * s * 4, st);
+        uint32_t* P = part.m.as<uint32_t>();
+        const uint64_t ps = (uint64_t)parts * rows * s;
+        mj = MacJobX{a.m.as<uint32_t>(), b.m.as<uint32_t>(), P, P + ps, P + 2 * ps, 0, 0, count, parts, 0, 0};
+        if (knob == kTuneMacTriple)
+            launch = [&] { return launch_mac_triple_jobs(T, &mj, 1, L, st); };
+        else
+            launch = [&] { return launch_mac_jobs(T, &mj, 1, L, knob == kTuneMacSplit, st); };
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = launch();  // warm-up
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int i = 0; i < reps && e == cudaSuccess; ++i) e = launch();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("tuning_measure: ") + cudaGetErrorString(e));
+    *ms_per_launch = (double)ms / reps;
+    return DAMASCUS_OK;
 }
 
 // ------------------------------------------------------------------ verifier

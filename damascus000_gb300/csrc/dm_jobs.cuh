@@ -13,6 +13,17 @@ constexpr int kMaxJobs = 48;
 // Column splits of one multiply-accumulate.  The finish sums a row's parts with
 // plain 32-bit adds: 16 residues below 2^28 cannot overflow.
 constexpr uint32_t kMaxMacParts = 16;
+
+// Launch-shape knobs (set per context; defaults are the built-in choices, an
+// autotuner measures and overrides them per ring size).
+enum TuneKnob : int {
+    kTuneNttGroup = 0,   // threads per block of the forward transform for rings of 2^L < 2^10: 32 or 64
+    kTuneMacTriple = 1,  // resident blocks per SM a triple MAC's column split fills: 1..32
+    kTuneMacSplit = 2,   // the same for the split MAC
+    kTuneMacPlain = 3,   // the same for the single-sum MAC
+    kTuneKnobs = 4,
+};
+constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8};
 static_assert((uint64_t)kMaxMacParts * ((1u << 28) - 1) < (1ull << 32), "part sums fit 32 bits");
 
 // ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][9][2^L] ----
@@ -109,7 +120,8 @@ struct HashJob {
     uint32_t cta0;
 };
 
-cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st);
+// group: threads per block for rings below 2^10 (32 or 64, kTuneNttGroup)
+cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group = 64);
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st);
 // Triple MAC (count = h column pairs): out0 = full sum, out1 = L, out2 = R.
 cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st);

@@ -37,6 +37,9 @@ int Context::create(int device, uint64_t hbm_budget, Context** out, std::string*
     }
     std::unique_ptr<Context> c(new Context());
     c->device_ = device;
+    c->sm_count_ = prop.multiProcessorCount > 0 ? prop.multiProcessorCount : 152;
+    for (int k = 0; k < kTuneKnobs; ++k)
+        for (int L = 0; L <= kLogMaxProverRing; ++L) c->tune_[k][L].store(kTuneDefault[k]);
     if ((e = cudaStreamCreateWithFlags(&c->stream_, cudaStreamNonBlocking)) != cudaSuccess) {
         *err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
         return kECuda;
@@ -56,6 +59,25 @@ int Context::create(int device, uint64_t hbm_budget, Context** out, std::string*
     c->budget_ = hbm_budget ? hbm_budget : (uint64_t)(free_b * 0.9);
     *out = c.release();
     return kOk;
+}
+
+int Context::set_tuning(int knob, uint32_t L, int value) {
+    if (knob < 0 || knob >= kTuneKnobs || L > (uint32_t)kLogMaxProverRing) return kEInval;
+    if (knob == kTuneNttGroup ? (value != 32 && value != 64) : (value < 1 || value > 32)) return kEInval;
+    tune_[knob][L].store(value, std::memory_order_relaxed);
+    return kOk;
+}
+
+uint32_t Context::mac_parts(int knob, uint32_t L, uint32_t threads_per_row, uint32_t count) const {
+    return mac_parts_for(tuning(knob, L), threads_per_row, count);
+}
+
+uint32_t Context::mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uint32_t count) const {
+    const uint32_t per_part = ((threads_per_row + 127) / 128) * (uint32_t)(kRank * kPrimes);
+    uint32_t parts = (uint32_t)sm_count_ * (uint32_t)blocks_per_sm / per_part;
+    if (parts > kMaxMacParts) parts = kMaxMacParts;
+    if (parts > count) parts = count;
+    return parts ? parts : 1;
 }
 
 int Context::flush_l2() {

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "dm_jobs.cuh"
 #include "dm_kernels.cuh"
 #include "dm_ref.cuh"
 #include "protocol.h"
@@ -69,8 +70,20 @@ class Context {
 
     std::mutex& mutex() { return mu_; }
 
+    // Launch-shape knobs (TuneKnob) per ring size 2^L; thread-safe.
+    int tuning(int knob, uint32_t L) const { return tune_[knob][L].load(std::memory_order_relaxed); }
+    int set_tuning(int knob, uint32_t L, int value);
+    int sm_count() const { return sm_count_; }
+    // Column splits of a MAC over `count` columns whose rows take threads_per_row
+    // threads (128 per block): enough parts to fill sm_count x the knob's blocks
+    // per SM, at most kMaxMacParts and `count`, at least one.
+    uint32_t mac_parts(int knob, uint32_t L, uint32_t threads_per_row, uint32_t count) const;
+    uint32_t mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uint32_t count) const;
+
    private:
     int device_ = 0;
+    int sm_count_ = 152;
+    std::atomic<int> tune_[kTuneKnobs][kLogMaxProverRing + 1];
     cudaStream_t stream_ = nullptr;
     DeviceTables tables_{};
     RefDeviceTables ref_tables_{};

@@ -60,10 +60,11 @@ struct RowShape {
 // threads with kPrimesPerThread residue rows per thread; shared memory holds
 // kPrimesPerThread x P rows, prime-major, so each prime's rows sit together as
 // in a one-prime block.
-template <int L>
+template <int L, int G = DM_ROW_GROUP_THREADS>
 struct FwdShape {
+    static_assert(G == 32 || G == 64, "row groups of 32 or 64 threads");
     static constexpr int T = 1 << (L - 4);
-    static constexpr int P = T >= DM_ROW_GROUP_THREADS ? 1 : DM_ROW_GROUP_THREADS / T;
+    static constexpr int P = T >= G ? 1 : G / T;
     static constexpr int THREADS = P * T;
     static constexpr int PASSES = (L + 3) / 4;
     static constexpr size_t SMEM = PASSES > 1 ? (size_t)kPrimesPerThread * P * (1u << L) * sizeof(uint32_t) : 0;
@@ -83,17 +84,17 @@ DM_D void row_sync() {
     if constexpr ((1 << (L - 4)) <= 32) {
         __syncwarp();
     } else {
-        static_assert(RowShape<L>::P == 1 && FwdShape<L>::P == 1, "groups above a warp fill their block");
+        static_assert(RowShape<L>::P == 1 && FwdShape<L, 64>::P == 1, "groups above a warp fill their block");
         __syncthreads();
     }
 }
 
 // ================================================================ forward NTT
 
-template <int L>
-__global__ void __launch_bounds__(FwdShape<L>::THREADS, FwdShape<L>::MIN_BLOCKS)
+template <int L, int G>
+__global__ void __launch_bounds__(FwdShape<L, G>::THREADS, FwdShape<L, G>::MIN_BLOCKS)
     ntt_fwd_kernel(JobList<NttJob> J, PrimeConsts pc, const Tw* __restrict__ fwd, const Tw* __restrict__ fwd_last) {
-    using S = FwdShape<L>;
+    using S = FwdShape<L, G>;
     constexpr int K = kPrimesPerThread;
     extern __shared__ __align__(16) uint32_t sm[];
     const NttJob jb = J.j[find_job(J)];
@@ -490,21 +491,29 @@ __global__ void __launch_bounds__(kPointThreads) pointwise_jobs_kernel(JobList<P
 }
 
 // ---------------------------------------------------------------- launch helpers
+template <int L, int G>
+cudaError_t ntt_launch_LG(const DeviceTables& T, JobList<NttJob>& JL, NttJob* jobs, int n, cudaStream_t st) {
+    using S = FwdShape<L, G>;
+    const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
+        return ((uint64_t)(j.npolys + S::P - 1) / S::P) * kGroups;
+    });
+    if (!ctas) return cudaSuccess;
+    ntt_fwd_kernel<L, G><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.fwd, T.fwd_last);
+    return cudaGetLastError();
+}
+
 template <int L>
-cudaError_t ntt_launch_L(const DeviceTables& T, JobList<NttJob>& JL, NttJob* jobs, int n, cudaStream_t st) {
+cudaError_t ntt_launch_L(const DeviceTables& T, JobList<NttJob>& JL, NttJob* jobs, int n, cudaStream_t st, int group) {
     if constexpr (L < 4) {
         const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
             return ((uint64_t)j.npolys * kPrimes + 127) / 128;
         });
         if (!ctas) return cudaSuccess;
         ntt_fwd_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, T.fwd);
+    } else if constexpr (L < 10) {
+        return group == 32 ? ntt_launch_LG<L, 32>(T, JL, jobs, n, st) : ntt_launch_LG<L, 64>(T, JL, jobs, n, st);
     } else {
-        using S = FwdShape<L>;
-        const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
-            return ((uint64_t)(j.npolys + S::P - 1) / S::P) * kGroups;
-        });
-        if (!ctas) return cudaSuccess;
-        ntt_fwd_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.fwd, T.fwd_last);
+        return ntt_launch_LG<L, 64>(T, JL, jobs, n, st);
     }
     return cudaGetLastError();
 }
@@ -578,11 +587,11 @@ void free_tables(DeviceTables* t) {
     t->fwd = t->inv = t->fwd_last = t->inv_last = nullptr;
 }
 
-cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st) {
+cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group) {
     if (n <= 0) return cudaSuccess;
-    if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
+    if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing || (group != 32 && group != 64)) return cudaErrorInvalidValue;
     JobList<NttJob> JL;
-#define DM_NTT_CALL(l) ntt_launch_L<l>(T, JL, jobs, n, st)
+#define DM_NTT_CALL(l) ntt_launch_L<l>(T, JL, jobs, n, st, group)
     DM_DISPATCH_L(L, DM_NTT_CALL)
 #undef DM_NTT_CALL
     return cudaErrorInvalidValue;

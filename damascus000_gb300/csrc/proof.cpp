@@ -15,18 +15,6 @@ constexpr size_t kTail = 128;  // pinned tail: [0,32) file id, [32,40) flags, [4
 
 constexpr uint32_t kRows = kRank * kPrimes;  // MAC rows per job: (coordinate, prime)
 
-// Column splits of a MAC: as many parts as fit one full wave of blocks (152 SMs
-// x 8 resident blocks), at most kMaxParts and at least one column per part.
-// Long column runs per thread keep more loads in flight than extra parts, and a
-// single wave has no tail.
-uint32_t mac_parts(uint32_t threads_per_row, uint32_t count) {
-    const uint32_t per_part = ((threads_per_row + 127) / 128) * kRows;
-    uint32_t parts = (152u * 8u) / per_part;
-    if (parts > kMaxParts) parts = kMaxParts;
-    if (parts > count) parts = count;
-    return parts ? parts : 1;
-}
-
 void unpack_module(const uint8_t* src, uint32_t n, Module& m) {
     m.n = n;
     m.c.resize((size_t)kRank * n);
@@ -137,7 +125,8 @@ int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
         if ((rc = timed("ntt_fwd", bytes, ops, [&] {
                  for (size_t i = 0; i < ntt[L].size(); i += kMaxJobs) {
                      const int n = (int)std::min<size_t>(kMaxJobs, ntt[L].size() - i);
-                     cudaError_t e = launch_ntt_jobs(T, ntt[L].data() + i, n, (uint32_t)L, st);
+                     cudaError_t e = launch_ntt_jobs(T, ntt[L].data() + i, n, (uint32_t)L, st,
+                                                     ctx->tuning(kTuneNttGroup, (uint32_t)L));
                      if (e != cudaSuccess) return (int)e;
                      ++launches;
                  }
@@ -313,7 +302,7 @@ bool ProofState::plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, con
     if (cols < 2) {
         ntt(m_src, mh, c);
         ntt(g_src, gh, 8ull * c);
-        parts_ = mac_parts((uint32_t)s, c);
+        parts_ = ctx_->mac_parts(kTuneMacPlain, L, (uint32_t)s, c);
         P.mac[L].push_back(MacJobX{gh, mh, part, nullptr, nullptr, 0, 0, c, parts_, 0, 0});
         return false;
     }
@@ -322,13 +311,13 @@ bool ProofState::plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, con
         ntt(m_src, mh, c);
         ntt(g_src, gh, 8ull * c);
         ntt(g_src + half * gcol_in, gh + half * gcol_out, 8ull * c);
-        parts_ = mac_parts(s / 2, c);
+        parts_ = ctx_->mac_parts(kTuneMacTriple, L, (uint32_t)(s / 2), c);
         const size_t ps = (size_t)parts_ * kRows * s;
         P.triple[L].push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, c, parts_, 0, half});
     } else {
         ntt(m_src, mh, cols);
         ntt(g_src, gh, 8ull * cols);
-        parts_ = mac_parts(s / 2, half);
+        parts_ = ctx_->mac_parts(kTuneMacTriple, L, (uint32_t)(s / 2), half);
         const size_t ps = (size_t)parts_ * kRows * s;
         P.triple[L].push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, half, parts_, 0, 0});
     }
@@ -386,7 +375,7 @@ void ProofState::plan_stage(Plan& P) {
             P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), c, 0});
             P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8ull * c, 0});
         }
-        parts_ = mac_parts(h, c);
+        parts_ = ctx_->mac_parts(kTuneMacSplit, L, h, c);
         uint32_t* pchk = part;
         uint32_t* plp = part + (size_t)parts_ * kRows * s;
         uint32_t* prp = plp + (size_t)parts_ * kRows * h;

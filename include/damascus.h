@@ -238,6 +238,26 @@ int damascus_ctx_synchronize(damascus_ctx* ctx);
 /* Writes 256 MiB (more than the 129 MB L2) on the context stream and waits. */
 int damascus_ctx_flush_l2(damascus_ctx* ctx);
 
+/* ------------------------------------------------------------------ launch-shape tuning */
+/* Knobs of the kernels' launch shapes per ring size 2^log_ring (no reference
+ * counterpart: the reference has no device launch shapes).  Defaults are the
+ * built-in choices; damascus000_gb300/autotune.py measures the candidates with
+ * damascus_tuning_measure and sets the fastest.  Results never depend on them. */
+enum {
+    DAMASCUS_TUNE_NTT_GROUP = 0,  /* threads per block of the forward transform, rings below 2^10: 32 or 64 */
+    DAMASCUS_TUNE_MAC_TRIPLE = 1, /* resident blocks per SM the column split of a triple MAC fills: 1..32 */
+    DAMASCUS_TUNE_MAC_SPLIT = 2,  /* the same for the split (vector-stage) MAC */
+    DAMASCUS_TUNE_MAC_PLAIN = 3   /* the same for the single-sum MAC */
+};
+int damascus_tuning_set(damascus_ctx* ctx, int knob, uint32_t log_ring, int value);
+int damascus_tuning_get(damascus_ctx* ctx, int knob, uint32_t log_ring, int* value);
+/* Mean device time of one launch over `reps` launches (CUDA events, context
+ * stream, after one warm-up launch) of the knob's kernel with `value`, on
+ * synthetic device data: `count` polynomials (transform), column pairs (triple
+ * MAC) or columns (split, single-sum MAC). */
+int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int value, uint32_t count, int reps,
+                            double* ms_per_launch);
+
 #ifdef __cplusplus
 }
 #endif

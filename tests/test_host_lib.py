@@ -1,6 +1,7 @@
 """CPU tests of the shipped library: it loads, exports every symbol the C header
 declares, and its host-side logic (field, BLAKE3, transcript, layout and bincode
 sizes) matches the oracle.  No compute call needs a GPU here."""
+import json
 import random
 import re
 from pathlib import Path
@@ -123,3 +124,33 @@ def test_parallel_hashing_from_many_threads(oracle_lib):
     for t in threads:
         t.join()
     assert not errors
+
+
+def test_autotune_table_apply_and_candidates():
+    """The autotuner's table round trip on a stand-in context (no GPU): every entry
+    is set through tuning_set with the knob ids of include/damascus.h."""
+    from damascus000_gb300 import autotune as A
+
+    class FakeCtx:
+        def __init__(self):
+            self.calls = []
+
+        def tuning_set(self, knob, L, v):
+            self.calls.append((knob, L, v))
+
+    table = {"entries": [{"knob": "ntt_group", "log_ring": 6, "value": 32},
+                         {"knob": "mac_triple", "log_ring": 11, "value": 12},
+                         {"knob": "mac_split", "log_ring": 9, "value": 4},
+                         {"knob": "mac_plain", "log_ring": 5, "value": 2}]}
+    c = FakeCtx()
+    assert A.apply(c, table=table) == 4
+    assert c.calls == [(0, 6, 32), (1, 11, 12), (2, 9, 4), (3, 5, 2)]
+    assert set(A.CANDIDATES[A.NTT_GROUP]) == {32, 64}
+    assert all(1 <= v <= 32 for k in (A.MAC_TRIPLE, A.MAC_SPLIT, A.MAC_PLAIN) for v in A.CANDIDATES[k])
+    assert A.work_size(A.NTT_GROUP, 9) == 9 * 512 and A.work_size(A.MAC_TRIPLE, 11) == 1024
+    if A.DEFAULT_TABLE.exists():  # the packaged table only names valid knobs and values
+        t = json.loads(A.DEFAULT_TABLE.read_text())
+        c = FakeCtx()
+        assert A.apply(c, table=t) == len(t["entries"]) > 0
+        for knob, L, v in c.calls:
+            assert 0 <= L <= 12 and (v in (32, 64) if knob == 0 else 1 <= v <= 32)
