@@ -204,10 +204,11 @@ int main(int argc, char** argv) {
             }
         }
     }
-    for (int L = 5; L <= max_L; ++L) {
-        const int rows = (1 << (L - 4)) >= 64 ? 1 : 64 >> (L - 4);
-        check_banks(L, rows);
-    }
+    for (int L = 5; L <= max_L; ++L)  // blocks of 64 and of 32 threads for small rings (the tuning knob)
+        for (int group : {64, 32}) {
+            const int rows = (1 << (L - 4)) >= group ? 1 : group >> (L - 4);
+            check_banks(L, rows);
+        }
     for (int L = 0; L <= max_L; ++L) {
         const uint32_t s = 1u << L;
         // a commitment coordinate: sum of `cols` products, the first of all-(q-1) operands
