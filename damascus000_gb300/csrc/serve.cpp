@@ -30,7 +30,7 @@ struct Engine::Wave {
     int stream_idx;
 };
 
-Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_waves_(max_waves > 0 ? max_waves : 6) {
+Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_waves_(max_waves > 0 ? max_waves : 16) {
     cudaSetDevice(ctx_->device());
     cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
     cudaEventCreateWithFlags(&admit_ev_, cudaEventDisableTiming);

@@ -167,7 +167,7 @@ int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const u
  * context's HBM budget, keep their state on the device across rounds, and the
  * same stage of every ready request runs in shared launches while host threads
  * compute the Fiat-Shamir challenges of others.  host_threads / max_waves <= 0
- * pick defaults (cores - 1 / 6 stage waves in flight, each on its own stream).
+ * pick defaults (cores - 1 / 16 stage waves in flight, each on its own stream).
  * Proofs are the same bytes damascus_prove returns. */
 typedef struct damascus_engine damascus_engine;
 int damascus_engine_create(damascus_ctx* ctx, int host_threads, int max_waves, damascus_engine** out);
