@@ -346,15 +346,14 @@ int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const voi
         e0 = C->take_event();
         cudaEventRecord(e0, s);
     }
-    PointwiseJob pj{ra.m.as<uint32_t>(), rb.m.as<uint32_t>(), ra.m.as<uint32_t>(), count, 0};
+    // slotwise products feed the inverse transform directly (no product buffer)
     FinishJobX fj{ra.m.as<uint32_t>(), static_cast<uint4*>(d_out), nullptr, nullptr, 1, kFinishPlain,
-                  (uint32_t)(count * kPrimes), 0};
-    if (e == cudaSuccess) e = launch_pointwise_jobs(T, &pj, 1, L, s);
+                  (uint32_t)(count * kPrimes), 0, rb.m.as<uint32_t>()};
     if (e == cudaSuccess) e = launch_finish_jobs(T, &fj, 1, L, s);
     if (e0) {
         e1 = C->take_event();
         cudaEventRecord(e1, s);
-        C->record("ring_mul", e0, e1, (double)count * n * (3 * kPrimes * 4 + 16), (double)count * kPrimes * (n / 2) * L, 3);
+        C->record("ring_mul", e0, e1, (double)count * n * (2 * kPrimes * 4 + 16), (double)count * kPrimes * (n / 2) * L, 2);
     }
     // Scratch is released when this returns: wait for the kernels that read it.
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

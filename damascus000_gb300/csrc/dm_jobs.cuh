@@ -65,16 +65,12 @@ struct FinishJobX {
     uint32_t mode;         // FinishMode
     uint32_t rows;         // npolys * kPrimes
     uint32_t cta0;         // filled by the launcher
+    // When set (with parts == 1): the row's input is the slotwise product of the
+    // transformed rows `partials` and `rhs` (a negacyclic ring product per
+    // polynomial) instead of a sum of partials.
+    const uint32_t* rhs;
 };
 
-// ---- pointwise products of two transformed sets (ring products of pairs) ----
-struct PointwiseJob {
-    const uint32_t* a;  // [npolys][9][2^L]
-    const uint32_t* b;
-    uint32_t* out;
-    uint64_t npolys;
-    uint32_t cta0;
-};
 
 // ---- folds and commitment algebra in the coefficient domain ----
 enum FoldMode : uint32_t {
@@ -126,7 +122,6 @@ cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_
 // Triple MAC (count = h column pairs): out0 = full sum, out1 = L, out2 = R.
 cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st);
 cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);  // 2 launches
-cudaError_t launch_pointwise_jobs(const DeviceTables& T, PointwiseJob* jobs, int n, uint32_t L, cudaStream_t st);
 cudaError_t launch_fold_jobs(FoldJob* jobs, int n, cudaStream_t st);
 cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st);
 cudaError_t launch_unpack_jobs(UnpackJob* jobs, int n, cudaStream_t st);

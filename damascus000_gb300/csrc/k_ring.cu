@@ -382,19 +382,32 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
 #pragma unroll
     for (int r = 0; r < kNttE; ++r) a[r] = 0;
     if (active) {
-        // plain 32-bit sums (at most kMaxMacParts residues below 2^28), loads of
-        // several parts in flight, one reduction at the end
         const uint4* src = reinterpret_cast<const uint4*>(jb.partials + ((uint64_t)row << L) + t * kNttE);
-        const uint64_t pstep = ((uint64_t)jb.rows << L) / 4;  // one part, in uint4
-#pragma unroll 4
-        for (uint32_t part = 0; part < jb.parts; ++part) {
+        if (jb.rhs) {
+            // slotwise product of two transformed rows, below 4p
+            const uint4* sb = reinterpret_cast<const uint4*>(jb.rhs + ((uint64_t)row << L) + t * kNttE);
 #pragma unroll
             for (int q4 = 0; q4 < 4; ++q4) {
-                const uint4 v = src[part * pstep + q4];
-                a[4 * q4] += v.x;
-                a[4 * q4 + 1] += v.y;
-                a[4 * q4 + 2] += v.z;
-                a[4 * q4 + 3] += v.w;
+                const uint4 u = src[q4], v = sb[q4];
+                a[4 * q4] = red64_lazy(mul64(u.x, v.x), pc, pi);
+                a[4 * q4 + 1] = red64_lazy(mul64(u.y, v.y), pc, pi);
+                a[4 * q4 + 2] = red64_lazy(mul64(u.z, v.z), pc, pi);
+                a[4 * q4 + 3] = red64_lazy(mul64(u.w, v.w), pc, pi);
+            }
+        } else {
+            // plain 32-bit sums (at most kMaxMacParts residues below 2^28), loads of
+            // several parts in flight, one reduction at the end
+            const uint64_t pstep = ((uint64_t)jb.rows << L) / 4;  // one part, in uint4
+#pragma unroll 4
+            for (uint32_t part = 0; part < jb.parts; ++part) {
+#pragma unroll
+                for (int q4 = 0; q4 < 4; ++q4) {
+                    const uint4 v = src[part * pstep + q4];
+                    a[4 * q4] += v.x;
+                    a[4 * q4 + 1] += v.y;
+                    a[4 * q4 + 2] += v.z;
+                    a[4 * q4 + 3] += v.w;
+                }
             }
         }
         // to [0, 2p): the twist's Shoup product takes any 32-bit value
@@ -444,9 +457,15 @@ __global__ void __launch_bounds__(128)
     uint32_t a[s];
 #pragma unroll
     for (uint32_t c = 0; c < s; ++c) a[c] = 0;
-    for (uint32_t part = 0; part < jb.parts; ++part)  // at most kMaxMacParts residues: no overflow
+    if (jb.rhs) {
 #pragma unroll
-        for (uint32_t c = 0; c < s; ++c) a[c] += jb.partials[(((uint64_t)part * jb.rows + row) << L) + c];
+        for (uint32_t c = 0; c < s; ++c)
+            a[c] = red64_lazy(mul64(jb.partials[((uint64_t)row << L) + c], jb.rhs[((uint64_t)row << L) + c]), pc, pi);
+    } else {
+        for (uint32_t part = 0; part < jb.parts; ++part)  // at most kMaxMacParts residues: no overflow
+#pragma unroll
+            for (uint32_t c = 0; c < s; ++c) a[c] += jb.partials[(((uint64_t)part * jb.rows + row) << L) + c];
+    }
 #pragma unroll
     for (uint32_t c = 0; c < s; ++c)
         a[c] = jb.mode == kFinishPlain ? shoup_one(a[c], pc.one_s[pi], p)
@@ -477,17 +496,6 @@ __global__ void __launch_bounds__(kCrtThreads) crt_jobs_kernel(JobList<FinishJob
         const uint4 x = jb.expect[e];
         if (x.x != v.w[0] || x.y != v.w[1] || x.z != v.w[2] || x.w != v.w[3]) atomicOr(jb.flag, 1u);
     }
-}
-
-// ================================================================ pointwise
-constexpr int kPointThreads = 256;
-__global__ void __launch_bounds__(kPointThreads) pointwise_jobs_kernel(JobList<PointwiseJob> J, uint32_t L,
-                                                                       PrimeConsts pc) {
-    const PointwiseJob jb = J.j[find_job(J)];
-    const uint64_t e = (uint64_t)(blockIdx.x - jb.cta0) * kPointThreads + threadIdx.x;
-    if (e >= (jb.npolys * kPrimes) << L) return;
-    const uint32_t pi = (uint32_t)((e >> L) % kPrimes);
-    jb.out[e] = red64(mul64(jb.a[e], jb.b[e]), pc, pi);
 }
 
 // ---------------------------------------------------------------- launch helpers
@@ -638,7 +646,8 @@ cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, u
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
     for (int i = 0; i < n; ++i)
-        if (jobs[i].parts == 0 || jobs[i].parts > kMaxMacParts) return cudaErrorInvalidValue;
+        if (jobs[i].parts == 0 || jobs[i].parts > kMaxMacParts || (jobs[i].rhs && jobs[i].parts != 1))
+            return cudaErrorInvalidValue;
     const HostTables& H = host_tables();
     FinishConsts plain, split;
     for (int i = 0; i < kPrimes; ++i) {
@@ -673,20 +682,5 @@ cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, u
     return cudaGetLastError();
 }
 
-cudaError_t launch_pointwise_jobs(const DeviceTables& T, PointwiseJob* jobs, int n, uint32_t L, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    if (n > kMaxJobs) return cudaErrorInvalidValue;
-    JobList<PointwiseJob> JL;
-    uint64_t total = 0;
-    JL.n = n;
-    for (int i = 0; i < n; ++i) {
-        jobs[i].cta0 = (uint32_t)total;
-        JL.j[i] = jobs[i];
-        total += (((jobs[i].npolys * kPrimes) << L) + kPointThreads - 1) / kPointThreads;
-    }
-    if (!total) return cudaSuccess;
-    pointwise_jobs_kernel<<<(unsigned)total, kPointThreads, 0, st>>>(JL, L, T.pc);
-    return cudaGetLastError();
-}
 
 }  // namespace dm
