@@ -360,25 +360,20 @@ DM_D uint32_t twist(uint32_t x, uint32_t mode, uint32_t idx, const Tw* fwd, cons
     return x;
 }
 
-// Block -> ROWS consecutive rows of one job.  Sums the column partials of each
-// row, applies the split twist (w_i or w_i^-1; the 1/4 is in the final scale),
-// inverse-transforms, scales, and writes the residues over the row's part-0
-// partials.
+// The row part of a finish: the row's input (the sum of its column partials, or
+// the slotwise product of two transformed rows), the split twist (w_i or w_i^-1;
+// the 1/4 is in the final scale), the inverse transform through the row's
+// shared-memory slice at `base` and the final scale.  Leaves the row's residues
+// in a (register r of thread t holds coefficient place(L, 0, t, r)).  Every
+// thread of a row group runs the same passes and barriers, active or not.
 template <int L>
-__global__ void __launch_bounds__(RowShape<L>::THREADS)
-    inv_rows_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
-                    const Tw* __restrict__ fwd, const Tw* __restrict__ inv, const Tw* __restrict__ inv_last) {
-    using S = RowShape<L>;
+DM_D void finish_row(const FinishJobX& jb, uint32_t row, uint32_t t, uint32_t base, bool active, const PrimeConsts& pc,
+                     const FinishConsts& plain, const FinishConsts& split, const Tw* __restrict__ fwd,
+                     const Tw* __restrict__ inv, const Tw* __restrict__ inv_last, uint32_t* sm, uint32_t a[kNttE]) {
     constexpr uint32_t s = 1u << L;
-    extern __shared__ __align__(16) uint32_t sm[];
-    const FinishJobX jb = J.j[find_job(J)];
-    const uint32_t brow = threadIdx.x / S::T;
-    const uint32_t t = threadIdx.x % S::T;
-    const uint32_t row = (blockIdx.x - jb.cta0) * S::ROWS + brow;
-    const bool active = row < jb.rows;
+    constexpr int PASSES = (L + 3) / 4;
     const uint32_t pi = active ? row % kPrimes : 0;
     const uint32_t p = pc.p[pi];
-    uint32_t a[kNttE];
 #pragma unroll
     for (int r = 0; r < kNttE; ++r) a[r] = 0;
     if (active) {
@@ -419,9 +414,8 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
     }
     const Tw* tw = inv + pi * kMaxRing;
     const Tw* twl = inv_last + pi * kLastSpan + (1u << L) - 16u;
-    const uint32_t base = brow << L;
 #pragma unroll
-    for (int pass = S::PASSES - 1; pass >= 0; --pass) {
+    for (int pass = PASSES - 1; pass >= 0; --pass) {
         ntt_inv_pass(a, L, pass, t, tw, twl, p);
         if (pass > 0) {
             const uint32_t ws = ntt_swz_base(base, L, pass, t);
@@ -437,9 +431,81 @@ __global__ void __launch_bounds__(RowShape<L>::THREADS)
     if (active) {
         const FinishConsts& fc = (jb.mode == kFinishPlain) ? plain : split;
         const uint32_t f = fc.f[pi], fs = fc.fs[pi];
+#pragma unroll
+        for (int r = 0; r < kNttE; ++r) a[r] = red_below(shoup_mul(a[r], f, fs, p), p);
+    }
+}
+
+// Block -> ROWS consecutive rows of one job: the row part of the finish, residues
+// written over the row's part-0 partials for crt_jobs_kernel.
+template <int L>
+__global__ void __launch_bounds__(RowShape<L>::THREADS)
+    inv_rows_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
+                    const Tw* __restrict__ fwd, const Tw* __restrict__ inv, const Tw* __restrict__ inv_last) {
+    using S = RowShape<L>;
+    extern __shared__ __align__(16) uint32_t sm[];
+    const FinishJobX jb = J.j[find_job(J)];
+    const uint32_t brow = threadIdx.x / S::T;
+    const uint32_t t = threadIdx.x % S::T;
+    const uint32_t row = (blockIdx.x - jb.cta0) * S::ROWS + brow;
+    const bool active = row < jb.rows;
+    uint32_t a[kNttE];
+    finish_row<L>(jb, row, t, brow << L, active, pc, plain, split, fwd, inv, inv_last, sm, a);
+    if (active) {
         uint32_t* dst = jb.partials + ((uint64_t)row << L);
 #pragma unroll
-        for (int r = 0; r < kNttE; ++r) dst[ntt_place(L, 0, t, r)] = red_below(shoup_mul(a[r], f, fs, p), p);
+        for (int r = 0; r < kNttE; ++r) dst[ntt_place(L, 0, t, r)] = a[r];
+    }
+}
+
+// The whole finish of P polynomials in one block, rings of 2^4 .. 2^10: the
+// nine prime rows of each polynomial go through finish_row, stay in shared
+// memory, and the same block recombines them by Garner CRT into Z_q (no
+// residue round trip through HBM, one launch instead of two).
+template <int L>
+struct FusedShape {
+    static constexpr int T = 1 << (L - 4);
+    static constexpr int P = T >= 32 ? 1 : 32 / T;  // polynomials per block
+    static constexpr int ROWS = kPrimes * P;
+    static constexpr int THREADS = ROWS * T;        // 288 or 576
+    static constexpr size_t SMEM = (size_t)ROWS * (1u << L) * sizeof(uint32_t);
+};
+
+template <int L>
+__global__ void __launch_bounds__(FusedShape<L>::THREADS)
+    finish_fused_kernel(JobList<FinishJobX> J, PrimeConsts pc, CrtConsts cc, FinishConsts plain, FinishConsts split,
+                        const Tw* __restrict__ fwd, const Tw* __restrict__ inv, const Tw* __restrict__ inv_last) {
+    using S = FusedShape<L>;
+    constexpr uint32_t s = 1u << L;
+    extern __shared__ __align__(16) uint32_t sm[];
+    const FinishJobX jb = J.j[find_job(J)];
+    const uint32_t brow = threadIdx.x / S::T;
+    const uint32_t t = threadIdx.x % S::T;
+    const uint32_t poly0 = (blockIdx.x - jb.cta0) * S::P;
+    const uint32_t row = poly0 * kPrimes + brow;
+    const bool active = row < jb.rows;
+    const uint32_t base = brow << L;
+    uint32_t a[kNttE];
+    finish_row<L>(jb, row, t, base, active, pc, plain, split, fwd, inv, inv_last, sm, a);
+    row_sync<L>();  // the row is done reading its exchange slice
+#pragma unroll
+    for (int r = 0; r < kNttE; ++r) sm[base + ntt_place(L, 0, t, r)] = a[r];
+    __syncthreads();
+    const uint32_t npolys = jb.rows / kPrimes;
+    for (uint32_t idx = threadIdx.x; idx < (uint32_t)S::P * s; idx += S::THREADS) {
+        const uint32_t q = idx >> L, j = idx & (s - 1);
+        const uint32_t poly = poly0 + q;
+        if (poly >= npolys) continue;
+        uint32_t r[kPrimes];
+#pragma unroll
+        for (int i = 0; i < kPrimes; ++i) r[i] = sm[((q * kPrimes + i) << L) + j];
+        const fq v = crt_to_fq(r, pc, cc);
+        const uint64_t e = ((uint64_t)poly << L) + j;
+        stq(jb.out, e, v);
+        if (jb.expect) {
+            const uint4 x = jb.expect[e];
+            if (x.x != v.w[0] || x.y != v.w[1] || x.z != v.w[2] || x.w != v.w[3]) atomicOr(jb.flag, 1u);
+        }
     }
 }
 
@@ -544,6 +610,23 @@ cudaError_t inv_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJ
         inv_rows_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, plain, split, T.fwd, T.inv, T.inv_last);
     }
     return cudaGetLastError();
+}
+
+template <int L>
+cudaError_t fused_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJobX* jobs, int n,
+                           const FinishConsts& plain, const FinishConsts& split, cudaStream_t st) {
+    if constexpr (L < 4 || L > 10) {
+        return cudaErrorInvalidValue;
+    } else {
+        using S = FusedShape<L>;
+        const uint32_t ctas = assign_ctas<FinishJobX>(jobs, n, JL, [](const FinishJobX& j) -> uint64_t {
+            return ((uint64_t)j.rows / kPrimes + S::P - 1) / S::P;
+        });
+        if (!ctas) return cudaSuccess;
+        finish_fused_kernel<L><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.cc, plain, split, T.fwd, T.inv,
+                                                                  T.inv_last);
+        return cudaGetLastError();
+    }
 }
 
 #define DM_DISPATCH_L(L, CALL)                                                                                 \
@@ -655,6 +738,13 @@ cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, u
         plain.fs[i] = H.ninvs[i][L];
         split.f[i] = H.ninv4[i][L];
         split.fs[i] = H.ninv4s[i][L];
+    }
+    if (L >= 4 && L <= 10) {
+        JobList<FinishJobX> JL;
+#define DM_FUSED_CALL(l) fused_launch_L<l>(T, JL, jobs, n, plain, split, st)
+        DM_DISPATCH_L(L, DM_FUSED_CALL)
+#undef DM_FUSED_CALL
+        return cudaErrorInvalidValue;
     }
     cudaError_t e = cudaErrorInvalidValue;
     {
