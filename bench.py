@@ -364,13 +364,19 @@ def run_gpu(args, wl):
         total_ms = max_over_ranks(dev_ms)
         value = world * args.steps * pairs / (total_ms / 1000.0)
         lib = D.load()
+
+        def host_call():
+            ctx.check(lib.damascus_ring_mul_batch(ctx.handle, ctypes.cast(pa.data_ptr(), ctypes.c_char_p),
+                                                  ctypes.cast(pb.data_ptr(), ctypes.c_char_p),
+                                                  ctypes.c_void_p(po.data_ptr()), n, pairs), "ring_mul_batch")
+
+        for _ in range(args.warmup):  # the host path's own buffers enter the device pool here
+            host_call()
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            ctx.check(lib.damascus_ring_mul_batch(ctx.handle, ctypes.cast(pa.data_ptr(), ctypes.c_char_p),
-                                                  ctypes.cast(pb.data_ptr(), ctypes.c_char_p),
-                                                  ctypes.c_void_p(po.data_ptr()), n, pairs), "ring_mul_batch")
+            host_call()
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
         ok = bytes(po.numpy()) == bytes(dout.cpu().numpy())
@@ -419,6 +425,9 @@ def run_gpu(args, wl):
         value = world * args.steps * file_bytes / MIB / (total_ms / 1000.0)
         lib = D.load()
         n_out = ctypes.c_size_t()
+        for i in range(args.warmup):  # the host path's staging buffers enter the pools here
+            ctx.check(lib.damascus_prove(ctx.handle, ctypes.c_char_p(pinned[i].data_ptr()), file_bytes,
+                                         files[i][1], EPOCH, out, cap, ctypes.byref(n_out)), "prove")
         barrier()
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
