@@ -250,14 +250,24 @@ def run_reference(args, wl):
         if i >= args.warmup:
             vals.append(r["value"])
     value = statistics.median(vals) if vals else base["value"]
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+    # one step of the GPU arm's workload at the sampled rate (the sample itself is bounded)
+    if wl["kind"] == "ringmul":
+        step_ms = wl["pairs"] / value * 1000.0
+    elif wl["kind"] == "plain":
+        step_ms = wl["file_bytes"] / MIB / value * 1000.0
+    else:
+        step_ms = sum(len(d) for d, _, _ in workload_files(wl)) / MIB / value * 1000.0
+    metric, unit = ("ring-mults/s", "products/s") if wl["kind"] == "ringmul" else (METRIC, UNIT)
+    line = {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "ms_per_step_note": "one step of the workload at the sampled rate (each timed step is a bounded sample)",
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32/u128 integer", "data": "synthetic",
             "config": {"workload": wl["desc"], "impl_note": "CPU restatement of the reference algorithm; the Rust "
                        "reference cannot be built here (no cargo/rustc on either machine)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": "port",
+            "cpu_baseline": {"value": value, "unit": unit, "cores": base["cores"], "kind": "port",
                              "sample": base["sample"]},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
