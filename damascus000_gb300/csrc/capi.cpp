@@ -237,7 +237,7 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
     if (!ctx || !witness || !generators || !com_out || N == 0 || !pow2(n) || n > (1u << kLogMaxProverRing))
         return set_err(ctx, DAMASCUS_EINVAL, "bad commitment shape");
     // CRT headroom of the single NTT-domain sum: N * n * q^2 < P / 2 (P > 2^251).
-    if (N * n > (1ull << 24)) return set_err(ctx, DAMASCUS_EUNSUPPORTED, "N * n above 2^24 exceeds the CRT range");
+    if (N * n > (1ull << 26)) return set_err(ctx, DAMASCUS_EUNSUPPORTED, "N * n above 2^26 exceeds the CRT range");
     if (N > 0xFFFFFFFFull / kRank) return set_err(ctx, DAMASCUS_EINVAL, "too many columns");
     Context* C = ctx->ctx;
     std::lock_guard<std::mutex> g(C->mutex());
@@ -733,7 +733,7 @@ int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint
                             const uint64_t* primes, const uint64_t* stage_roots, const uint64_t* inv_roots,
                             const uint64_t* inv_sizes) {
     if (!host_a || !host_b || !host_out || !primes || !stage_roots || !inv_roots || !inv_sizes || !pow2(n)) return 1;
-    if (n > (1u << kLogMaxProverRing)) return 12;
+    if (n > (1u << (kLogMaxRing - 1))) return 12;  // the cyclic convolution zero-pads to 2n <= 2^13
     for (int i = 0; i < kRefPrimes; ++i)
         if (primes[i] != kRefCrtPrimes[i]) return 13;  // the kernels are specialised to the reference's primes
     damascus_ctx* ctx = default_ctx();

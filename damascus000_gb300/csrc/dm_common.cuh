@@ -38,18 +38,19 @@ static_assert(kPrimesPerThread == 1 || kPrimesPerThread == 3, "transform block s
 // reference-compatible FFI convolution hook, whose caller passes them in.
 constexpr int kRefPrimes = 8;
 // Largest negacyclic NTT the twiddle tables cover: 2^13 points (the prover uses
-// ring degrees up to 2^12; the reference-compatible cyclic convolution of
+// ring degrees up to 2^13; the reference-compatible cyclic convolution of
 // length n <= 2^12 zero-pads to 2n).
 constexpr int kLogMaxRing = 13;
 // Largest ring degree of the commitment / fold kernels.
-constexpr int kLogMaxProverRing = 12;
+constexpr int kLogMaxProverRing = 13;
 constexpr uint32_t kMaxRing = 1u << kLogMaxRing;
-// Last-pass twiddle tables: one block of 2^L entries per ring size 2^L, L = 4..12,
+// Last-pass twiddle tables: one block of 2^L entries per ring size 2^L, L = 4..13,
 // at offset 2^L - 16 within a prime's span.
 constexpr uint32_t kLastSpan = (2u << kLogMaxProverRing) - 16u;
 // Deepest fold the prover accepts: the ring of degree 2^d must fit the transform
-// kernels (2^12) and N * n * q^2 < P / 2 must hold (2^248 < 2^250.9 at d = 12).
-constexpr int kMaxDepth = 12;
+// kernels (2^13) and N * n * q^2 < P / 2 must hold (2^250 < 2^250.98 at d = 13;
+// d = 14 would need a tenth prime).
+constexpr int kMaxDepth = 13;
 // Minimum fold depth (src/utils/config.rs:5).
 constexpr int kMinDepth = 6;
 constexpr int kBytesPerCoeff = 13;

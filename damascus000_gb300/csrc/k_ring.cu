@@ -644,6 +644,7 @@ cudaError_t fused_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, Finis
         case 10: return CALL(10);                                                                              \
         case 11: return CALL(11);                                                                              \
         case 12: return CALL(12);                                                                              \
+        case 13: return CALL(13);                                                                              \
     }
 
 }  // namespace

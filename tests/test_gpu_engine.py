@@ -71,8 +71,8 @@ def test_engine_failure_is_isolated(ctx):
     good = _files(92, [40_000, 70_000])
     with D.Engine(ctx) as eng:
         t0 = eng.submit(*good[0], EPOCH)
-        # 218 MB + 1 byte lands on depth 13, above the supported maximum (12)
-        bad = eng.submit(bytes(4096 * 4096 * 13 + 1), bytes(32), EPOCH)
+        # 872 MB + 1 byte lands on depth 14, above the supported maximum (13: the CRT range)
+        bad = eng.submit(bytes(8192 * 8192 * 13 + 1), bytes(32), EPOCH)
         t1 = eng.submit(*good[1], EPOCH)
         p0 = eng.wait(t0)[0]
         with pytest.raises(D.DamascusError) as e:

@@ -288,9 +288,28 @@ def test_d11_prove_verifies_on_gpu(ctx):
 
 
 @pytest.mark.slow
+def test_d13_prove_verifies_on_gpu(ctx):
+    """Depth 13 (8192 x 8192 witness, rings of 2^13, the deepest the nine-prime CRT
+    range holds: sums up to 2^250 < P / 2).  The reference accepts it once its
+    memory limit is raised (the estimate is 2 GiB); the engine has no such limit."""
+    nbytes = 4096 * 4096 * 13 + 1  # just above the depth-12 capacity
+    data, seed = synth.random_file(13, nbytes, 0)
+    assert D.layout_for_byte_len(nbytes)[0] == 13
+    with D.Engine(ctx, host_threads=4) as eng:
+        proof = eng.prove_batch([(data, seed, EPOCH)])[0]
+    assert len(proof) == D.proof_size(nbytes)
+    assert ctx.verify(proof, EPOCH)
+    bad = bytearray(proof)
+    bad[len(bad) - 5] ^= 1  # the opening
+    assert not ctx.verify(bytes(bad), EPOCH)
+    p = D.DamascusProver(ctx, data, seed, EPOCH, max_preprocess_bytes=4 << 30)
+    assert p.statement() == proof[:len(p.statement())]
+
+
+@pytest.mark.slow
 def test_d12_prove_verifies_on_gpu(ctx):
-    """Depth 12 (4096 x 4096 witness, the largest ring the transform kernels take):
-    the commitment sums reach 2^248 in magnitude, inside the nine-prime CRT range."""
+    """Depth 12 (4096 x 4096 witness): the commitment sums reach 2^248 in magnitude,
+    inside the nine-prime CRT range."""
     nbytes = 2048 * 2048 * 13 + 4096 * 1024  # just above the depth-11 capacity
     data, seed = synth.random_file(12, nbytes, 0)
     assert D.layout_for_byte_len(nbytes)[0] == 12

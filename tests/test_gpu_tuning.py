@@ -19,7 +19,7 @@ def test_tuning_set_get_and_validation():
         c.tuning_set(A.MAC_SPLIT, 9, 24)
         assert c.tuning_get(A.NTT_GROUP, 6) == 32 and c.tuning_get(A.MAC_SPLIT, 9) == 24
         for knob, L, v in [(A.NTT_GROUP, 6, 48), (A.MAC_TRIPLE, 6, 0), (A.MAC_PLAIN, 6, 33), (7, 6, 8),
-                           (A.MAC_SPLIT, 13, 8)]:
+                           (A.MAC_SPLIT, 14, 8)]:
             with pytest.raises(D.DamascusError):
                 c.tuning_set(knob, L, v)
 
@@ -40,7 +40,7 @@ def test_proofs_identical_under_extreme_shapes(shape, oracle_lib):
     with D.Context(0, tuning=None) as base:
         want = [base.prove(f, s, EPOCH) for f, s in files]
     with D.Context(0, tuning=None) as c:
-        for L in range(0, 13):
+        for L in range(0, 14):
             if L >= 4:
                 c.tuning_set(A.NTT_GROUP, L, 32 if shape == "small" else 64)
             for knob in (A.MAC_TRIPLE, A.MAC_SPLIT, A.MAC_PLAIN):

@@ -153,4 +153,4 @@ def test_autotune_table_apply_and_candidates():
         c = FakeCtx()
         assert A.apply(c, table=t) == len(t["entries"]) > 0
         for knob, L, v in c.calls:
-            assert 0 <= L <= 12 and (v in (32, 64) if knob == 0 else 1 <= v <= 32)
+            assert 0 <= L <= 13 and (v in (32, 64) if knob == 0 else 1 <= v <= 32)
