@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kGenThreads) gen_jobs_kernel(JobList<GenJob> J
     const GenJob jb = J.j[find_job(J)];
     const uint64_t base = (uint64_t)(blockIdx.x - jb.cta0) * kGenThreads * kGenItems + threadIdx.x;
     const uint32_t* key = jb.key;
-    // Round 1's column steps on words (0, 1), (2, 3), (4, 5), (6, 7) depend on
+    // The first compression round's column steps on words (0, 1), (2, 3), (4, 5), (6, 7) depend on
     // i, k, c and nothing respectively: the last once per thread, the first two
     // again only when the item's (i, k) changes (never within a thread once a
     // ring has 1024 coefficients).
