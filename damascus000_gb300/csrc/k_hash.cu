@@ -4,33 +4,12 @@
 #include <cuda_runtime.h>
 
 #include "dm_blake3.cuh"
+#include "dm_jobs.cuh"
 #include "dm_kernels.cuh"
 
 namespace dm {
 
 namespace {
-
-struct Key8 {
-    uint32_t w[8];
-};
-
-// One coefficient per thread: keyed_hash(g_seed, "g"||i||k||c) reduced mod q.
-__global__ void gen_kernel(Key8 key, uint64_t total, uint32_t log_n, uint4* __restrict__ g) {
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t c = e & ((1ull << log_n) - 1);
-        const uint64_t k = (e >> log_n) & 7u;
-        const uint64_t i = e >> (log_n + 3);
-        uint32_t m[16], out[16];
-        b3_generator_block(i, k, c, m);
-        b3_compress(key.w, m, 0, 25, kB3ChunkStart | kB3ChunkEnd | kB3Root | kB3Keyed, out);
-        uint32_t r[8];
-#pragma unroll
-        for (int t = 0; t < 8; ++t) r[t] = out[t];
-        const fq v = fq_reduce8(r);
-        g[e] = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
-    }
-}
 
 __global__ void unpack_kernel(const uint8_t* __restrict__ file, uint64_t len, uint64_t total,
                               uint4* __restrict__ m) {
@@ -136,15 +115,17 @@ cudaError_t launch_file_hash(const uint8_t* d_file, uint64_t len, uint32_t* d_cv
     return cudaGetLastError();
 }
 
+// The generator expansion of one statement through the multi-job kernel the
+// prover uses (gen_jobs_kernel, k_jobs.cu), as a single job.
 cudaError_t launch_gen_generators(const uint8_t g_seed[32], uint64_t N, uint32_t log_n, uint4* d_g,
                                   cudaStream_t st) {
-    Key8 key;
-    for (int i = 0; i < 8; ++i) key.w[i] = b3_load_le32(g_seed + 4 * i);
-    const uint64_t total = N * kRank << log_n;
-    if (total == 0) return cudaSuccess;
-    const uint64_t blocks = (total + 255) / 256;
-    gen_kernel<<<(unsigned)(blocks < 152ull * 64 ? blocks : 152ull * 64), 256, 0, st>>>(key, total, log_n, d_g);
-    return cudaGetLastError();
+    GenJob job{};
+    for (int i = 0; i < 8; ++i) job.key[i] = b3_load_le32(g_seed + 4 * i);
+    job.dst = d_g;
+    job.total = N * kRank << log_n;
+    job.log_n = log_n;
+    if (job.total == 0) return cudaSuccess;
+    return launch_gen_jobs(&job, 1, st);
 }
 
 cudaError_t launch_unpack_witness(const uint8_t* d_file, uint64_t len, uint64_t total_coeffs, uint4* d_m,
