@@ -105,12 +105,26 @@ bool decode_statement(const uint8_t*& p, const uint8_t* end, Statement& s) {
     return true;
 }
 
+namespace {
+struct ScaledArgs {
+    const fq* a;
+    const fq* b;
+    fq s;
+    fq* r;
+};
+void scaled_range(void* p, size_t begin, size_t end) {
+    const ScaledArgs* A = static_cast<const ScaledArgs*>(p);
+    for (size_t i = begin; i < end; ++i) A->r[i] = fq_fma(A->a[i], A->s, A->b[i]);
+}
+}  // namespace
+
 bool module_add_scaled(const Module& a, const Module& b, const fq& s, Module& out) {
     if (a.n != b.n) return false;
     Module r;
     r.n = a.n;
     r.c.resize(a.c.size());
-    for (size_t i = 0; i < a.c.size(); ++i) r.c[i] = fq_fma(a.c[i], s, b.c[i]);
+    ScaledArgs args{a.c.data(), b.c.data(), s, r.c.data()};
+    host_parallel_for(a.c.size(), 2048, scaled_range, &args);  // 112-bit products: split large modules
     out = std::move(r);
     return true;
 }
