@@ -310,6 +310,8 @@ def roofline(stats, measured_on="the timed steps"):
         # the kernel's own limit is an integer pipe; the HBM fraction above is the share of
         # the copy bandwidth it uses, the pipe fraction below how close it runs to its limit
         out["int_pipe"] = dict(INT_PIPE[dom], achieved_rate=ops / (ms / 1000.0), source=INT_PIPE_SOURCE)
+        out["note"] = ("integer-bound kernel: frac is its share of the HBM copy peak; its own limit is the "
+                       "int_pipe fraction (ncu)")
     return out
 
 
