@@ -335,8 +335,9 @@ __global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<Mac
             const uint2 mv = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
             b0 += mul64(gv.x, mv.x);
             b1 += mul64(gv.y, mv.y);
-            bl += mul64(red_below(gv.x + p - gv.y, p), red_below(mv.x + mv.y, p));
-            br += mul64(red_below(gv.x + gv.y, p), red_below(mv.x + p - mv.y, p));
+            // sums and differences below 2p: products below 4p^2 < 2^58, 16 of them fit
+            bl += mul64(gv.x + p - gv.y, mv.x + mv.y);
+            br += mul64(gv.x + gv.y, mv.x + p - mv.y);
         }
         acc96(l0, h0, b0);
         acc96(l1, h1, b1);
