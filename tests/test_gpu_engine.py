@@ -111,3 +111,39 @@ def test_engine_many_small_requests_and_profile(ctx):
         assert ctx.verify(p, EPOCH)
     for (d, s), p in list(zip(files, proofs))[::17]:
         assert p == ctx.prove(d, s, EPOCH)
+
+
+@pytest.mark.slow
+def test_engine_soak_streamed_submissions_under_budget():
+    """A long stream (400 requests, 1 KB - 2 MiB, log-uniform) submitted while earlier
+    ones are still running, under a budget that holds only a few large proofs at
+    once: every request completes, sampled proofs verify and equal the plain path,
+    and the budget is fully released at the end."""
+    rng = random.Random(2026)
+    sizes = [int(10 ** rng.uniform(3, 6.32)) for _ in range(400)]
+    files = _files(95, sizes)
+    budget = 3 * D.prover_footprint(2 << 20)
+    c = D.Context(0, hbm_budget_bytes=budget)
+    try:
+        with D.Engine(c, host_threads=8) as eng:
+            tickets, proofs = [], {}
+            for i, (d, s) in enumerate(files):
+                tickets.append(eng.submit(d, s, EPOCH))
+                if i % 50 == 49:  # collect the oldest half while the rest keeps running
+                    for t in tickets[: len(tickets) // 2]:
+                        if t not in proofs:
+                            proofs[t] = eng.wait(t)[0]
+            for t in tickets:
+                if t not in proofs:
+                    proofs[t] = eng.wait(t)[0]
+            st = eng.stats()
+        assert st["completed"] == 400 and st["failed"] == 0
+        assert st["peak_reserved"] <= budget
+        assert c.reserved == 0
+        for i in range(0, 400, 23):
+            p = proofs[tickets[i]]
+            assert len(p) == D.proof_size(sizes[i])
+            assert c.verify(p, EPOCH)
+            assert p == c.prove(*files[i], EPOCH)
+    finally:
+        c.close()
