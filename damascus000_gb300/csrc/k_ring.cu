@@ -510,18 +510,15 @@ __global__ void __launch_bounds__(FusedShape<L>::THREADS)
     }
 }
 
-// Rings below 16 coefficients: one thread per row.
+// Rings below 16 coefficients: one thread per row holds the whole row.  The row
+// part of the finish (input, twist, inverse, scale) into a[].
 template <int L>
-__global__ void __launch_bounds__(128)
-    inv_rows_small_kernel(JobList<FinishJobX> J, PrimeConsts pc, FinishConsts plain, FinishConsts split,
-                          const Tw* __restrict__ fwd, const Tw* __restrict__ inv) {
+DM_D void finish_row_small(const FinishJobX& jb, uint32_t row, const PrimeConsts& pc, const FinishConsts& plain,
+                           const FinishConsts& split, const Tw* __restrict__ fwd, const Tw* __restrict__ inv,
+                           uint32_t a[1u << L]) {
     constexpr uint32_t s = 1u << L;
-    const FinishJobX jb = J.j[find_job(J)];
-    const uint32_t row = (blockIdx.x - jb.cta0) * blockDim.x + threadIdx.x;
-    if (row >= jb.rows) return;
     const uint32_t pi = row % kPrimes;
     const uint32_t p = pc.p[pi];
-    uint32_t a[s];
 #pragma unroll
     for (uint32_t c = 0; c < s; ++c) a[c] = 0;
     if (jb.rhs) {
@@ -540,8 +537,44 @@ __global__ void __launch_bounds__(128)
     ntt_inv_small<L>(a, inv + pi * kMaxRing, p);
     const FinishConsts& fc = (jb.mode == kFinishPlain) ? plain : split;
 #pragma unroll
-    for (uint32_t c = 0; c < s; ++c)
-        jb.partials[((uint64_t)row << L) + c] = red_below(shoup_mul(a[c], fc.f[pi], fc.fs[pi], p), p);
+    for (uint32_t c = 0; c < s; ++c) a[c] = red_below(shoup_mul(a[c], fc.f[pi], fc.fs[pi], p), p);
+}
+
+// The whole finish of rings below 16 coefficients: P polynomials per block, one
+// thread per prime row, the CRT from shared memory in the same block.
+constexpr int kFusedSmallPolys = 32;
+template <int L>
+__global__ void __launch_bounds__(kFusedSmallPolys * kPrimes)
+    finish_fused_small_kernel(JobList<FinishJobX> J, PrimeConsts pc, CrtConsts cc, FinishConsts plain,
+                              FinishConsts split, const Tw* __restrict__ fwd, const Tw* __restrict__ inv) {
+    constexpr uint32_t s = 1u << L;
+    __shared__ uint32_t sm[kFusedSmallPolys * kPrimes * s];
+    const FinishJobX jb = J.j[find_job(J)];
+    const uint32_t poly0 = (blockIdx.x - jb.cta0) * kFusedSmallPolys;
+    const uint32_t row = poly0 * kPrimes + threadIdx.x;
+    if (row < jb.rows) {
+        uint32_t a[s];
+        finish_row_small<L>(jb, row, pc, plain, split, fwd, inv, a);
+#pragma unroll
+        for (uint32_t c = 0; c < s; ++c) sm[threadIdx.x * s + c] = a[c];
+    }
+    __syncthreads();
+    const uint32_t npolys = jb.rows / kPrimes;
+    for (uint32_t idx = threadIdx.x; idx < kFusedSmallPolys * s; idx += kFusedSmallPolys * kPrimes) {
+        const uint32_t q = idx >> L, j = idx & (s - 1);
+        const uint32_t poly = poly0 + q;
+        if (poly >= npolys) continue;
+        uint32_t r[kPrimes];
+#pragma unroll
+        for (int i = 0; i < kPrimes; ++i) r[i] = sm[(q * kPrimes + i) * s + j];
+        const fq v = crt_to_fq(r, pc, cc);
+        const uint64_t e = ((uint64_t)poly << L) + j;
+        stq(jb.out, e, v);
+        if (jb.expect) {
+            const uint4 x = jb.expect[e];
+            if (x.x != v.w[0] || x.y != v.w[1] || x.z != v.w[2] || x.w != v.w[3]) atomicOr(jb.flag, 1u);
+        }
+    }
 }
 
 // Thread per output coefficient: the nine residues of (poly, slot) -> Z_q.
@@ -597,11 +630,7 @@ template <int L>
 cudaError_t inv_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJobX* jobs, int n,
                          const FinishConsts& plain, const FinishConsts& split, cudaStream_t st) {
     if constexpr (L < 4) {
-        const uint32_t ctas = assign_ctas<FinishJobX>(jobs, n, JL, [](const FinishJobX& j) -> uint64_t {
-            return ((uint64_t)j.rows + 127) / 128;
-        });
-        if (!ctas) return cudaSuccess;
-        inv_rows_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, plain, split, T.fwd, T.inv);
+        return cudaErrorInvalidValue;  // rings below 16 finish in finish_fused_small_kernel
     } else {
         using S = RowShape<L>;
         const uint32_t ctas = assign_ctas<FinishJobX>(jobs, n, JL, [](const FinishJobX& j) -> uint64_t {
@@ -616,7 +645,15 @@ cudaError_t inv_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJ
 template <int L>
 cudaError_t fused_launch_L(const DeviceTables& T, JobList<FinishJobX>& JL, FinishJobX* jobs, int n,
                            const FinishConsts& plain, const FinishConsts& split, cudaStream_t st) {
-    if constexpr (L < 4 || L > 10) {
+    if constexpr (L < 4) {
+        const uint32_t ctas = assign_ctas<FinishJobX>(jobs, n, JL, [](const FinishJobX& j) -> uint64_t {
+            return ((uint64_t)j.rows / kPrimes + kFusedSmallPolys - 1) / kFusedSmallPolys;
+        });
+        if (!ctas) return cudaSuccess;
+        finish_fused_small_kernel<L><<<ctas, kFusedSmallPolys * kPrimes, 0, st>>>(JL, T.pc, T.cc, plain, split, T.fwd,
+                                                                                  T.inv);
+        return cudaGetLastError();
+    } else if constexpr (L > 10) {
         return cudaErrorInvalidValue;
     } else {
         using S = FusedShape<L>;
@@ -741,7 +778,7 @@ cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, u
         split.f[i] = H.ninv4[i][L];
         split.fs[i] = H.ninv4s[i][L];
     }
-    if (L >= 4 && L <= 10) {
+    if (L <= 10) {
         JobList<FinishJobX> JL;
 #define DM_FUSED_CALL(l) fused_launch_L<l>(T, JL, jobs, n, plain, split, st)
         DM_DISPATCH_L(L, DM_FUSED_CALL)
