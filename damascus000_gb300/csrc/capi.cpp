@@ -255,7 +255,7 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
     NttJob nj[2] = {{m.m.as<uint4>(), mh.m.as<uint32_t>(), (uint32_t)N, 0},
                     {gg.m.as<uint4>(), gh.m.as<uint32_t>(), (uint32_t)(N * kRank), 0}};
     MacJobX mj{gh.m.as<uint32_t>(), mh.m.as<uint32_t>(), part.m.as<uint32_t>(), nullptr, nullptr, 0, 0, (uint32_t)N,
-               parts, 0};
+               parts, 0, 0, L};
     FinishJobX fj{part.m.as<uint32_t>(), out.m.as<uint4>(), nullptr, nullptr, parts, kFinishPlain, rows, 0};
     cudaError_t e = cudaMemcpyAsync(m.m.as<uint8_t>(), witness, N * n * 16, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(gg.m.as<uint8_t>(), generators, N * kRank * n * 16, cudaMemcpyHostToDevice, s);
@@ -263,7 +263,7 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
     if (e == cudaSuccess) e = launch_canon(m.m.as<uint4>(), N * n, s);
     if (e == cudaSuccess) e = launch_canon(gg.m.as<uint4>(), N * kRank * n, s);
     if (e == cudaSuccess) e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L));
-    if (e == cudaSuccess) e = launch_mac_jobs(T, &mj, 1, L, false, s);
+    if (e == cudaSuccess) e = launch_mac_jobs(T, &mj, 1, false, s);
     if (e == cudaSuccess) e = launch_finish_jobs(T, &fj, 1, L, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(com_out, out.m.as<uint8_t>(), kRank * n * 16, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -521,11 +521,11 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
         cudaMemsetAsync(b.m.as<uint8_t>(), 0x01, cols * kPrimes * s * 4, st);
         uint32_t* P = part.m.as<uint32_t>();
         const uint64_t ps = (uint64_t)parts * rows * s;
-        mj = MacJobX{a.m.as<uint32_t>(), b.m.as<uint32_t>(), P, P + ps, P + 2 * ps, 0, 0, count, parts, 0, 0};
+        mj = MacJobX{a.m.as<uint32_t>(), b.m.as<uint32_t>(), P, P + ps, P + 2 * ps, 0, 0, count, parts, 0, 0, L};
         if (knob == kTuneMacTriple)
-            launch = [&] { return launch_mac_triple_jobs(T, &mj, 1, L, st); };
+            launch = [&] { return launch_mac_triple_jobs(T, &mj, 1, st); };
         else
-            launch = [&] { return launch_mac_jobs(T, &mj, 1, L, knob == kTuneMacSplit, st); };
+            launch = [&] { return launch_mac_jobs(T, &mj, 1, knob == kTuneMacSplit, st); };
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = launch();  // warm-up

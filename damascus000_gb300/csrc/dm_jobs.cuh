@@ -49,6 +49,7 @@ struct MacJobX {
     // (i, i + pair) for i < count <= pair with every witness column from `pair`
     // on zero, so the witness is read at i only and R is zero.
     uint32_t pair;
+    uint32_t L;  // ring size 2^L of this job (jobs of any sizes share a launch)
 };
 
 // ---- sum partials, inverse NTT, CRT to Z_q, optional compare (all jobs share L) ----
@@ -118,9 +119,9 @@ struct HashJob {
 
 // group: threads per block for rings below 2^10 (32 or 64, kTuneNttGroup)
 cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group = 64);
-cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st);
+cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st);
 // Triple MAC (count = h column pairs): out0 = full sum, out1 = L, out2 = R.
-cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st);
+cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, cudaStream_t st);
 cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);  // 2 launches
 cudaError_t launch_fold_jobs(FoldJob* jobs, int n, cudaStream_t st);
 cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st);

@@ -192,8 +192,9 @@ DM_D uint64_t mul64(uint32_t a, uint32_t b) { return (uint64_t)a * b; }
 
 
 // grid: per job, nblk * 72 * parts blocks; block -> (part, row, slot block).
-__global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+__global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
     const MacJobX jb = J.j[find_job(J)];
+    const uint32_t L = jb.L;
     const uint32_t s = 1u << L;
     const uint32_t nblk = slot_block_count(s);
     uint32_t c = blockIdx.x - jb.cta0;
@@ -234,8 +235,9 @@ __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> 
 // (out2).  h = count, or h = pair when the witness columns from h on are known
 // zero: then i runs over the count < h leading columns only, the witness is read
 // at i alone and R is zero.  Thread per slot pair (8-byte loads), L >= 1.
-__global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+__global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
     const MacJobX jb = J.j[find_job(J)];
+    const uint32_t L = jb.L;
     const uint32_t sp = 1u << (L - 1);
     const uint32_t nblk = slot_block_count(sp);
     uint32_t c = blockIdx.x - jb.cta0;
@@ -304,8 +306,9 @@ __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<Ma
 // Split MAC: thread per slot pair (2 i2, 2 i2 + 1) of ring 2^L (L >= 1): the
 // recompute check over all slots and the even/odd cross terms
 // (g(w) - g(-w)) (m(w) + m(-w)) and (g(w) + g(-w)) (m(w) - m(-w)) at 2^(L-1).
-__global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<MacJobX> J, uint32_t L, PrimeConsts pc) {
+__global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
     const MacJobX jb = J.j[find_job(J)];
+    const uint32_t L = jb.L;
     const uint32_t hs = 1u << (L - 1);
     const uint32_t nblk = slot_block_count(hs);
     uint32_t c = blockIdx.x - jb.cta0;
@@ -727,40 +730,58 @@ cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    if (n > kMaxJobs || L == 0) return cudaErrorInvalidValue;
-    JobList<MacJobX> JL;
-    const uint32_t slots = 1u << (L - 1);  // slot pairs
-    uint64_t total = 0;
+// Jobs of any ring sizes share a launch: each job's blocks cover its own rows and
+// slots; blocks are 128 threads unless every job's rows are shorter.
+namespace {
+template <class Slots>
+cudaError_t mac_launch_common(MacJobX* jobs, int n, Slots slots_of, JobList<MacJobX>& JL, uint64_t* total,
+                              unsigned* bx) {
+    uint32_t widest = 1;
+    *total = 0;
     JL.n = n;
     for (int i = 0; i < n; ++i) {
-        jobs[i].cta0 = (uint32_t)total;
+        if (jobs[i].L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
+        const uint32_t slots = slots_of(jobs[i]);
+        if (slots == 0) return cudaErrorInvalidValue;
+        jobs[i].cta0 = (uint32_t)*total;
         JL.j[i] = jobs[i];
-        total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
+        *total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
+        widest = slots > widest ? slots : widest;
     }
-    const unsigned bx = slots < (uint32_t)kMacThreads ? slots : kMacThreads;
-    mac_triple_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+    *bx = widest < (uint32_t)kMacThreads ? widest : kMacThreads;
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxJobs) return cudaErrorInvalidValue;
+    JobList<MacJobX> JL;
+    uint64_t total;
+    unsigned bx;
+    cudaError_t e = mac_launch_common(jobs, n, [](const MacJobX& j) { return j.L ? 1u << (j.L - 1) : 0u; }, JL,
+                                      &total, &bx);  // slot pairs
+    if (e != cudaSuccess) return e;
+    if (!total) return cudaSuccess;
+    mac_triple_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, T.pc);
     return cudaGetLastError();
 }
 
-cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, uint32_t L, bool split, cudaStream_t st) {
+cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (n > kMaxJobs || (split && L == 0)) return cudaErrorInvalidValue;
+    if (n > kMaxJobs) return cudaErrorInvalidValue;
     JobList<MacJobX> JL;
-    const uint32_t slots = split ? (1u << (L - 1)) : (1u << L);
-    uint64_t total = 0;
-    JL.n = n;
-    for (int i = 0; i < n; ++i) {
-        jobs[i].cta0 = (uint32_t)total;
-        JL.j[i] = jobs[i];
-        total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
-    }
-    const unsigned bx = slots < (uint32_t)kMacThreads ? slots : kMacThreads;
+    uint64_t total;
+    unsigned bx;
+    cudaError_t e = split ? mac_launch_common(jobs, n, [](const MacJobX& j) { return j.L ? 1u << (j.L - 1) : 0u; },
+                                              JL, &total, &bx)
+                          : mac_launch_common(jobs, n, [](const MacJobX& j) { return 1u << j.L; }, JL, &total, &bx);
+    if (e != cudaSuccess) return e;
+    if (!total) return cudaSuccess;
     if (split)
-        mac_split_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+        mac_split_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, T.pc);
     else
-        mac_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, L, T.pc);
+        mac_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, T.pc);
     return cudaGetLastError();
 }
 

@@ -41,22 +41,25 @@ int launch_chunks(std::vector<J>& v, cudaError_t (*fn)(J*, int, cudaStream_t), c
 void Plan::clear() {
     hash.clear();
     unpack.clear();
+    mac.clear();
+    split.clear();
+    triple.clear();
     gen.clear();
     fold.clear();
     for (int L = 0; L <= kLogMaxProverRing; ++L) {
         ntt[L].clear();
-        mac[L].clear();
-        split[L].clear();
-        triple[L].clear();
+
         finish[L].clear();
     }
     d2h.clear();
 }
 
 bool Plan::empty() const {
-    if (!hash.empty() || !unpack.empty() || !gen.empty() || !fold.empty()) return false;
+    if (!hash.empty() || !unpack.empty() || !gen.empty() || !fold.empty() || !mac.empty() || !split.empty() ||
+        !triple.empty())
+        return false;
     for (int L = 0; L <= kLogMaxProverRing; ++L)
-        if (!ntt[L].empty() || !mac[L].empty() || !split[L].empty() || !triple[L].empty() || !finish[L].empty())
+        if (!ntt[L].empty() || !finish[L].empty())
             return false;
     return d2h.empty();
 }
@@ -135,32 +138,30 @@ int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
             return rc;
     }
     for (int pass = 0; pass < 3; ++pass) {
-        for (int L = 0; L <= kLogMaxProverRing; ++L) {
-            auto& v = pass == 0 ? mac[L] : (pass == 1 ? split[L] : triple[L]);
-            if (v.empty()) continue;
-            // columns read: count (plain, split) or 2 * count (triple pairs)
-            const double cols_per_count = pass == 2 ? 2.0 : 1.0;
-            const double macs_per_col = pass == 0 ? 1.0 : 2.0;
-            double macs = 0, bytes = 0;
-            for (auto& j : v) {
-                const double cols = (double)j.count * cols_per_count;
-                macs += cols * (double)kRows * (double)(1u << L) * macs_per_col;
-                // G residues (4 B per column, coordinate, prime, slot) + M residues (shared by 8 coordinates)
-                bytes += cols * (double)(1u << L) * (kRows * 4.0 + kPrimes * 4.0);
-            }
-            const char* name = pass == 0 ? "mac" : (pass == 1 ? "mac_split" : "mac");
-            if ((rc = timed(name, bytes, macs, [&] {
-                     for (size_t i = 0; i < v.size(); i += kMaxJobs) {
-                         const int n = (int)std::min<size_t>(kMaxJobs, v.size() - i);
-                         cudaError_t e = pass == 2 ? launch_mac_triple_jobs(T, v.data() + i, n, (uint32_t)L, st)
-                                                   : launch_mac_jobs(T, v.data() + i, n, (uint32_t)L, pass == 1, st);
-                         if (e != cudaSuccess) return (int)e;
-                         ++launches;
-                     }
-                     return 0;
-                 })))
-                return rc;
+        auto& v = pass == 0 ? mac : (pass == 1 ? split : triple);
+        if (v.empty()) continue;
+        // columns read: count (plain, split) or 2 * count (triple pairs)
+        const double cols_per_count = pass == 2 ? 2.0 : 1.0;
+        const double macs_per_col = pass == 0 ? 1.0 : 2.0;
+        double macs = 0, bytes = 0;
+        for (auto& j : v) {
+            const double cols = (double)j.count * cols_per_count;
+            macs += cols * (double)kRows * (double)(1u << j.L) * macs_per_col;
+            // G residues (4 B per column, coordinate, prime, slot) + M residues (shared by 8 coordinates)
+            bytes += cols * (double)(1u << j.L) * (kRows * 4.0 + kPrimes * 4.0);
         }
+        const char* name = pass == 0 ? "mac" : (pass == 1 ? "mac_split" : "mac");
+        if ((rc = timed(name, bytes, macs, [&] {
+                 for (size_t i = 0; i < v.size(); i += kMaxJobs) {
+                     const int n = (int)std::min<size_t>(kMaxJobs, v.size() - i);
+                     cudaError_t e = pass == 2 ? launch_mac_triple_jobs(T, v.data() + i, n, st)
+                                               : launch_mac_jobs(T, v.data() + i, n, pass == 1, st);
+                     if (e != cudaSuccess) return (int)e;
+                     ++launches;
+                 }
+                 return 0;
+             })))
+            return rc;
     }
     for (int L = kLogMaxProverRing; L >= 0; --L) {
         if (finish[L].empty()) continue;
@@ -303,7 +304,7 @@ bool ProofState::plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, con
         ntt(m_src, mh, c);
         ntt(g_src, gh, 8ull * c);
         parts_ = ctx_->mac_parts(kTuneMacPlain, L, (uint32_t)s, c);
-        P.mac[L].push_back(MacJobX{gh, mh, part, nullptr, nullptr, 0, 0, c, parts_, 0, 0});
+        P.mac.push_back(MacJobX{gh, mh, part, nullptr, nullptr, 0, 0, c, parts_, 0, 0, L});
         return false;
     }
     const uint32_t half = cols / 2;
@@ -313,13 +314,13 @@ bool ProofState::plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, con
         ntt(g_src + half * gcol_in, gh + half * gcol_out, 8ull * c);
         parts_ = ctx_->mac_parts(kTuneMacTriple, L, (uint32_t)(s / 2), c);
         const size_t ps = (size_t)parts_ * kRows * s;
-        P.triple[L].push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, c, parts_, 0, half});
+        P.triple.push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, c, parts_, 0, half, L});
     } else {
         ntt(m_src, mh, cols);
         ntt(g_src, gh, 8ull * cols);
         parts_ = ctx_->mac_parts(kTuneMacTriple, L, (uint32_t)(s / 2), half);
         const size_t ps = (size_t)parts_ * kRows * s;
-        P.triple[L].push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, half, parts_, 0, 0});
+        P.triple.push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, half, parts_, 0, 0, L});
     }
     return true;
 }
@@ -379,7 +380,7 @@ void ProofState::plan_stage(Plan& P) {
         uint32_t* pchk = part;
         uint32_t* plp = part + (size_t)parts_ * kRows * s;
         uint32_t* prp = plp + (size_t)parts_ * kRows * h;
-        P.split[L].push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, c, parts_, 0, 0});
+        P.split.push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, c, parts_, 0, 0, L});
         P.finish[L].push_back(FinishJobX{pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain, kRows, 0});
         P.finish[L - 1].push_back(FinishJobX{plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL, kRows, 0});
         P.finish[L - 1].push_back(FinishJobX{prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR, kRows, 0});

@@ -34,9 +34,8 @@ class Plan {
     std::vector<GenJob> gen;
     std::vector<FoldJob> fold;
     std::vector<NttJob> ntt[kLogMaxProverRing + 1];
-    std::vector<MacJobX> mac[kLogMaxProverRing + 1];
-    std::vector<MacJobX> split[kLogMaxProverRing + 1];
-    std::vector<MacJobX> triple[kLogMaxProverRing + 1];
+    // multiply-accumulates of every ring size (each job carries its own)
+    std::vector<MacJobX> mac, split, triple;
     std::vector<FinishJobX> finish[kLogMaxProverRing + 1];
     std::vector<Copy> d2h;
     // Launches every non-empty job kind in dependency order on `st`, then the copies.
