@@ -76,7 +76,11 @@ uint32_t Context::mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uin
     const uint32_t per_part = ((threads_per_row + 127) / 128) * (uint32_t)(kRank * kPrimes);
     uint32_t parts = (uint32_t)sm_count_ * (uint32_t)blocks_per_sm / per_part;
     if (parts > kMaxMacParts) parts = kMaxMacParts;
-    if (parts > count) parts = count;
+#ifndef DM_MIN_PART_COLS
+#define DM_MIN_PART_COLS 8
+#endif
+    const uint32_t most = (count + DM_MIN_PART_COLS - 1) / DM_MIN_PART_COLS;  // columns per part at least this
+    if (parts > most) parts = most;
     return parts ? parts : 1;
 }
 
