@@ -147,3 +147,15 @@ def test_engine_soak_streamed_submissions_under_budget():
             assert p == c.prove(*files[i], EPOCH)
     finally:
         c.close()
+
+
+def test_engine_empty_and_one_byte_files(ctx, oracle_lib):
+    """The smallest inputs (an empty file: one zero coefficient; one byte) prove through
+    the engine exactly as through the plain path and the oracle."""
+    items = [(b"", bytes(range(32))), (b"\x07", bytes(32))]
+    with D.Engine(ctx, host_threads=2) as eng:
+        proofs = eng.prove_batch([(d, s, EPOCH) for d, s in items])
+    for (d, s), p in zip(items, proofs):
+        assert p == ctx.prove(d, s, EPOCH)
+        assert p == oracle_lib.prove(d, s, EPOCH)
+        assert ctx.verify(p, EPOCH)
