@@ -6,11 +6,11 @@
 //    identity as field.rs:229-258.
 //  * Arithmetic modulo the nine NTT primes p < 2^28 (p = 1 mod 2^14) that carry
 //    every ring product: Shoup products by constants give [0, 2p), so the
-//    transforms run four stages on values below 12p < 2^32 without reducing
+//    transforms run four stages on values below 16p < 2^32 without reducing
 //    (lazy Harvey butterflies), and products of two reduced residues fit 56 bits.
 //  * Garner recombination of the nine residues into Z_q with a centred lift
-//    (the integer result of src/algebra/ntt.rs:372-427; P > 2^251 leaves room for
-//    any commitment sum, |X| < 2^248, up to depth 12).
+//    (the integer result of src/algebra/ntt.rs:372-427; P = 2^251.98 leaves room
+//    for any commitment sum, |X| < 2^250, up to depth 13).
 #pragma once
 
 #include "dm_common.cuh"
