@@ -23,7 +23,7 @@ namespace dm {
 // Module rank K of R_q^K (src/utils/config.rs:7).
 constexpr int kRank = 8;
 // NTT primes carrying the ring products: nine primes p < 2^28 with p = 1 mod 2^14
-// (their product P > 2^251 bounds every commitment sum, |X| < 2^248, up to depth 12).
+// (their product P = 2^251.98 bounds every commitment sum, |X| < 2^250, up to depth 13).
 constexpr int kPrimes = 9;
 // Primes per thread of the forward transforms (kPrimes / kPrimesPerThread blocks
 // per polynomial): 1 or 3.  Three read each 16-byte coefficient once for three
