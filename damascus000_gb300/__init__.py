@@ -59,6 +59,9 @@ EXPORTED_SYMBOLS = (
     "damascus_engine_poll",
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
     "damascus_tuning_set", "damascus_tuning_get", "damascus_tuning_measure",
+    "damascus_verify_service_create", "damascus_verify_service_destroy", "damascus_verify_service_submit",
+    "damascus_verify_service_poll", "damascus_verify_service_wait", "damascus_verify_service_drain",
+    "damascus_verify_service_stats",
 )
 
 
@@ -167,6 +170,13 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_tuning_set", i32, vp, i32, u32, i32)
     sig("damascus_tuning_get", i32, vp, i32, u32, P(i32))
     sig("damascus_tuning_measure", i32, vp, i32, u32, i32, u32, i32, P(ctypes.c_double))
+    sig("damascus_verify_service_create", i32, vp, i32, u64, P(vp))
+    sig("damascus_verify_service_destroy", None, vp)
+    sig("damascus_verify_service_submit", i32, vp, cp, sz, cp, P(u64))
+    sig("damascus_verify_service_poll", i32, vp, u64, P(i32), P(ctypes.c_double))
+    sig("damascus_verify_service_wait", i32, vp, u64, P(i32), P(ctypes.c_double))
+    sig("damascus_verify_service_drain", i32, vp)
+    sig("damascus_verify_service_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64), P(u64))
 
 
 # ------------------------------------------------------------------ encoding helpers
@@ -631,6 +641,88 @@ class Engine:
         """items: iterable of (data, seed_generators, epoch_seed); returns the proofs in order."""
         tickets = [self.submit(d, s, e) for d, s, e in items]
         return [self.wait(t)[0] for t in tickets]
+
+
+class VerifyService:
+    """Streaming verifier: proofs submitted from any thread are verified by worker
+    threads on their own streams, admitted against the context's HBM budget, with
+    initial generator families shared through an HBM cache (``cache_bytes``, 0
+    disables).  Each verdict equals ``Context.verify``'s on the same bytes."""
+
+    def __init__(self, ctx: Context, workers: int = 0, cache_bytes: int = 16 << 30):
+        self._ctx = ctx
+        self._lib = ctx._lib
+        h = ctypes.c_void_p()
+        ctx.check(self._lib.damascus_verify_service_create(ctx.handle, workers, cache_bytes, ctypes.byref(h)),
+                  "verify service create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.damascus_verify_service_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, proof: bytes, epoch_seed: bytes = DEFAULT_EPOCH_SEED) -> int:
+        t = ctypes.c_uint64()
+        self._ctx.check(self._lib.damascus_verify_service_submit(self._h, proof, len(proof), epoch_seed,
+                                                                 ctypes.byref(t)), "verify service submit")
+        return t.value
+
+    def _result(self, ticket: int, block: bool):
+        v = ctypes.c_int32()
+        lat = ctypes.c_double()
+        fn = self._lib.damascus_verify_service_wait if block else self._lib.damascus_verify_service_poll
+        rc = fn(self._h, ticket, ctypes.byref(v), ctypes.byref(lat))
+        if rc == 0:
+            return None
+        if rc < 0:
+            raise DamascusError(rc, f"verify service ticket {ticket}")
+        return v.value, lat.value
+
+    def wait(self, ticket: int):
+        """(verdict code, latency ms): 0 accepts, else the code ``damascus_verify`` returns."""
+        return self._result(ticket, True)
+
+    def poll(self, ticket: int):
+        """(verdict code, latency ms), or None while running."""
+        return self._result(ticket, False)
+
+    def drain(self) -> None:
+        self._ctx.check(self._lib.damascus_verify_service_drain(self._h), "verify service drain")
+
+    def stats(self) -> dict:
+        v = [ctypes.c_uint64() for _ in range(6)]
+        self._ctx.check(self._lib.damascus_verify_service_stats(self._h, *[ctypes.byref(x) for x in v]),
+                        "verify service stats")
+        return dict(zip(("completed", "accepted", "rejected", "cache_hits", "cache_misses", "peak_reserved"),
+                        (x.value for x in v)))
+
+    def verify_batch(self, proofs, epoch_seed: bytes = DEFAULT_EPOCH_SEED) -> list:
+        """Verdicts as ``Context.verify`` gives them (False for a rejected or
+        undecodable proof; other failures raise)."""
+        tickets = [self.submit(p, epoch_seed) for p in proofs]
+        out = []
+        for t in tickets:
+            code, _ = self.wait(t)
+            if code in (EVERIFY, EDESERIALIZE):
+                out.append(False)
+            elif code:
+                raise DamascusError(code, f"verify service ticket {t}: {self._ctx.last_error()}")
+            else:
+                out.append(True)
+        return out
 
 
 # ------------------------------------------------------------------ reference FFI drop-ins

@@ -19,6 +19,7 @@
 #include "proof.h"
 #include "serve.h"
 #include "host_blake3.h"
+#include "verify_service.h"
 
 using namespace dm;
 
@@ -33,6 +34,10 @@ struct damascus_prover {
 struct damascus_verifier {
     damascus_ctx* owner;
     GpuVerifier* v;
+};
+struct damascus_verify_service {
+    damascus_ctx* owner;
+    VerifyService* s;
 };
 struct damascus_engine {
     damascus_ctx* owner;
@@ -684,6 +689,67 @@ int damascus_engine_profile(damascus_engine* e, double* host_stage_ms, double* g
     const EngineStats s = e->e->stats();
     if (host_stage_ms) *host_stage_ms = s.host_stage_ms;
     if (gpu_idle_ms) *gpu_idle_ms = s.gpu_idle_ms;
+    return DAMASCUS_OK;
+}
+
+// ------------------------------------------------------------------ verifier service
+int damascus_verify_service_create(damascus_ctx* ctx, int workers, uint64_t cache_bytes,
+                                   damascus_verify_service** out) {
+    if (!ctx || !out) return DAMASCUS_EINVAL;
+    *out = new damascus_verify_service{ctx, new VerifyService(ctx->ctx, workers, cache_bytes)};
+    return DAMASCUS_OK;
+}
+
+void damascus_verify_service_destroy(damascus_verify_service* s) {
+    if (!s) return;
+    delete s->s;
+    delete s;
+}
+
+int damascus_verify_service_submit(damascus_verify_service* s, const uint8_t* proof, size_t len,
+                                   const uint8_t epoch_seed[32], uint64_t* ticket) {
+    if (!s) return DAMASCUS_EINVAL;
+    return s->s->submit(proof, len, epoch_seed, ticket);
+}
+
+static int verify_service_result(damascus_verify_service* s, uint64_t ticket, bool block, int* verdict,
+                                 double* latency_ms) {
+    if (!s) return DAMASCUS_EINVAL;
+    int v = 0;
+    std::string err;
+    const int rc = block ? s->s->wait(ticket, &v, latency_ms, &err) : s->s->poll(ticket, &v, latency_ms, &err);
+    if (rc == 1) {
+        if (verdict) *verdict = v;
+        if (v != DAMASCUS_OK) s->owner->ctx->set_error(err);
+    }
+    return rc;
+}
+
+int damascus_verify_service_poll(damascus_verify_service* s, uint64_t ticket, int* verdict, double* latency_ms) {
+    return verify_service_result(s, ticket, false, verdict, latency_ms);
+}
+
+int damascus_verify_service_wait(damascus_verify_service* s, uint64_t ticket, int* verdict, double* latency_ms) {
+    return verify_service_result(s, ticket, true, verdict, latency_ms);
+}
+
+int damascus_verify_service_drain(damascus_verify_service* s) {
+    if (!s) return DAMASCUS_EINVAL;
+    s->s->drain();
+    return DAMASCUS_OK;
+}
+
+int damascus_verify_service_stats(damascus_verify_service* s, uint64_t* completed, uint64_t* accepted,
+                                  uint64_t* rejected, uint64_t* cache_hits, uint64_t* cache_misses,
+                                  uint64_t* peak_reserved_bytes) {
+    if (!s) return DAMASCUS_EINVAL;
+    const VerifyStats v = s->s->stats();
+    if (completed) *completed = v.completed;
+    if (accepted) *accepted = v.accepted;
+    if (rejected) *rejected = v.rejected;
+    if (cache_hits) *cache_hits = v.cache_hits;
+    if (cache_misses) *cache_misses = v.cache_misses;
+    if (peak_reserved_bytes) *peak_reserved_bytes = v.peak_reserved;
     return DAMASCUS_OK;
 }
 

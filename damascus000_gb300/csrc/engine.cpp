@@ -264,23 +264,162 @@ inline fq to_fq(const uint4& v) { return fq{{v.x, v.y, v.z, v.w}}; }
         }                                                                                  \
     } while (0)
 
+// ============================== GenCache ==============================
+
+struct GenCache::Entry {
+    void* ptr = nullptr;
+    uint64_t bytes = 0;
+    cudaEvent_t ready = nullptr;
+    int refs = 0;
+    uint64_t last_use = 0;
+};
+
+GenCache::~GenCache() {
+    std::lock_guard<std::mutex> g(mu_);
+    for (auto& kv : map_) {
+        Entry* e = kv.second;
+        if (e->ready) cudaEventSynchronize(e->ready);
+        cudaFree(e->ptr);
+        ctx_->release(e->bytes);
+        if (e->ready) cudaEventDestroy(e->ready);
+        delete e;
+    }
+    map_.clear();
+}
+
+bool GenCache::evict_one() {
+    auto victim = map_.end();
+    for (auto it = map_.begin(); it != map_.end(); ++it)
+        if (it->second->refs == 0 && (victim == map_.end() || it->second->last_use < victim->second->last_use))
+            victim = it;
+    if (victim == map_.end()) return false;
+    Entry* e = victim->second;
+    // every holder synchronised its stream before releasing, so nothing reads it
+    cudaFree(e->ptr);
+    ctx_->release(e->bytes);
+    cudaEventDestroy(e->ready);
+    st_.bytes -= e->bytes;
+    st_.entries -= 1;
+    st_.evictions += 1;
+    delete e;
+    map_.erase(victim);
+    return true;
+}
+
+bool GenCache::evict_for(uint64_t bytes) {
+    for (;;) {
+        if (st_.bytes + bytes <= cap_ && ctx_->reserve(bytes)) return true;
+        if (!evict_one()) return false;
+    }
+}
+
+bool GenCache::trim(uint64_t bytes) {
+    std::lock_guard<std::mutex> g(mu_);
+    for (;;) {
+        if (ctx_->reserved() + bytes <= ctx_->budget()) return true;
+        if (!evict_one()) return false;
+    }
+}
+
+int GenCache::acquire(const uint8_t seed[32], uint64_t N, uint32_t log_n, cudaStream_t s, Ref* out) {
+    std::vector<uint8_t> key(seed, seed + 32);
+    for (int i = 0; i < 8; ++i) key.push_back((uint8_t)(N >> (8 * i)));
+    key.push_back((uint8_t)log_n);
+    const uint64_t bytes = (N * kRank << log_n) * 16;
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = map_.find(key);
+    if (it != map_.end()) {
+        Entry* e = it->second;
+        e->refs += 1;
+        e->last_use = ++clock_;
+        st_.hits += 1;
+        *out = Ref{static_cast<const uint4*>(e->ptr), e->ready, e};
+        return kOk;
+    }
+    st_.misses += 1;
+    if (bytes > cap_ || !evict_for(bytes)) return kENoMem;
+    Entry* e = new Entry;
+    e->bytes = bytes;
+    if (cudaMalloc(&e->ptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        ctx_->release(bytes);
+        delete e;
+        return kENoMem;
+    }
+    // launched and recorded under the lock: a reader that finds the entry always
+    // waits on a recorded event
+    cudaEvent_t ta = nullptr;
+    if (ctx_->profiling()) {
+        ta = ctx_->take_event();
+        cudaEventRecord(ta, s);
+    }
+    cudaError_t err = launch_gen_generators(seed, N, log_n, static_cast<uint4*>(e->ptr), s);
+    if (ta) {
+        cudaEvent_t tb = ctx_->take_event();
+        cudaEventRecord(tb, s);
+        ctx_->record("gen_generators", ta, tb, (double)bytes, (double)(bytes / 16));
+    }
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e->ready, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventRecord(e->ready, s);
+    if (err != cudaSuccess) {
+        if (e->ready) cudaEventDestroy(e->ready);
+        cudaStreamSynchronize(s);
+        cudaFree(e->ptr);
+        ctx_->release(bytes);
+        delete e;
+        return kECuda;
+    }
+    e->refs = 1;
+    e->last_use = ++clock_;
+    map_[key] = e;
+    st_.bytes += bytes;
+    st_.entries += 1;
+    *out = Ref{static_cast<const uint4*>(e->ptr), e->ready, e};
+    return kOk;
+}
+
+void GenCache::release(const Ref& r) {
+    if (!r.entry) return;
+    std::lock_guard<std::mutex> g(mu_);
+    static_cast<Entry*>(r.entry)->refs -= 1;
+}
+
+GenCache::Stats GenCache::stats() {
+    std::lock_guard<std::mutex> g(mu_);
+    return st_;
+}
+
 // ============================== GpuVerifier ==============================
 
-uint64_t GpuVerifier::footprint(uint64_t N, uint64_t n) { return 2 * N * kRank * n * 16 + 64; }
+// What init allocates without a cache hit: g_0 and the first fold's half, each
+// rounded to the allocator's 256 bytes.
+uint64_t GpuVerifier::footprint(uint64_t N, uint64_t n) {
+    const uint64_t full = N * kRank * n * 16;
+    return ((full + 255) & ~(uint64_t)255) + ((full / 2 + 16 + 255) & ~(uint64_t)255);
+}
 
 GpuVerifier::~GpuVerifier() {
+    if (done_) cudaEventDestroy(done_);
     if (s_) {
-        cudaStreamSynchronize(s_);
+        cudaStreamSynchronize(s_);  // the folds may still read g_0 and the buffers
         g_[0].reset();
         g_[1].reset();
-        cudaStreamSynchronize(s_);
-        cudaStreamDestroy(s_);
+        if (cache_ && cache_ref_.entry) cache_->release(cache_ref_);
+        if (own_stream_) {
+            cudaStreamSynchronize(s_);
+            cudaStreamDestroy(s_);
+        }
     }
 }
 
 int GpuVerifier::fail(int code, const std::string& msg) {
+    err_ = msg;
     ctx_->set_error(msg);
     return code;
+}
+
+const uint4* GpuVerifier::source() const {
+    return (round_ == 0 && cache_ref_.g) ? cache_ref_.g : g_[cur_].as<uint4>();
 }
 
 int GpuVerifier::init(const uint8_t* statement, size_t len, const uint8_t epoch[32]) {
@@ -299,15 +438,29 @@ int GpuVerifier::init(const uint8_t* statement, size_t len, const uint8_t epoch[
     current_ = st_.com_0;
     tr_ = Transcript(epoch, st_.file_id);
     DM_CU(cudaSetDevice(ctx_->device()), "cudaSetDevice");
-    DM_CU(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (own_stream_) DM_CU(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking), "cudaStreamCreate");
     const uint64_t bytes = (uint64_t)N * kRank * n * 16;
-    if (g_[0].alloc(ctx_, bytes, s_) != kOk || g_[1].alloc(ctx_, bytes / 2 + 16, s_) != kOk)
-        return fail(kENoMem, "HBM budget exhausted allocating verifier generators");
     uint32_t Ln = 0;
     while ((1u << Ln) < n) ++Ln;
-    cudaError_t e = launch_gen_generators(st_.g_0_seed, N, Ln, g_[0].as<uint4>(), s_);
-    if (e != cudaSuccess) return fail(kECuda, std::string("gen_generators: ") + cudaGetErrorString(e));
     cur_ = 0;
+    if (cache_ && cache_->acquire(st_.g_0_seed, N, Ln, s_, &cache_ref_) == kOk) {
+        // the first fold writes at most half of g_0, every later one at most a quarter
+        // (both dimensions of a non-trivial family halve while above one)
+        DM_CU(cudaStreamWaitEvent(s_, cache_ref_.ready, 0), "cudaStreamWaitEvent");
+        if (g_[1].alloc(ctx_, bytes / 2 + 16, s_) == kOk && g_[0].alloc(ctx_, bytes / 4 + 16, s_) == kOk) return kOk;
+        // no room beside the cached family: drop it (once its expansion, which may
+        // be this stream's, has finished) and hold a private copy, as without a cache
+        g_[0].reset();
+        g_[1].reset();
+        cudaStreamSynchronize(s_);
+        cache_->release(cache_ref_);
+        cache_->trim(footprint(N, n));
+    }
+    cache_ref_ = GenCache::Ref{};
+    if (g_[0].alloc(ctx_, bytes, s_) != kOk || g_[1].alloc(ctx_, bytes / 2 + 16, s_) != kOk)
+        return fail(kENoMem, "HBM budget exhausted allocating verifier generators");
+    // one keyed BLAKE3 compression and 16 written bytes per coefficient
+    DM_LAUNCH("gen_generators", bytes, bytes / 16, launch_gen_generators(st_.g_0_seed, N, Ln, g_[0].as<uint4>(), s_));
     return kOk;
 }
 
@@ -319,8 +472,7 @@ int GpuVerifier::update_commitment(const RoundRecord& rec) {
     if (vec) {
         const fq x = tr_.challenge_vec(round_, current_, rec.l_vec, rec.r_vec);
         x_inv = fq_inv(x);
-        Module t;
-        if (!module_add_scaled(current_, rec.l_vec, x_inv, t) || !module_add_scaled(t, rec.r_vec, x, vfc))
+        if (!module_fold(current_, false, rec.l_vec, x_inv, rec.r_vec, x, vfc))
             return fail(kEVerify, "module ring length mismatch");
     } else {
         const Module zero = Module::zero(current_.n);
@@ -335,8 +487,7 @@ int GpuVerifier::update_commitment(const RoundRecord& rec) {
         const fq y = tr_.challenge_poly(round_, vfc, rec.l_poly, rec.r_poly);
         y_inv = fq_inv(y);
         if (vfc.n < 2) return fail(kEVerify, "cannot split scalar commitment");
-        Module t;
-        if (!module_add_scaled(module_even(vfc), rec.l_poly, y_inv, t) || !module_add_scaled(t, rec.r_poly, y, next))
+        if (!module_fold(vfc, true, rec.l_poly, y_inv, rec.r_poly, y, next))
             return fail(kEVerify, "module ring length mismatch");
     } else {
         const Module zero = Module::zero(1);
@@ -347,9 +498,11 @@ int GpuVerifier::update_commitment(const RoundRecord& rec) {
     }
     uint32_t L = 0;
     while ((1u << L) < n_) ++L;
-    cudaError_t e = launch_fold_gen_round(g_[cur_].as<uint4>(), g_[cur_ ^ 1].as<uint4>(), N_, L, x_inv, y_inv, vec,
-                                          poly, s_);
-    if (e != cudaSuccess) return fail(kECuda, std::string("fold_gen_round: ") + cudaGetErrorString(e));
+    // reads the whole family, writes the folded one: two (or one) coefficients in per coefficient out
+    const uint64_t in_elems = (uint64_t)N_ * kRank * n_;
+    const uint64_t out_elems = in_elems >> ((vec ? 1 : 0) + (poly ? 1 : 0));
+    DM_LAUNCH("fold_gen", (in_elems + out_elems) * 16, out_elems,
+              launch_fold_gen_round(source(), g_[cur_ ^ 1].as<uint4>(), N_, L, x_inv, y_inv, vec, poly, s_));
     cur_ ^= 1;
     if (vec) N_ /= 2;
     if (poly) n_ /= 2;
@@ -362,7 +515,16 @@ int GpuVerifier::verify_final_opening(const fq& opening) {
     if (round_ != rounds_) return fail(kEVerify, "cannot verify final opening before all rounds replay");
     if (N_ != 1) return fail(kEVerify, "terminal generator family must have length one");
     std::vector<uint4> g((size_t)kRank * n_);
-    cudaError_t e = cudaMemcpyAsync(g.data(), g_[cur_].as<uint4>(), g.size() * 16, cudaMemcpyDeviceToHost, s_);
+    cudaError_t e = cudaSuccess;
+    if (!own_stream_) {
+        // on a borrowed (service worker's) stream, sleep rather than spin until the
+        // folds are done: the service runs a verifier per core, and a spinning wait
+        // takes a core from another proof's replay
+        e = cudaEventCreateWithFlags(&done_, cudaEventBlockingSync | cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(done_, s_);
+        if (e == cudaSuccess) e = cudaEventSynchronize(done_);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g.data(), source(), g.size() * 16, cudaMemcpyDeviceToHost, s_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
     if (e != cudaSuccess) return fail(kECuda, std::string("D2H generators: ") + cudaGetErrorString(e));
     Module rhs;
@@ -376,37 +538,53 @@ int GpuVerifier::verify_final_opening(const fq& opening) {
 
 // ============================== one-shot ==============================
 
-int verify_proof(Context* ctx, const uint8_t* proof, size_t len, const uint8_t epoch[32]) {
+int verify_proof(Context* ctx, const uint8_t* proof, size_t len, const uint8_t epoch[32], cudaStream_t stream,
+                 GenCache* cache, std::string* err, bool* cache_hit) {
+    if (cache_hit) *cache_hit = false;
+    auto bad = [&](int code, const char* msg) {
+        ctx->set_error(msg);
+        if (err) *err = msg;
+        return code;
+    };
     const uint8_t *p = proof, *end = proof + len;
     Statement st;
-    if (!decode_statement(p, end, st)) {
-        ctx->set_error("statement deserialization failed");
-        return kEDeserialize;
-    }
-    GpuVerifier v(ctx);
+    if (!decode_statement(p, end, st)) return bad(kEDeserialize, "statement deserialization failed");
+    GpuVerifier v(ctx, stream, cache);
+    auto done = [&](int rc) {
+        if (rc != kOk && err && !v.error().empty()) *err = v.error();
+        if (cache_hit) *cache_hit = v.cache_hit();
+        return rc;
+    };
     int rc = v.init(proof, (size_t)(p - proof), epoch);
-    if (rc != kOk) return rc;
-    if (end - p < 8) {
-        ctx->set_error("proof truncated");
-        return kEDeserialize;
-    }
+    if (rc != kOk) return done(rc);
+    if (end - p < 8) return done(bad(kEDeserialize, "proof truncated"));
     uint64_t count = 0;
     for (int i = 7; i >= 0; --i) count = (count << 8) | p[i];
     p += 8;
     for (uint64_t r = 0; r < count; ++r) {
         RoundRecord rec;
-        if (!decode_record(p, end, rec)) {
-            ctx->set_error("round record deserialization failed");
-            return kEDeserialize;
-        }
+        if (!decode_record(p, end, rec)) return done(bad(kEDeserialize, "round record deserialization failed"));
         rc = v.update_commitment(rec);
-        if (rc != kOk) return rc;
+        if (rc != kOk) return done(rc);
     }
-    if (end - p < 16) {
-        ctx->set_error("proof truncated");
-        return kEDeserialize;
-    }
-    return v.verify_final_opening(fq_from_bytes(p));
+    if (end - p < 16) return done(bad(kEDeserialize, "proof truncated"));
+    return done(v.verify_final_opening(fq_from_bytes(p)));
+}
+
+bool proof_shape(const uint8_t* proof, size_t len, uint64_t* N, uint32_t* n, uint64_t* footprint) {
+    const uint8_t* p = proof;
+    Statement st;
+    if (!decode_statement(p, proof + len, st)) return false;
+    uint32_t d;
+    uint64_t dim;
+    if (!square_layout_for_byte_len(st.original_len_bytes, &d, &dim)) return false;
+    const uint32_t ring = st.com_0.n;
+    if (ring == 0 || (ring & (ring - 1)) || ring > (1u << kLogMaxProverRing) || dim > (1u << kLogMaxProverRing))
+        return false;
+    *N = dim;
+    *n = ring;
+    *footprint = GpuVerifier::footprint(dim, ring);
+    return true;
 }
 
 }  // namespace dm

@@ -142,11 +142,55 @@ class DevMem {
     cudaStream_t stream_ = nullptr;
 };
 
+// Initial generator families g_0(seed, N, n) kept in HBM and shared read-only by
+// verifiers.  g_0 depends on nothing but the system seed and the witness shape
+// (src/commitment/sis.rs:198-245), and deployments use one seed for every file
+// (SystemParams::default, src/utils/config.rs:19, 33-44), so a verifier of a stream
+// of proofs expands each shape once.  Entries are charged to the context budget,
+// evicted least recently used when unreferenced, and capped at `cap_bytes`.
+class GenCache {
+   public:
+    struct Ref {
+        const uint4* g = nullptr;
+        cudaEvent_t ready = nullptr;  // recorded after the expansion; readers wait on it
+        void* entry = nullptr;
+    };
+    GenCache(Context* ctx, uint64_t cap_bytes) : ctx_(ctx), cap_(cap_bytes) {}
+    ~GenCache();
+    // The family for (seed, N, 2^log_n); on a miss it is expanded on `s`.  kENoMem
+    // when it does not fit under the cap or the budget (the caller expands its own).
+    int acquire(const uint8_t seed[32], uint64_t N, uint32_t log_n, cudaStream_t s, Ref* out);
+    // After every reader of `r` has finished on the device.
+    void release(const Ref& r);
+    // Evicts unreferenced entries, least recently used first, until `bytes` more
+    // fit under the context budget; false when they still do not.
+    bool trim(uint64_t bytes);
+    struct Stats {
+        uint64_t hits = 0, misses = 0, evictions = 0, bytes = 0, entries = 0;
+    };
+    Stats stats();
+
+   private:
+    struct Entry;
+    bool evict_for(uint64_t bytes);  // called with mu_ held
+    bool evict_one();                // called with mu_ held
+    Context* ctx_;
+    uint64_t cap_;
+    std::mutex mu_;
+    std::map<std::vector<uint8_t>, Entry*> map_;
+    uint64_t clock_ = 0;
+    Stats st_;
+};
+
 // Round-by-round verifier (src/protocol/verifier.rs:11-134): commitments and
 // challenges on the host, generator folds enqueued on the device without syncs.
+// With a stream the verifier borrows it (else it owns one); with a cache the
+// first fold reads the shared g_0 and the verifier holds half and a quarter of
+// it instead of one and a half.
 class GpuVerifier {
    public:
-    explicit GpuVerifier(Context* ctx) : ctx_(ctx) {}
+    explicit GpuVerifier(Context* ctx, cudaStream_t stream = nullptr, GenCache* cache = nullptr)
+        : ctx_(ctx), s_(stream), own_stream_(stream == nullptr), cache_(cache) {}
     ~GpuVerifier();
     int init(const uint8_t* statement, size_t len, const uint8_t epoch_seed[32]);
     int update_commitment(const RoundRecord& rec);
@@ -154,12 +198,19 @@ class GpuVerifier {
     uint64_t round() const { return round_; }
     uint32_t vector_len() const { return N_; }
     uint32_t ring_len() const { return current_.n; }
+    bool cache_hit() const { return cache_ref_.g != nullptr; }
+    const std::string& error() const { return err_; }
     static uint64_t footprint(uint64_t N, uint64_t n);
 
    private:
     int fail(int code, const std::string& msg);
+    const uint4* source() const;  // the family the next fold reads
     Context* ctx_;
     cudaStream_t s_ = nullptr;
+    bool own_stream_ = true;
+    GenCache* cache_ = nullptr;
+    GenCache::Ref cache_ref_{};
+    std::string err_;
     Statement st_{};
     Transcript tr_;
     Module current_;
@@ -167,11 +218,20 @@ class GpuVerifier {
     uint64_t round_ = 0, rounds_ = 0;
     DevMem g_[2];
     int cur_ = 0;
+    cudaEvent_t done_ = nullptr;
 };
 
 // One-shot helpers used by the C ABI.
 int prove_all(Context* ctx, const uint8_t* file, uint64_t len, bool on_device, const uint8_t seed[32],
               const uint8_t epoch[32], std::vector<uint8_t>* proof, double* device_ms = nullptr);
-int verify_proof(Context* ctx, const uint8_t* proof, size_t len, const uint8_t epoch[32]);
+// Decodes and replays a bincode((Statement, Vec<RoundRecord>, Fp)) proof.  With a
+// stream and a cache the verification runs on that stream and shares g_0; with
+// `err` the failure text is returned there as well as set on the context.
+int verify_proof(Context* ctx, const uint8_t* proof, size_t len, const uint8_t epoch[32],
+                 cudaStream_t stream = nullptr, GenCache* cache = nullptr, std::string* err = nullptr,
+                 bool* cache_hit = nullptr);
+// The statement's generator-family shape and the verifier's device footprint
+// (false when the statement does not decode or its shape is unsupported).
+bool proof_shape(const uint8_t* proof, size_t len, uint64_t* N, uint32_t* n, uint64_t* footprint);
 
 }  // namespace dm

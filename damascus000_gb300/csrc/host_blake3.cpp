@@ -222,7 +222,18 @@ void chunk_cvs(void* a, size_t begin, size_t end) {
 
 }  // namespace
 
+namespace {
+thread_local bool t_serial = false;
+}  // namespace
+
+HostSerialScope::HostSerialScope() : prev_(t_serial) { t_serial = true; }
+HostSerialScope::~HostSerialScope() { t_serial = prev_; }
+
 void host_parallel_for(size_t n, size_t min_per_task, void (*fn)(void*, size_t, size_t), void* arg) {
+    if (t_serial) {
+        fn(arg, 0, n);
+        return;
+    }
     Pool& P = Pool::get();
     size_t tasks = (n + min_per_task - 1) / (min_per_task ? min_per_task : 1);
     if (tasks > P.size()) tasks = P.size();
@@ -240,7 +251,7 @@ void host_parallel_for(size_t n, size_t min_per_task, void (*fn)(void*, size_t, 
 
 void blake3_hash_parallel(const void* data, size_t len, uint8_t out[32]) {
     const size_t nchunks = (len + kB3ChunkLen - 1) / kB3ChunkLen;
-    if (len < (64u << 10) || nchunks < 2) {
+    if (len < (64u << 10) || nchunks < 2 || t_serial) {
         blake3_hash(data, len, out);
         return;
     }

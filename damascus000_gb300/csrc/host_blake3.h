@@ -38,6 +38,21 @@ void blake3_hash_parallel(const void* data, size_t len, uint8_t out[32]);
 
 // Fixed pool of host threads: fn(begin, end) over a split of [0, n).
 void host_parallel_for(size_t n, size_t min_per_task, void (*fn)(void*, size_t, size_t), void* arg);
+
+// While alive, host_parallel_for and blake3_hash_parallel run on the calling
+// thread alone: for callers that already keep every core busy with independent
+// work (a verifier worker per core), where splitting each hash over the pool
+// only adds hand-offs.  Results are unchanged.
+class HostSerialScope {
+   public:
+    HostSerialScope();
+    ~HostSerialScope();
+    HostSerialScope(const HostSerialScope&) = delete;
+    HostSerialScope& operator=(const HostSerialScope&) = delete;
+
+   private:
+    bool prev_;
+};
 void blake3_keyed_hash(const uint8_t key[32], const void* data, size_t len, uint8_t out[32]);
 
 }  // namespace dm

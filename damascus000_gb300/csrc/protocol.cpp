@@ -129,6 +129,37 @@ bool module_add_scaled(const Module& a, const Module& b, const fq& s, Module& ou
     return true;
 }
 
+namespace {
+struct FoldArgs {
+    const fq* base;
+    const fq* l;
+    const fq* r;
+    fq sl, sr;
+    fq* out;
+    uint32_t step;  // 2 for the even coefficients of base, else 1
+};
+void fold_range(void* p, size_t begin, size_t end) {
+    const FoldArgs* A = static_cast<const FoldArgs*>(p);
+    // coordinate k, coefficient j of the output is coefficient step*j of the
+    // base's coordinate k: index (k*n + j) * step = i * step
+    for (size_t i = begin; i < end; ++i)
+        A->out[i] = fq_fma(fq_fma(A->base[i * A->step], A->sl, A->l[i]), A->sr, A->r[i]);
+}
+}  // namespace
+
+bool module_fold(const Module& base, bool even, const Module& l, const fq& sl, const Module& r, const fq& sr,
+                 Module& out) {
+    const uint32_t n = even ? base.n / 2 : base.n;
+    if (l.n != n || r.n != n || (even && base.n < 2)) return false;
+    Module m;
+    m.n = n;
+    m.c.resize((size_t)kRank * n);
+    FoldArgs args{base.c.data(), l.c.data(), r.c.data(), sl, sr, m.c.data(), even ? 2u : 1u};
+    host_parallel_for(m.c.size(), 2048, fold_range, &args);
+    out = std::move(m);
+    return true;
+}
+
 Module module_even(const Module& a) {
     Module r = Module::zero(a.n / 2);
     for (int k = 0; k < kRank; ++k)
@@ -194,7 +225,10 @@ static void append_commitment(std::vector<uint8_t>& msg, const Module& m) {
 // transcript.rs:42-75: the absorbed bytes are assembled once and hashed in
 // parallel; only the trailing u32 counter changes between attempts.
 fq Transcript::challenge(const char* label, uint64_t round, const Module& c, const Module& l, const Module& r) const {
-    std::vector<uint8_t> msg;
+    // one buffer per thread, reused: a fresh multi-megabyte vector per challenge
+    // costs a page fault per 4 KiB
+    thread_local std::vector<uint8_t> msg;
+    msg.clear();
     msg.reserve(128 + 3 * (8 + (size_t)kRank * 8) + 16 * (c.c.size() + l.c.size() + r.c.size()));
     msg.insert(msg.end(), epoch_seed_, epoch_seed_ + 32);
     const size_t ll = std::strlen(label);

@@ -63,6 +63,12 @@ bool decode_statement(const uint8_t*& p, const uint8_t* end, Statement& s);
 // a + s * b; false on ring length mismatch (module.rs:34-59).
 bool module_add_scaled(const Module& a, const Module& b, const fq& s, Module& out);
 Module module_even(const Module& a);
+// One verifier commitment update in a single pass: out = b + sl*l + sr*r with b =
+// base, or its even coefficients when `even` (src/protocol/verifier.rs:64-103),
+// each coefficient through the same two fused multiply-adds as two calls of
+// module_add_scaled.  False when the ring lengths differ.
+bool module_fold(const Module& base, bool even, const Module& l, const fq& sl, const Module& r, const fq& sr,
+                 Module& out);
 
 // ---- layout (src/utils/io.rs:72-120) ----
 uint64_t coeff_count_for_byte_len(uint64_t len);

@@ -193,6 +193,33 @@ int damascus_engine_stats(damascus_engine* e, uint64_t* completed, uint64_t* fai
  * requests were unfinished. */
 int damascus_engine_profile(damascus_engine* e, double* host_stage_ms, double* gpu_idle_ms);
 
+/* Streaming verifier service (no counterpart in the reference, which verifies
+ * one proof at a time through DamascusVerifier, src/protocol/verifier.rs:22-134).
+ * Proofs in the damascus_prove() container are verified by `workers` threads
+ * (<= 0: one per host core, at most 16), each on its own stream, admitted in
+ * arrival order against the context's HBM budget.  Initial generator families
+ * g_0(seed, N, n) are kept in HBM, up to cache_bytes (0 disables), and shared by
+ * proofs of the same shape and system seed.  Each verdict equals
+ * damascus_verify()'s on the same bytes. */
+typedef struct damascus_verify_service damascus_verify_service;
+int damascus_verify_service_create(damascus_ctx* ctx, int workers, uint64_t cache_bytes,
+                                   damascus_verify_service** out);
+/* Finishes the submitted proofs, then frees the service. */
+void damascus_verify_service_destroy(damascus_verify_service* s);
+/* Copies the proof and returns at once with a ticket. */
+int damascus_verify_service_submit(damascus_verify_service* s, const uint8_t* proof, size_t len,
+                                   const uint8_t epoch_seed[32], uint64_t* ticket);
+/* 1 = finished: *verdict = DAMASCUS_OK for an accepted proof, else the code
+ * damascus_verify() returns (its text via damascus_last_error); the ticket is
+ * then forgotten.  0 = still running; DAMASCUS_EINVAL = unknown ticket. */
+int damascus_verify_service_poll(damascus_verify_service* s, uint64_t ticket, int* verdict, double* latency_ms);
+/* Blocks until the ticket finishes; same results as poll. */
+int damascus_verify_service_wait(damascus_verify_service* s, uint64_t ticket, int* verdict, double* latency_ms);
+int damascus_verify_service_drain(damascus_verify_service* s);
+int damascus_verify_service_stats(damascus_verify_service* s, uint64_t* completed, uint64_t* accepted,
+                                  uint64_t* rejected, uint64_t* cache_hits, uint64_t* cache_misses,
+                                  uint64_t* peak_reserved_bytes);
+
 /* ------------------------------------------------------------------ reference FFI */
 /* Drop-in for the reference's own CUDA hooks, same signatures and argument
  * meaning (src/utils/gpu.rs:69-93; cuda/fold_kernel.cu:209, cuda/ntt_kernel.cu:106).
