@@ -7,6 +7,8 @@ Workloads (seeded ChaCha20 random files; no public dataset is involved):
           seeds, 150 GB HBM budget.  A step replays the whole stream.
   batched 64 files, log-uniform 50 KB-4 MiB (d = 6..10), one engine batch per step.
   d6/d9/d11  the plain single-proof full flows (53,248 B / 1 MiB / 16 MiB).
+  serve_seed  the serving stream with every file under the default system seed and
+          the provers' generator cache on (each shape expanded and transformed once).
   verify  the serving stream's files proven under the default system seed, then
           verified by the streaming verifier service; a step verifies every proof.
 
@@ -63,6 +65,10 @@ WORKLOADS = {
                    desc="verifier stream: proofs of the serving stream's 96 files (d 6-11) under the default "
                         "system seed, verified by the streaming verifier service (16 GiB generator cache)"),
 }
+WORKLOADS["serve_seed"] = dict(kind="serve", requests=96, rate=200.0, system_seed=True, generator_cache=16 << 30,
+                               desc="serving stream under one system seed (SystemParams default) with the provers' "
+                                    "generator cache (16 GiB): Poisson 200 req/s, 50% 50KB-1MiB / 40% 1-8MiB / "
+                                    "10% 16MiB, 150 GB HBM budget")
 WORKLOADS["verify16m"] = dict(kind="verify", requests=32, file_bytes=16 << 20, rate=200.0, cache_bytes=16 << 30,
                               desc="verifier stream of large proofs: 32 proofs of 16 MiB files (d = 11, 2048 x "
                                    "2048 witness) under the default system seed, streaming verifier service "
@@ -132,7 +138,7 @@ def workload_files(wl, rank: int = 0):
     if wl["kind"] in ("serve", "verify"):
         reqs = synth.serving_stream(base, wl["requests"], wl["rate"])
         files = [synth.random_file(base, r.size, 10_000 + r.index) + (r.arrival_s,) for r in reqs]
-        if wl["kind"] == "verify":  # one system seed for every file, as SystemParams::default
+        if wl["kind"] == "verify" or wl.get("system_seed"):  # one seed for every file, as SystemParams::default
             files = [(d, SYSTEM_SEED, a) for d, _, a in files]
         return files
     if wl["kind"] == "batched":
@@ -393,6 +399,8 @@ def run_gpu(args, wl):
     barrier, max_over_ranks = ranks.barrier, ranks.max
 
     ctx = D.Context(local, hbm_budget_bytes=SERVE_BUDGET if wl["kind"] != "plain" else 0)
+    if wl.get("generator_cache"):
+        ctx.set_generator_cache(wl["generator_cache"])
     cpu_inputs = None  # the verify workloads time the oracle verifier on their own proofs
     line = {"metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/u128 integer",
@@ -717,7 +725,8 @@ def run_gpu(args, wl):
                                 "waves_per_step": (st1["waves"] - st0["waves"]) / args.steps,
                                 "launches_per_step": (st1["launches"] - st0["launches"]) / args.steps,
                                 "gpu_idle_ms_per_step": (st1["gpu_idle_ms"] - st0["gpu_idle_ms"]) / args.steps,
-                                "host_stage_ms_per_step": (st1["host_stage_ms"] - st0["host_stage_ms"]) / args.steps},
+                                "host_stage_ms_per_step": (st1["host_stage_ms"] - st0["host_stage_ms"]) / args.steps,
+                                "generator_cache": ctx.generator_cache_stats() if wl.get("generator_cache") else None},
                      "e2e": {"value": world * total / MIB / e2e_s, "unit": UNIT, "h2d_bytes_per_step": total,
                              "d2h_bytes_per_step": d2h},
                      "plain_mib_s": plain, "serving_vs_plain": value / plain,

@@ -61,7 +61,7 @@ EXPORTED_SYMBOLS = (
     "damascus_tuning_set", "damascus_tuning_get", "damascus_tuning_measure",
     "damascus_verify_service_create", "damascus_verify_service_destroy", "damascus_verify_service_submit",
     "damascus_verify_service_poll", "damascus_verify_service_wait", "damascus_verify_service_drain",
-    "damascus_verify_service_stats",
+    "damascus_verify_service_stats", "damascus_ctx_set_generator_cache", "damascus_ctx_generator_cache_stats",
 )
 
 
@@ -170,6 +170,8 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_tuning_set", i32, vp, i32, u32, i32)
     sig("damascus_tuning_get", i32, vp, i32, u32, P(i32))
     sig("damascus_tuning_measure", i32, vp, i32, u32, i32, u32, i32, P(ctypes.c_double))
+    sig("damascus_ctx_set_generator_cache", i32, vp, u64)
+    sig("damascus_ctx_generator_cache_stats", i32, vp, P(u64), P(u64), P(u64), P(u64))
     sig("damascus_verify_service_create", i32, vp, i32, u64, P(vp))
     sig("damascus_verify_service_destroy", None, vp)
     sig("damascus_verify_service_submit", i32, vp, cp, sz, cp, P(u64))
@@ -333,6 +335,18 @@ class Context:
     @property
     def reserved(self) -> int:
         return self._lib.damascus_ctx_reserved(self._h)
+
+    # -- provers' generator cache (damascus_ctx_set_generator_cache)
+    def set_generator_cache(self, cap_bytes: int) -> None:
+        """Keep provers' initial generator families and their transforms in HBM
+        (a key is cached on its second sighting); 0 turns the cache off."""
+        self.check(self._lib.damascus_ctx_set_generator_cache(self._h, cap_bytes), "set_generator_cache")
+
+    def generator_cache_stats(self) -> dict:
+        v = [ctypes.c_uint64() for _ in range(4)]
+        self.check(self._lib.damascus_ctx_generator_cache_stats(self._h, *[ctypes.byref(x) for x in v]),
+                   "generator_cache_stats")
+        return dict(zip(("hits", "fills", "misses", "bytes"), (x.value for x in v)))
 
     # -- launch-shape tuning (damascus_tuning_*; autotune.py measures and sets them)
     def tuning_set(self, knob: int, log_ring: int, value: int) -> None:

@@ -473,6 +473,26 @@ int damascus_ctx_flush_l2(damascus_ctx* ctx) {
     return ctx->ctx->flush_l2();
 }
 
+// ------------------------------------------------------------------ generator cache
+int damascus_ctx_set_generator_cache(damascus_ctx* ctx, uint64_t cap_bytes) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    if (ctx->ctx->set_prover_cache(cap_bytes) != kOk)
+        return set_err(ctx, DAMASCUS_ESTATE, "a running prover holds a cached generator family");
+    return DAMASCUS_OK;
+}
+
+int damascus_ctx_generator_cache_stats(damascus_ctx* ctx, uint64_t* hits, uint64_t* fills, uint64_t* misses,
+                                       uint64_t* bytes) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    ProverGenCache::Stats st{};
+    if (ctx->ctx->prover_cache()) st = ctx->ctx->prover_cache()->stats();
+    if (hits) *hits = st.hits;
+    if (fills) *fills = st.fills;
+    if (misses) *misses = st.misses;
+    if (bytes) *bytes = st.bytes;
+    return DAMASCUS_OK;
+}
+
 // ------------------------------------------------------------------ tuning
 int damascus_tuning_set(damascus_ctx* ctx, int knob, uint32_t log_ring, int value) {
     if (!ctx) return DAMASCUS_EINVAL;

@@ -84,6 +84,17 @@ uint32_t Context::mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uin
     return parts ? parts : 1;
 }
 
+int Context::set_prover_cache(uint64_t cap_bytes) {
+    cudaSetDevice(device_);
+    if (prover_cache_) {
+        // the old cache goes once nothing holds it: every entry must be unreferenced
+        if (!prover_cache_->trim(~0ull >> 1) && prover_cache_->bytes() > 0) return kEState;
+        prover_cache_.reset();
+    }
+    if (cap_bytes) prover_cache_.reset(new ProverGenCache(this, cap_bytes));
+    return kOk;
+}
+
 int Context::flush_l2() {
     constexpr size_t kFlushBytes = 256ull << 20;
     cudaSetDevice(device_);
@@ -118,6 +129,7 @@ void Context::put_pinned(void* p, size_t bytes) {
 
 Context::~Context() {
     cudaSetDevice(device_);
+    prover_cache_.reset();  // returns its budget while the accounting is alive
     if (stream_) cudaStreamSynchronize(stream_);
     if (flush_buf_) cudaFree(flush_buf_);
     for (auto& pp : pinned_free_) cudaFreeHost(pp.second);
@@ -385,6 +397,178 @@ void GenCache::release(const Ref& r) {
 }
 
 GenCache::Stats GenCache::stats() {
+    std::lock_guard<std::mutex> g(mu_);
+    return st_;
+}
+
+// ============================== ProverGenCache ==============================
+
+struct ProverGenCache::Entry {
+    void* g = nullptr;
+    void* ghat = nullptr;
+    uint64_t bytes = 0;
+    cudaEvent_t ready = nullptr;
+    int refs = 0;
+    uint64_t last_use = 0;
+    bool published = false;  // the fill is enqueued and `ready` recorded
+    bool poisoned = false;
+    const void* filler = nullptr;  // the plan that fills it, until published
+};
+
+uint64_t ProverGenCache::entry_bytes(uint32_t L) {
+    const uint64_t S2 = 1ull << (2 * L);
+    return 8 * S2 * 16 + 8 * S2 * kPrimes * 4;
+}
+
+ProverGenCache::~ProverGenCache() {
+    std::lock_guard<std::mutex> g(mu_);
+    for (auto& kv : map_) {
+        Entry* e = kv.second;
+        if (e->ready) cudaEventSynchronize(e->ready);
+        cudaFree(e->g);
+        cudaFree(e->ghat);
+        ctx_->release(e->bytes);
+        if (e->ready) cudaEventDestroy(e->ready);
+        delete e;
+    }
+    map_.clear();
+}
+
+bool ProverGenCache::evict_one() {
+    auto victim = map_.end();
+    for (auto it = map_.begin(); it != map_.end(); ++it)
+        if (it->second->refs == 0 && (victim == map_.end() || it->second->last_use < victim->second->last_use))
+            victim = it;
+    if (victim == map_.end()) return false;
+    Entry* e = victim->second;
+    // holders release after their last reading stage completed on the device
+    cudaFree(e->g);
+    cudaFree(e->ghat);
+    ctx_->release(e->bytes);
+    cudaEventDestroy(e->ready);
+    st_.bytes -= e->bytes;
+    st_.entries -= 1;
+    st_.evictions += 1;
+    delete e;
+    map_.erase(victim);
+    return true;
+}
+
+int ProverGenCache::acquire(const uint8_t g0_seed[32], uint32_t L, const void* plan, Ref* out) {
+    std::vector<uint8_t> key(g0_seed, g0_seed + 32);
+    key.push_back((uint8_t)L);
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = map_.find(key);
+    if (it != map_.end()) {
+        Entry* e = it->second;
+        const bool same_plan = !e->published && plan && e->filler == plan;
+        if (e->poisoned || (!e->published && !same_plan)) {
+            // still being filled by a stage not yet enqueued (an event not yet
+            // recorded cannot be waited on), or dropped by its last holder
+            st_.misses += 1;
+            return kENoMem;
+        }
+        e->refs += 1;
+        e->last_use = ++clock_;
+        st_.hits += 1;
+        // in the filling plan itself the stream order covers the fill: no wait
+        *out = Ref{static_cast<uint4*>(e->g), static_cast<uint32_t*>(e->ghat), same_plan ? nullptr : e->ready, e,
+                   false};
+        return kOk;
+    }
+    // first sighting: remember the key only (bounded; forgotten wholesale when full)
+    int& seen = seen_[key];
+    if (seen++ == 0) {
+        if (seen_.size() > 4096) seen_.clear();
+        st_.misses += 1;
+        return kENoMem;
+    }
+    const uint64_t bytes = entry_bytes(L);
+    if (bytes > cap_) {
+        st_.misses += 1;
+        return kENoMem;
+    }
+    for (;;) {
+        if (st_.bytes + bytes <= cap_ && ctx_->reserve(bytes)) break;
+        if (!evict_one()) {
+            st_.misses += 1;
+            return kENoMem;
+        }
+    }
+    Entry* e = new Entry;
+    e->bytes = bytes;
+    const uint64_t S2 = 1ull << (2 * L);
+    if (cudaMalloc(&e->g, 8 * S2 * 16) != cudaSuccess || cudaMalloc(&e->ghat, 8 * S2 * kPrimes * 4) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->ready, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        if (e->g) cudaFree(e->g);
+        if (e->ghat) cudaFree(e->ghat);
+        if (e->ready) cudaEventDestroy(e->ready);
+        ctx_->release(bytes);
+        delete e;
+        st_.misses += 1;
+        return kENoMem;
+    }
+    e->refs = 1;
+    e->last_use = ++clock_;
+    e->filler = plan;
+    map_[key] = e;
+    st_.bytes += bytes;
+    st_.entries += 1;
+    st_.fills += 1;
+    *out = Ref{static_cast<uint4*>(e->g), static_cast<uint32_t*>(e->ghat), e->ready, e, true};
+    return kOk;
+}
+
+void ProverGenCache::release(const Ref& r) {
+    if (!r.entry) return;
+    std::lock_guard<std::mutex> g(mu_);
+    Entry* e = static_cast<Entry*>(r.entry);
+    e->refs -= 1;
+    if (e->poisoned && e->refs == 0) {
+        for (auto it = map_.begin(); it != map_.end(); ++it)
+            if (it->second == e) {
+                cudaFree(e->g);
+                cudaFree(e->ghat);
+                ctx_->release(e->bytes);
+                cudaEventDestroy(e->ready);
+                st_.bytes -= e->bytes;
+                st_.entries -= 1;
+                delete e;
+                map_.erase(it);
+                break;
+            }
+    }
+}
+
+void ProverGenCache::publish(const Ref& r) {
+    if (!r.entry) return;
+    std::lock_guard<std::mutex> g(mu_);
+    static_cast<Entry*>(r.entry)->published = true;
+    static_cast<Entry*>(r.entry)->filler = nullptr;
+}
+
+void ProverGenCache::poison(const Ref& r) {
+    if (!r.entry) return;
+    std::lock_guard<std::mutex> g(mu_);
+    static_cast<Entry*>(r.entry)->poisoned = true;
+    static_cast<Entry*>(r.entry)->filler = nullptr;
+}
+
+bool ProverGenCache::trim(uint64_t bytes) {
+    std::lock_guard<std::mutex> g(mu_);
+    for (;;) {
+        if (ctx_->reserved() + bytes <= ctx_->budget()) return true;
+        if (!evict_one()) return false;
+    }
+}
+
+uint64_t ProverGenCache::bytes() {
+    std::lock_guard<std::mutex> g(mu_);
+    return st_.bytes;
+}
+
+ProverGenCache::Stats ProverGenCache::stats() {
     std::lock_guard<std::mutex> g(mu_);
     return st_;
 }

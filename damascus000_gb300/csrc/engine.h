@@ -40,6 +40,8 @@ struct KernelStat {
     double ops = 0.0;    // algorithmic integer operations
 };
 
+class ProverGenCache;
+
 class Context {
    public:
     static int create(int device, uint64_t hbm_budget, Context** out, std::string* err);
@@ -82,7 +84,13 @@ class Context {
     uint32_t mac_parts(int knob, uint32_t L, uint32_t threads_per_row, uint32_t count) const;
     uint32_t mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uint32_t count) const;
 
+    // Provers' generator cache (off until a capacity is set; 0 turns it off and
+    // frees it once no prover holds an entry).  Set it before proving starts.
+    int set_prover_cache(uint64_t cap_bytes);
+    ProverGenCache* prover_cache() const { return prover_cache_.get(); }
+
    private:
+    std::unique_ptr<ProverGenCache> prover_cache_;
     int device_ = 0;
     int sm_count_ = 152;
     std::atomic<int> tune_[kTuneKnobs][kLogMaxProverRing + 1];
@@ -178,6 +186,61 @@ class GenCache {
     uint64_t cap_;
     std::mutex mu_;
     std::map<std::vector<uint8_t>, Entry*> map_;
+    uint64_t clock_ = 0;
+    Stats st_;
+};
+
+// Initial generator families of provers with their forward transforms, kept in
+// HBM: g_0(seed, S) as coefficients ([S][8][S], 16 B each) and as nine-prime
+// residues ([S][8][9][S] words), the two forms the commitment stage reads.  A
+// key is cached the second time it is seen, so a stream of per-file seeds never
+// pays for a fill while a deployment proving every file under one seed expands
+// and transforms each shape once.  The prover that fills an entry writes it in
+// its own Init stage (expansion and a transform of every column), records
+// `ready` after that stage and publishes the entry; readers that acquire it
+// afterwards wait on `ready`.  Entries are charged to the
+// context budget and evicted least recently used when unreferenced.
+class ProverGenCache {
+   public:
+    struct Ref {
+        uint4* g = nullptr;
+        uint32_t* ghat = nullptr;
+        cudaEvent_t ready = nullptr;
+        void* entry = nullptr;
+        bool fill = false;  // the caller writes the entry and records `ready` after
+    };
+    ProverGenCache(Context* ctx, uint64_t cap_bytes) : ctx_(ctx), cap_(cap_bytes) {}
+    ~ProverGenCache();
+    static uint64_t entry_bytes(uint32_t L);
+    // kOk with a hit or a fill; kENoMem when the key is not cached (first
+    // sighting, no room under the cap or the budget, or a fill not yet enqueued by
+    // another plan): the caller uses its own buffers.  `plan` identifies the
+    // caller's stage plan: requests in the plan that fills an entry share it (their
+    // stream runs the fill first) with no event to wait on (ready is null).
+    int acquire(const uint8_t g0_seed[32], uint32_t L, const void* plan, Ref* out);
+    // After the holder's last reading stage has finished on the device.
+    void release(const Ref& r);
+    // A fill whose stage is enqueued with `ready` recorded after it: from now on
+    // the entry is handed out.  Until then other provers use their own buffers.
+    void publish(const Ref& r);
+    // A fill whose stage failed to launch: the entry is dropped when unreferenced
+    // and never handed out again.
+    void poison(const Ref& r);
+    bool trim(uint64_t bytes);  // evicts unreferenced entries until `bytes` more fit the budget
+    uint64_t bytes();
+    struct Stats {
+        uint64_t hits = 0, fills = 0, misses = 0, evictions = 0, bytes = 0, entries = 0;
+    };
+    Stats stats();
+
+   private:
+    struct Entry;
+    bool evict_one();  // called with mu_ held
+    Context* ctx_;
+    uint64_t cap_;
+    std::mutex mu_;
+    std::map<std::vector<uint8_t>, Entry*> map_;
+    std::map<std::vector<uint8_t>, int> seen_;
     uint64_t clock_ = 0;
     Stats st_;
 };

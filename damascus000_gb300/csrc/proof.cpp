@@ -52,6 +52,9 @@ void Plan::clear() {
         finish[L].clear();
     }
     d2h.clear();
+    wait_events.clear();
+    record_events.clear();
+    fills.clear();
 }
 
 bool Plan::empty() const {
@@ -65,8 +68,24 @@ bool Plan::empty() const {
 }
 
 int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
+    const int n = launch_all(ctx, st, err);
+    for (auto& f : fills) {
+        if (n < 0) ctx->prover_cache()->poison(f);
+        else ctx->prover_cache()->publish(f);
+    }
+    return n;
+}
+
+int Plan::launch_all(Context* ctx, cudaStream_t st, std::string* err) {
     const DeviceTables& T = ctx->tables();
     int launches = 0;
+    for (cudaEvent_t e : wait_events) {
+        const cudaError_t we = cudaStreamWaitEvent(st, e, 0);
+        if (we != cudaSuccess) {
+            *err = std::string("wait for a cached generator family: ") + cudaGetErrorString(we);
+            return kECuda;
+        }
+    }
     const bool prof = ctx->profiling();
     auto timed = [&](const char* name, double bytes, double ops, auto&& body) -> int {
         cudaEvent_t a = nullptr;
@@ -178,6 +197,13 @@ int Plan::launch(Context* ctx, cudaStream_t st, std::string* err) {
              })))
             return rc;
     }
+    for (cudaEvent_t e : record_events) {
+        const cudaError_t re = cudaEventRecord(e, st);
+        if (re != cudaSuccess) {
+            *err = std::string("record a cached generator family: ") + cudaGetErrorString(re);
+            return kECuda;
+        }
+    }
     for (auto& c : d2h) {
         cudaError_t e = cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) {
@@ -201,7 +227,15 @@ uint64_t ProofState::footprint(uint64_t len) {
            r((uint64_t)kSlots * kRank * S * 16) + r(64);
 }
 
+const uint4* ProofState::g_round0() const { return cached_.g ? cached_.g : g_a_.as<uint4>(); }
+
 void ProofState::release() {
+    if (cached_.entry) {
+        // a request ends only after its last stage's copies landed: nothing of it
+        // still reads the entry
+        ctx_->prover_cache()->release(cached_);
+        cached_ = ProverGenCache::Ref{};
+    }
     DevMem* all[] = {&file_, &hash_scratch_, &m_a_, &m_b_, &g_a_, &g_b_, &mhat_, &ghat_, &partials_, &comm_, &misc_};
     for (DevMem* m : all) m->reset();
     if (pinned_) ctx_->put_pinned(pinned_, pinned_bytes_);
@@ -255,17 +289,24 @@ int ProofState::setup(const uint8_t* file, uint64_t len, bool on_device, const u
     auto need = [&](DevMem& m, size_t bytes) {
         if (rc == kOk) rc = m.alloc(ctx_, bytes, stream);
     };
-    if (!on_device) need(file_, len + 16);
-    need(hash_scratch_, file_hash_scratch_words(len) * 4);
-    need(m_a_, S2 * 16);
-    need(m_b_, S2 / 2 * 16);
-    need(g_a_, 8 * S2 * 16);
-    need(g_b_, 4 * S2 * 16);
-    need(mhat_, S2 * kPrimes * 4);
-    need(ghat_, 8 * S2 * kPrimes * 4);
-    need(partials_, 3ull * kMaxParts * kRows * S * 4);
-    need(comm_, (uint64_t)kSlots * kRank * S * 16);
-    need(misc_, 64);
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        rc = kOk;
+        if (!on_device) need(file_, len + 16);
+        need(hash_scratch_, file_hash_scratch_words(len) * 4);
+        need(m_a_, S2 * 16);
+        need(m_b_, S2 / 2 * 16);
+        need(g_a_, 8 * S2 * 16);
+        need(g_b_, 4 * S2 * 16);
+        need(mhat_, S2 * kPrimes * 4);
+        need(ghat_, 8 * S2 * kPrimes * 4);
+        need(partials_, 3ull * kMaxParts * kRows * S * 4);
+        need(comm_, (uint64_t)kSlots * kRank * S * 16);
+        need(misc_, 64);
+        if (rc == kOk || !ctx_->prover_cache()) break;
+        // the budget is held by cached generator families: drop unreferenced ones, once
+        release();
+        if (!ctx_->prover_cache()->trim(footprint(len))) break;
+    }
     if (rc != kOk) return fail(rc, "HBM budget exhausted allocating prover state (" + std::to_string(footprint(len)) + " bytes)");
     pinned_bytes_ = 3ull * kRank * S * 16 + kTail;
     pinned_ = static_cast<uint8_t*>(ctx_->get_pinned(pinned_bytes_));
@@ -292,13 +333,14 @@ int ProofState::setup(const uint8_t* file, uint64_t len, bool on_device, const u
 // columns and the generator columns [0, c) and [cols/2, cols/2 + c) are
 // transformed and read, and R is zero.  Returns whether the cross terms exist.
 bool ProofState::plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, const uint4* m_src, const uint4* g_src,
-                             uint32_t* part) {
+                             uint32_t* part, uint32_t* ghat, bool g_transformed) {
     const uint64_t s = 1ull << L;
     uint32_t* mh = mhat_.as<uint32_t>();
-    uint32_t* gh = ghat_.as<uint32_t>();
+    uint32_t* gh = ghat ? ghat : ghat_.as<uint32_t>();
     const uint64_t gcol_in = 8 * s, gcol_out = 8 * (uint64_t)kPrimes * s;  // one generator column
     auto ntt = [&](const uint4* src, uint32_t* dst, uint64_t polys) {
-        if (polys) P.ntt[L].push_back(NttJob{src, dst, polys, 0});
+        // generator columns that are already in `ghat` (a cached family) are not transformed again
+        if (polys && !(g_transformed && dst != mh)) P.ntt[L].push_back(NttJob{src, dst, polys, 0});
     };
     if (cols < 2) {
         ntt(m_src, mh, c);
@@ -345,8 +387,26 @@ void ProofState::plan_stage(Plan& P) {
         g.dst = g_a_.as<uint4>();
         g.total = 8 * S2;
         g.log_n = L;
-        P.gen.push_back(g);
-        const bool nj = plan_commit(P, L, S, mcols_ < S ? mcols_ : S, m_a_.as<uint4>(), g_a_.as<uint4>(), part);
+        ProverGenCache* cache = ctx_->prover_cache();
+        cached_ = ProverGenCache::Ref{};
+        if (cache && cache->acquire(st_.g_0_seed, L, &P, &cached_) == kOk) {
+            if (cached_.fill) {
+                // expand into the entry and transform every column (later holders
+                // may have more nonzero witness columns than this file)
+                g.dst = cached_.g;
+                P.gen.push_back(g);
+                P.ntt[L].push_back(NttJob{cached_.g, cached_.ghat, 8ull * S, 0});
+                P.record_events.push_back(cached_.ready);
+                P.fills.push_back(cached_);
+            } else if (cached_.ready) {
+                P.wait_events.push_back(cached_.ready);
+            }
+        } else {
+            cached_ = ProverGenCache::Ref{};
+            P.gen.push_back(g);
+        }
+        const bool nj = plan_commit(P, L, S, mcols_ < S ? mcols_ : S, m_a_.as<uint4>(), g_round0(), part,
+                                    cached_.ghat, cached_.ghat != nullptr);
         if (nj) {
             const size_t pstride = (size_t)parts_ * kRows * S;
             P.finish[L].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
@@ -366,8 +426,8 @@ void ProofState::plan_stage(Plan& P) {
     if (stage_ == Stage::Vec) {
         P.fold.push_back(FoldJob{m_b_.as<uint4>(), m_a_.as<uint4>(), m_a_.as<uint4>() + (uint64_t)h * s, nullptr, x_,
                                  fq_zero(), (uint64_t)h * s, kFoldVec, 0});
-        P.fold.push_back(FoldJob{g_b_.as<uint4>(), g_a_.as<uint4>(), g_a_.as<uint4>() + 4 * s2, nullptr, xi_, fq_zero(),
-                                 4 * s2, kFoldVec, 0});
+        const uint4* gsrc = round_ == 0 ? g_round0() : g_a_.as<uint4>();
+        P.fold.push_back(FoldJob{g_b_.as<uint4>(), gsrc, gsrc + 4 * s2, nullptr, xi_, fq_zero(), 4 * s2, kFoldVec, 0});
         P.fold.push_back(FoldJob{cs(kCt), cs(kC), cs(kL), cs(kR), xi_, x_, (uint64_t)kRank * s, kCombine, 0});
         // the folded witness has h columns, of which the first c can be nonzero:
         // the check and both cross terms only need those columns
@@ -435,6 +495,11 @@ int ProofState::complete_stage() {
     }
     const uint32_t L = d_ - (uint32_t)round_, s = 1u << L, h = s / 2;
     if (stage_ == Stage::Vec) {
+        if (round_ == 0 && cached_.entry) {
+            // round 0's vector stage was the last reader of the cached family
+            ctx_->prover_cache()->release(cached_);
+            cached_ = ProverGenCache::Ref{};
+        }
         if (fl[0]) return fail(kEInvariant, "vector folding invariant failed");  // prover.rs:204-207
         unpack_module(pinned_, s, ct_);
         unpack_module(pinned_ + slot * 16, h, lp_);

@@ -38,10 +38,21 @@ class Plan {
     std::vector<MacJobX> mac, split, triple;
     std::vector<FinishJobX> finish[kLogMaxProverRing + 1];
     std::vector<Copy> d2h;
+    // Cached generator families: events the stream waits on before the first
+    // launch (entries other stages filled) and events recorded after the last
+    // (entries this plan fills), with the fills' references for poisoning when
+    // the plan fails to launch.
+    std::vector<cudaEvent_t> wait_events, record_events;
+    std::vector<ProverGenCache::Ref> fills;
     // Launches every non-empty job kind in dependency order on `st`, then the copies.
     // Returns the number of kernel launches, or a negative status.
     int launch(Context* ctx, cudaStream_t st, std::string* err);
     void clear();
+
+   private:
+    int launch_all(Context* ctx, cudaStream_t st, std::string* err);
+
+   public:
     bool empty() const;
 };
 
@@ -81,7 +92,8 @@ class ProofState {
    private:
     int fail(int code, const std::string& msg);
     bool plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, const uint4* m_src, const uint4* g_src,
-                     uint32_t* part);
+                     uint32_t* part, uint32_t* ghat = nullptr, bool g_transformed = false);
+    const uint4* g_round0() const;  // the family round 0's vector fold reads
     Context* ctx_;
     cudaStream_t alloc_stream_ = nullptr;
     Stage stage_ = Stage::Init;
@@ -108,6 +120,9 @@ class ProofState {
     uint32_t mcols_ = 0;
     uint8_t seed_[32];
     uint8_t epoch_copy_[32];
+    // g_0 and its transform from the context's cache, held from the Init stage
+    // until round 0's vector stage (the last reader) has completed
+    ProverGenCache::Ref cached_{};
 };
 
 // Round-by-round prover (src/protocol/prover.rs:56-313): one ProofState driven

@@ -137,6 +137,10 @@ void Engine::scheduler() {
         // Admission in arrival order while the HBM budget holds the request's footprint.
         while (!queued_.empty()) {
             Request* r = queued_.front();
+            // requests come before cached generator families: drop unreferenced
+            // ones when a request does not fit
+            if (ctx_->reserved() + r->footprint > ctx_->budget() && ctx_->prover_cache())
+                ctx_->prover_cache()->trim(r->footprint);
             const uint64_t reserved = ctx_->reserved();
             if (reserved + r->footprint > ctx_->budget()) {
                 const bool idle = ready_.empty() && host_q_.empty() && inflight_waves_ == 0 && reserved == 0;

@@ -253,6 +253,21 @@ int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint
  * (other streams, or other threads) race on it and must be serialised. */
 int damascus_file_id_noalloc(const void* d_file, size_t len, void* d_out32, void* stream);
 
+/* ------------------------------------------------------------------ generator cache */
+/* Provers' initial generator families g_0(seed, S) and their forward transforms
+ * kept in HBM (no reference counterpart: the reference expands them for every
+ * proof, src/commitment/sis.rs:198-245).  A (seed, ring size) pair is cached the
+ * second time a prover of this context sees it, up to cap_bytes (charged to the
+ * context budget; requests come first and evict unreferenced entries).  The
+ * reference's SystemParams::default uses one seed for every file
+ * (src/utils/config.rs:19, 33-44), so a deployment expands and transforms each
+ * shape once; per-file seeds only pay a lookup.  Off by default; 0 turns it off
+ * (DAMASCUS_ESTATE while a running prover holds an entry).  Proof bytes never
+ * depend on it. */
+int damascus_ctx_set_generator_cache(damascus_ctx* ctx, uint64_t cap_bytes);
+int damascus_ctx_generator_cache_stats(damascus_ctx* ctx, uint64_t* hits, uint64_t* fills, uint64_t* misses,
+                                       uint64_t* bytes);
+
 /* ------------------------------------------------------------------ measurement */
 /* Per-kernel CUDA-event timing on the launching stream (off by default). */
 int damascus_ctx_set_profiling(damascus_ctx* ctx, int on);

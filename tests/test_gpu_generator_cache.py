@@ -1,0 +1,146 @@
+"""Provers' generator cache: proofs are byte-identical with the cache on and off,
+through the plain path and the engine, when an entry is filled, hit, shared by
+the requests of the plan that fills it, evicted, or dropped for budget; per-file
+seeds never fill; turning it off returns its memory."""
+import pytest
+
+import damascus000_gb300 as D
+from damascus000_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+EPOCH = bytes([11]) * 32
+SYSTEM_SEED = bytes([7]) * 32
+
+
+def _files(tag, sizes):
+    return [synth.random_file(777 + tag, n, i)[0] for i, n in enumerate(sizes)]
+
+
+@pytest.fixture(scope="module")
+def reference_proofs(ctx):
+    """Proofs from the session context, which has no generator cache."""
+    cache = {}
+
+    def get(data, seed=SYSTEM_SEED):
+        key = (data, seed)
+        if key not in cache:
+            cache[key] = ctx.prove(data, seed, EPOCH)
+        return cache[key]
+    return get
+
+
+def test_plain_path_fill_hit_identical(reference_proofs):
+    c = D.Context(0, tuning=None)
+    try:
+        c.set_generator_cache(4 << 30)
+        files = _files(1, [1, 8192, 53_248, 60_000, 200_000, 250_000, 900_000, 1_000_000])
+        for rep in range(3):  # first sighting, fill, hits
+            for d in files:
+                assert c.prove(d, SYSTEM_SEED, EPOCH) == reference_proofs(d), (rep, len(d))
+        st = c.generator_cache_stats()
+        # shapes d = 6, 7, 8 (60 KB) ... : every shape fills once and hits afterwards
+        assert st["fills"] >= 4 and st["hits"] >= st["fills"]
+        assert st["bytes"] > 0
+        assert all(c.verify(c.prove(d, SYSTEM_SEED, EPOCH), EPOCH) for d in files[:3])
+        c.set_generator_cache(0)
+        assert c.reserved == 0
+    finally:
+        c.close()
+
+
+def test_per_file_seeds_never_fill(reference_proofs):
+    c = D.Context(0, tuning=None)
+    try:
+        c.set_generator_cache(4 << 30)
+        items = [synth.random_file(55, n, i) for i, n in enumerate([8192, 60_000, 200_000] * 2)]
+        for d, s in items:
+            assert c.prove(d, s, EPOCH) == reference_proofs(d, s)
+        st = c.generator_cache_stats()
+        assert st["fills"] == 0 and st["hits"] == 0 and st["bytes"] == 0
+    finally:
+        c.close()
+
+
+def test_engine_shares_fill_within_and_across_waves(reference_proofs):
+    c = D.Context(0, tuning=None)
+    try:
+        c.set_generator_cache(8 << 30)
+        files = _files(2, [60_000, 70_000, 80_000, 200_000, 210_000, 900_000, 950_000, 1 << 20] * 3)
+        with D.Engine(c) as eng:
+            first = eng.prove_batch([(d, SYSTEM_SEED, EPOCH) for d in files])
+            st1 = c.generator_cache_stats()
+            second = eng.prove_batch([(d, SYSTEM_SEED, EPOCH) for d in files])
+            st2 = c.generator_cache_stats()
+        for d, p, q in zip(files, first, second):
+            assert p == q == reference_proofs(d)
+        assert st1["fills"] >= 1
+        # the second batch finds every shape cached
+        assert st2["hits"] - st1["hits"] == len(files)
+        assert st2["fills"] == st1["fills"]
+    finally:
+        c.close()
+
+
+def test_small_cap_evicts_and_proofs_identical(reference_proofs):
+    c = D.Context(0, tuning=None)
+    try:
+        # room for one d = 9 family but not for a d = 7 one beside it
+        c.set_generator_cache(_entry_bytes(9) + (1 << 20))
+        a = _files(3, [200_000, 210_000])
+        b = _files(4, [900_000, 950_000])
+        order = [a[0], a[1], b[0], b[1], a[0], b[0], a[1], b[1], a[0]]
+        for d in order:
+            assert c.prove(d, SYSTEM_SEED, EPOCH) == reference_proofs(d)
+        st = c.generator_cache_stats()
+        assert st["fills"] >= 2
+    finally:
+        c.close()
+
+
+def _entry_bytes(d):
+    return (1 << (2 * d)) * 8 * (16 + 9 * 4)
+
+
+def test_tight_budget_drops_cached_families(reference_proofs):
+    """A budget that holds one d = 10 prover: a cached d = 9 family fills beside
+    a d = 9 prover, then gives way to the d = 10 request (plain path and engine);
+    every proof completes and matches."""
+    big9, big10 = D.prover_footprint(1 << 20), D.prover_footprint(4 << 20)
+    assert big9 + _entry_bytes(9) < big10
+    c = D.Context(0, hbm_budget_bytes=big10 + (1 << 20), tuning=None)
+    try:
+        c.set_generator_cache(64 << 30)
+        d9 = _files(5, [900_000, 1 << 20, 950_000])
+        d10 = _files(6, [4 << 20])[0]
+        for d in d9[:2]:  # first sighting, then a fill that stays cached
+            assert c.prove(d, SYSTEM_SEED, EPOCH) == reference_proofs(d)
+        assert c.generator_cache_stats()["bytes"] == _entry_bytes(9)
+        assert c.prove(d10, SYSTEM_SEED, EPOCH) == reference_proofs(d10)  # trims the d = 9 family
+        assert c.generator_cache_stats()["bytes"] == 0
+        for d in d9:  # refill
+            assert c.prove(d, SYSTEM_SEED, EPOCH) == reference_proofs(d)
+        assert c.generator_cache_stats()["bytes"] == _entry_bytes(9)
+        with D.Engine(c) as eng:  # admission trims for the d = 10 request
+            items = [d9[0], d10, d9[1]]
+            proofs = eng.prove_batch([(d, SYSTEM_SEED, EPOCH) for d in items])
+            st = eng.stats()
+        assert proofs == [reference_proofs(d) for d in items]
+        assert st["failed"] == 0 and st["peak_reserved"] <= c.budget
+    finally:
+        c.close()
+
+
+def test_turning_off_while_idle_frees_memory():
+    c = D.Context(0, tuning=None)
+    try:
+        c.set_generator_cache(1 << 30)
+        d = _files(6, [53_248])[0]
+        for _ in range(3):
+            c.prove(d, SYSTEM_SEED, EPOCH)
+        assert c.generator_cache_stats()["bytes"] > 0
+        assert c.reserved > 0
+        c.set_generator_cache(0)
+        assert c.reserved == 0
+        assert c.generator_cache_stats() == {"hits": 0, "fills": 0, "misses": 0, "bytes": 0}
+    finally:
+        c.close()
