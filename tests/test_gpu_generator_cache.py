@@ -144,3 +144,44 @@ def test_turning_off_while_idle_frees_memory():
         assert c.generator_cache_stats() == {"hits": 0, "fills": 0, "misses": 0, "bytes": 0}
     finally:
         c.close()
+
+
+def test_engine_plain_provers_and_verifier_share_one_context(reference_proofs):
+    """Everything at once on one context with the cache on: the engine, two
+    threads of plain provers and the verifier service.  Proofs match the
+    uncached ones, honest proofs verify, tampered ones do not, and the cache's
+    memory comes back when it is turned off.  (The budget is the default: a
+    plain prover does not wait for memory the engine holds, it fails.)"""
+    import threading
+    c = D.Context(0, tuning=None)
+    try:
+        c.set_generator_cache(8 << 30)
+        files = _files(7, [60_000, 200_000, 900_000, 1 << 20, 53_248, 250_000] * 3)
+        out, errors = {}, []
+
+        def plain(k):
+            try:
+                for i, d in enumerate(files[k::3]):
+                    out[("plain", k, i)] = (d, c.prove(d, SYSTEM_SEED, EPOCH))
+            except Exception as e:  # surfaced below
+                errors.append(e)
+
+        threads = [threading.Thread(target=plain, args=(k,)) for k in range(2)]
+        for t in threads:
+            t.start()
+        with D.Engine(c) as eng, D.VerifyService(c, workers=4, cache_bytes=1 << 30) as svc:
+            proofs = eng.prove_batch([(d, SYSTEM_SEED, EPOCH) for d in files])
+            bad = [p[:-1] for p in proofs[:4]] + [bytes(p[:100]) + bytes([p[100] ^ 1]) + p[101:] for p in proofs[4:8]]
+            verdicts = svc.verify_batch(proofs + bad, EPOCH)
+        for t in threads:
+            t.join()
+        assert not errors, errors
+        assert proofs == [reference_proofs(d) for d in files]
+        for d, p in out.values():
+            assert p == reference_proofs(d)
+        assert verdicts == [True] * len(proofs) + [False] * len(bad)
+        assert c.reserved <= c.budget
+        c.set_generator_cache(0)
+        assert c.reserved == 0
+    finally:
+        c.close()
