@@ -62,6 +62,7 @@ EXPORTED_SYMBOLS = (
     "damascus_verify_service_create", "damascus_verify_service_destroy", "damascus_verify_service_submit",
     "damascus_verify_service_poll", "damascus_verify_service_wait", "damascus_verify_service_drain",
     "damascus_verify_service_stats", "damascus_ctx_set_generator_cache", "damascus_ctx_generator_cache_stats",
+    "damascus_commit_witness",
 )
 
 
@@ -170,6 +171,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_tuning_set", i32, vp, i32, u32, i32)
     sig("damascus_tuning_get", i32, vp, i32, u32, P(i32))
     sig("damascus_tuning_measure", i32, vp, i32, u32, i32, u32, i32, P(ctypes.c_double))
+    sig("damascus_commit_witness", i32, vp, cp, u64, u64, cp, vp)
     sig("damascus_ctx_set_generator_cache", i32, vp, u64)
     sig("damascus_ctx_generator_cache_stats", i32, vp, P(u64), P(u64), P(u64), P(u64))
     sig("damascus_verify_service_create", i32, vp, i32, u64, P(vp))
@@ -399,6 +401,15 @@ class Context:
         out = ctypes.create_string_buffer(MODULE_RANK * ring_len * 16)
         self.check(self._lib.damascus_commit_with_generators(self._h, witness, generators, vector_len, ring_len,
                                                              out), "commit_with_generators")
+        return out.raw
+
+    def commit_witness(self, witness: bytes, vector_len: int, ring_len: int,
+                       seed_generators: bytes = DEFAULT_GENERATOR_SEED) -> bytes:
+        """ModuleSisCommitter::new(seed).commit_with_ntt(witness) (src/commitment/sis.rs:115-131):
+        generators derived on the device; an empty witness gives the zero module of ring length 1."""
+        out = ctypes.create_string_buffer(MODULE_RANK * (ring_len if vector_len else 1) * 16)
+        self.check(self._lib.damascus_commit_witness(self._h, witness, vector_len, ring_len, seed_generators, out),
+                   "commit_witness")
         return out.raw
 
     def commit(self, data: bytes, seed_generators: bytes = DEFAULT_GENERATOR_SEED) -> bytes:

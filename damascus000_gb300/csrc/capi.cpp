@@ -237,9 +237,13 @@ int damascus_derive_generators(damascus_ctx* ctx, const uint8_t g_seed[32], uint
     return DAMASCUS_OK;
 }
 
-int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, const uint8_t* generators, uint64_t N,
-                                    uint64_t n, uint8_t* com_out) {
-    if (!ctx || !witness || !generators || !com_out || N == 0 || !pow2(n) || n > (1u << kLogMaxProverRing))
+// The commitment sum_i g_i * m_i (sis.rs:146-167) of a host witness with the
+// generators either copied from the host (and reduced mod q, as any 128-bit words
+// are accepted) or expanded on the device from g_seed.
+static int commit_common(damascus_ctx* ctx, const uint8_t* witness, const uint8_t* generators,
+                         const uint8_t g_seed[32], uint64_t N, uint64_t n, uint8_t* com_out, const char* what) {
+    if (!ctx || !witness || !(generators || g_seed) || !com_out || N == 0 || !pow2(n) ||
+        n > (1u << kLogMaxProverRing))
         return set_err(ctx, DAMASCUS_EINVAL, "bad commitment shape");
     // CRT headroom of the single NTT-domain sum: N * n * q^2 < P / 2 (P > 2^251).
     if (N * n > (1ull << 26)) return set_err(ctx, DAMASCUS_EUNSUPPORTED, "N * n above 2^26 exceeds the CRT range");
@@ -263,17 +267,40 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
                parts, 0, 0, L};
     FinishJobX fj{part.m.as<uint32_t>(), out.m.as<uint4>(), nullptr, nullptr, parts, kFinishPlain, rows, 0};
     cudaError_t e = cudaMemcpyAsync(m.m.as<uint8_t>(), witness, N * n * 16, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(gg.m.as<uint8_t>(), generators, N * kRank * n * 16, cudaMemcpyHostToDevice, s);
     // inputs may be any 128-bit words: reduce them mod q first
     if (e == cudaSuccess) e = launch_canon(m.m.as<uint4>(), N * n, s);
-    if (e == cudaSuccess) e = launch_canon(gg.m.as<uint4>(), N * kRank * n, s);
+    if (generators) {
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(gg.m.as<uint8_t>(), generators, N * kRank * n * 16, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = launch_canon(gg.m.as<uint4>(), N * kRank * n, s);
+    } else if (e == cudaSuccess) {
+        e = launch_gen_generators(g_seed, N, L, gg.m.as<uint4>(), s);  // already below q
+    }
     if (e == cudaSuccess) e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L));
     if (e == cudaSuccess) e = launch_mac_jobs(T, &mj, 1, false, s);
     if (e == cudaSuccess) e = launch_finish_jobs(T, &fj, 1, L, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(com_out, out.m.as<uint8_t>(), kRank * n * 16, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("commit_with_generators: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
     return DAMASCUS_OK;
+}
+
+int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, const uint8_t* generators, uint64_t N,
+                                    uint64_t n, uint8_t* com_out) {
+    if (!generators) return set_err(ctx, DAMASCUS_EINVAL, "null generators");
+    return commit_common(ctx, witness, generators, nullptr, N, n, com_out, "commit_with_generators");
+}
+
+int damascus_commit_witness(damascus_ctx* ctx, const uint8_t* witness, uint64_t N, uint64_t n,
+                            const uint8_t seed_generators[32], uint8_t* com_out) {
+    if (!ctx || !seed_generators || !com_out) return set_err(ctx, DAMASCUS_EINVAL, "null argument");
+    if (N == 0) {  // an empty witness commits to the zero module of ring length one (sis.rs:120-122)
+        std::memset(com_out, 0, kRank * 16);
+        return DAMASCUS_OK;
+    }
+    uint8_t g_seed[32];
+    blake3_keyed_hash(seed_generators, "g0", 2, g_seed);  // ModuleSisCommitter::new, sis.rs:68-70
+    return commit_common(ctx, witness, nullptr, g_seed, N, n, com_out, "commit_witness");
 }
 
 int damascus_commit(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],

@@ -98,6 +98,12 @@ int damascus_derive_generators(damascus_ctx* ctx, const uint8_t g_seed[32], uint
  * R_q^8.  witness [N][n], generators [N][8][n], out [8][n]. */
 int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, const uint8_t* generators,
                                     uint64_t vector_len, uint64_t ring_len, uint8_t* com_out);
+/* ModuleSisCommitter::new(seed) + commit_with_ntt (src/commitment/sis.rs:68-70,
+ * 115-131): the generators of an N x n witness are derived on the device from
+ * keyed_hash(seed_generators, "g0"), with no host round trip.  witness [N][n],
+ * out [8][n]; N = 0 writes the zero module of ring length one (8 x 16 bytes). */
+int damascus_commit_witness(damascus_ctx* ctx, const uint8_t* witness, uint64_t vector_len, uint64_t ring_len,
+                            const uint8_t seed_generators[32], uint8_t* com_out);
 /* ModuleSisCommitter::new + register_with_ntt (src/commitment/sis.rs:68-70, 179-195)
  * via expand_file_to_square_polys (src/utils/io.rs:29-70): writes bincode(Statement). */
 int damascus_commit(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],

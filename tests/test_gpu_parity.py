@@ -113,6 +113,20 @@ def test_commit_with_generators_matches_oracle(ctx, oracle_lib, N, n):
     assert ctx.commit_with_generators(w, g, N, n) == oracle_lib.commit_with_generators(w, g, N, n, threads=8)
 
 
+@pytest.mark.parametrize("N,n", [(1, 1), (8, 8), (64, 64), (3, 256), (2, 2048)])
+def test_commit_witness_matches_oracle(ctx, oracle_lib, N, n):
+    """commit_with_ntt with the committer's own generators (derived on the device)."""
+    rng = random.Random(N * 13 + n)
+    w = D.fe_vec(rng.randrange(Q) for _ in range(N * n))
+    seed = bytes([N % 256]) * 32
+    g = oracle_lib.derive_generators(oracle_lib.derive_subseed(seed, b"g0"), N, n)
+    assert ctx.commit_witness(w, N, n, seed) == oracle_lib.commit_with_generators(w, g, N, n, threads=8)
+
+
+def test_commit_witness_empty_is_zero_module(ctx):
+    assert ctx.commit_witness(b"", 0, 64) == bytes(8 * 16)  # ModuleElement::zero(1), sis.rs:120-122
+
+
 @pytest.mark.parametrize("N,n", [(64, 64), (512, 512), (2048, 2048)])
 def test_commit_worst_case_crt_headroom(ctx, N, n):
     """All coefficients q-1: sum_i (-1)(-1) products = N * (2j + 2 - n) (mod q) per slot j."""
