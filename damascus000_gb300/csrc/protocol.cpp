@@ -243,13 +243,12 @@ fq Transcript::challenge(const char* label, uint64_t round, const Module& c, con
     append_commitment(msg, r);
     const size_t prefix = msg.size();
     msg.resize(prefix + 4);
-    for (uint32_t counter = 0;; ++counter) {
+    return sample_nonzero_challenge([&](uint32_t counter) {
         for (int i = 0; i < 4; ++i) msg[prefix + i] = (uint8_t)(counter >> (8 * i));
         uint8_t out[32];
         blake3_hash_parallel(msg.data(), msg.size(), out);
-        const fq v = fq_from_hash(out);
-        if (!fq_is_zero(v)) return v;
-    }
+        return fq_from_hash(out);
+    });
 }
 
 }  // namespace dm

@@ -10,6 +10,16 @@
 
 namespace dm {
 
+// sample_nonzero_challenge (src/protocol/transcript.rs:66-75): candidates for
+// counters 0, 1, 2, ... (wrapping) until one is nonzero.
+template <class Candidate>
+fq sample_nonzero_challenge(Candidate&& candidate) {
+    for (uint32_t counter = 0;; ++counter) {
+        const fq v = candidate(counter);
+        if (!fq_is_zero(v)) return v;
+    }
+}
+
 // ModuleElement<8> (src/algebra/module.rs:9): 8 coordinates of one ring length.
 struct Module {
     uint32_t n = 0;
