@@ -3,7 +3,8 @@
 //  * Z_q with q = 2^112 - 75 on four 32-bit limbs (little endian, the 16-byte
 //    serde form of src/algebra/field.rs:112-129).  Multiplication is a 4x4 limb
 //    schoolbook product reduced with 2^112 = 75 (mod q), the same pseudo-Mersenne
-//    identity as field.rs:229-258.
+//    identity as field.rs:229-258; host code multiplies reduced values with
+//    64-bit halves instead (same results).
 //  * Arithmetic modulo the nine NTT primes p < 2^28 (p = 1 mod 2^14) that carry
 //    every ring product: Shoup products by constants give [0, 2p), so the
 //    transforms run four stages on values below 16p < 2^32 without reducing
@@ -121,7 +122,7 @@ DM_HD fq fq_reduce8(const uint32_t r[8]) {
     return fq_canon(o);
 }
 
-DM_HD fq fq_mul(const fq& a, const fq& b) {
+DM_HD fq fq_mul_limbs(const fq& a, const fq& b) {
     uint32_t r[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 DM_UNROLL
     for (int i = 0; i < 4; ++i) {
@@ -135,6 +136,46 @@ DM_UNROLL
         r[i + 4] = (uint32_t)c;
     }
     return fq_reduce8(r);
+}
+
+#if !defined(__CUDA_ARCH__) && defined(__SIZEOF_INT128__)
+// Host form for inputs below 2^112 (every reduced value): four 64 x 64-bit
+// products instead of sixteen 32 x 32, the same reduction 2^112 = 75 (mod q) to
+// the canonical value, so the result equals fq_mul_limbs bit for bit.  False
+// for wider inputs (words of an unchecked proof), which take the limb form.
+inline bool fq_mul_wide(const fq& a, const fq& b, fq* out) {
+    if ((a.w[3] | b.w[3]) >> 16) return false;
+    typedef unsigned __int128 u128;
+    const uint64_t a0 = a.w[0] | (uint64_t)a.w[1] << 32, a1 = a.w[2] | (uint64_t)a.w[3] << 32;
+    const uint64_t b0 = b.w[0] | (uint64_t)b.w[1] << 32, b1 = b.w[2] | (uint64_t)b.w[3] << 32;
+    const u128 p00 = (u128)a0 * b0;
+    const u128 mid = (u128)a0 * b1 + (u128)a1 * b0;  // a1, b1 < 2^48: < 2^113
+    const u128 p11 = (u128)a1 * b1;                  // < 2^96
+    const uint64_t r0 = (uint64_t)p00;
+    u128 t = (p00 >> 64) + (uint64_t)mid;
+    const uint64_t r1 = (uint64_t)t;
+    t = (t >> 64) + (mid >> 64) + p11;  // the product's bits from 128 on (< 2^96)
+    const u128 m112 = ((u128)1 << 112) - 1;
+    const u128 lo = ((u128)(r1 & ((1ull << 48) - 1)) << 64) | r0;  // product mod 2^112
+    const u128 hi = (t << 16) | (r1 >> 48);                         // product >> 112, < 2^112
+    u128 r = lo + hi * 75u;                                         // < 2^119
+    r = (r & m112) + (r >> 112) * 75u;                              // < 2^112 + 2^14 < 2q
+    const u128 q = ((u128)1 << 112) - 75u;
+    if (r >= q) r -= q;
+    out->w[0] = (uint32_t)r;
+    out->w[1] = (uint32_t)(r >> 32);
+    out->w[2] = (uint32_t)(r >> 64);
+    out->w[3] = (uint32_t)(r >> 96);
+    return true;
+}
+#endif
+
+DM_HD fq fq_mul(const fq& a, const fq& b) {
+#if !defined(__CUDA_ARCH__) && defined(__SIZEOF_INT128__)
+    fq w;
+    if (fq_mul_wide(a, b, &w)) return w;
+#endif
+    return fq_mul_limbs(a, b);
 }
 
 // a + c * b (mod q): the fold map of src/protocol/prover.rs:332-457.

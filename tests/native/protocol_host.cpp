@@ -4,7 +4,8 @@
 //   serde_uses_fixed_width_encoding           (src/algebra/field.rs:305-311)
 //   hard_spec_constants_are_wired             (src/utils/config.rs:106-114)
 // plus the verifier's one-pass commitment update (module_fold) against two
-// module_add_scaled calls, the form of src/protocol/verifier.rs:64-103.
+// module_add_scaled calls, the form of src/protocol/verifier.rs:64-103, and the
+// host multiply against the device limb form.
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -73,6 +74,22 @@ int main() {
         uint64_t dim = 0;
         CHECK(square_layout_for_byte_len(1, &d, &dim) && d == 6 && dim == 64);  // MIN_RING_DEGREE = 2^6
         CHECK(coeff_count_for_byte_len(13) == 1 && coeff_count_for_byte_len(14) == 2);
+    }
+    // the host multiply (64-bit halves) equals the device limb form on every input:
+    // reduced values, edge values, and words of 2^112 and above (limb fallback)
+    {
+        std::mt19937_64 rng(11);
+        const fq qm1{{kQ0 - 1, kQ1, kQ2, kQ3}}, top{{0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFu}};
+        const fq wide{{0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}}, just{{0u, 0u, 0u, 0x10000u}};
+        const fq edge[] = {fq_zero(), fq_from_u32(1), fq_from_u32(75), qm1, top, wide, just};
+        for (const fq& a : edge)
+            for (const fq& b : edge) CHECK(fq_eq(fq_mul(a, b), fq_mul_limbs(a, b)));
+        for (int i = 0; i < 1000000; ++i) {
+            fq a = random_fq(rng), b = random_fq(rng);
+            if (i % 7 == 0) a.w[3] = (uint32_t)rng();  // unreduced words
+            CHECK(fq_eq(fq_mul(a, b), fq_mul_limbs(a, b)));
+            if (failures > 10) return 1;
+        }
     }
     // module_fold == two module_add_scaled calls, plain and on the even coefficients
     {
