@@ -72,19 +72,22 @@ void VerifyService::worker(int w) {
         // made yet): conservative by at most their footprint.  A job that cannot
         // fit even alone runs alone and fails or succeeds as the one-shot
         // verifier would.
-        const uint64_t want = ctx_->reserved() + admitted_bytes_ + job->footprint;
+        uint64_t want = ctx_->reserved() + admitted_bytes_ + job->footprint;
+        if (want > ctx_->budget() && cache_) {
+            // jobs come before cached families: drop the ones nobody holds
+            cache_->trim(admitted_bytes_ + job->footprint);
+            want = ctx_->reserved() + admitted_bytes_ + job->footprint;
+        }
         if ((want > ctx_->budget() || job->alone) && running_ > 0) {
             work_cv_.wait(lk);
             continue;
         }
         if (want > ctx_->budget() && job->footprint <= ctx_->budget()) {
-            // nothing of ours runs: drop cached families nobody holds, and if
-            // memory held by other users of the context is in the way (their
-            // releases do not signal this service) look again shortly
-            if (!(cache_ && cache_->trim(job->footprint))) {
-                work_cv_.wait_for(lk, std::chrono::milliseconds(2));
-                continue;
-            }
+            // nothing of ours runs and memory held by other users of the context
+            // is in the way: their releases do not signal this service, so look
+            // again shortly
+            work_cv_.wait_for(lk, std::chrono::milliseconds(2));
+            continue;
         }
         queue_.pop_front();
         running_ += 1;
