@@ -186,3 +186,20 @@ def test_service_matches_oracle_verifier(ctx, oracle_lib):
         got = [svc.wait(svc.submit(p, EPOCH))[0] for p in cases]
     assert [g == 0 for g in got] == [oracle_lib.verify(p, EPOCH) == 0 for p in cases]
     assert got[0::2] == [0, 0, 0]
+
+
+def test_service_cached_family_gives_way_to_a_job(ctx):
+    """A budget just above one d = 10 verification: the d = 9 family cached by
+    an earlier proof is evicted when the d = 10 job needs the room; both verify."""
+    fam10 = 1024 * 8 * 1024 * 16
+    private10 = fam10 + fam10 // 2 + 4096
+    c = D.Context(0, hbm_budget_bytes=private10 + (8 << 20))
+    try:
+        p9 = _proofs(ctx, [900_000], seed=SYSTEM_SEED, tag=9)[0]
+        p10 = _proofs(ctx, [4 << 20], seed=SYSTEM_SEED, tag=10)[0]
+        with D.VerifyService(c, workers=2, cache_bytes=8 << 30) as svc:
+            assert svc.verify_batch([p9], EPOCH) == [True]
+            assert svc.verify_batch([p10, p9], EPOCH) == [True, True]
+        assert c.reserved == 0
+    finally:
+        c.close()
