@@ -349,6 +349,14 @@ int GenCache::acquire(const uint8_t seed[32], uint64_t N, uint32_t log_n, cudaSt
         return kOk;
     }
     st_.misses += 1;
+    // a key is cached on its second sighting: proofs under per-file (or hostile)
+    // seeds take the stream-ordered private path instead of a synchronous
+    // allocation and an eviction each
+    int& seen = seen_[key];
+    if (seen++ == 0) {
+        if (seen_.size() > 4096) seen_.clear();
+        return kENoMem;
+    }
     if (bytes > cap_ || !evict_for(bytes)) return kENoMem;
     Entry* e = new Entry;
     e->bytes = bytes;

@@ -154,8 +154,9 @@ class DevMem {
 // verifiers.  g_0 depends on nothing but the system seed and the witness shape
 // (src/commitment/sis.rs:198-245), and deployments use one seed for every file
 // (SystemParams::default, src/utils/config.rs:19, 33-44), so a verifier of a stream
-// of proofs expands each shape once.  Entries are charged to the context budget,
-// evicted least recently used when unreferenced, and capped at `cap_bytes`.
+// of proofs expands each shape once.  A key is cached the second time it is seen.
+// Entries are charged to the context budget, evicted least recently used when
+// unreferenced, and capped at `cap_bytes`.
 class GenCache {
    public:
     struct Ref {
@@ -165,8 +166,9 @@ class GenCache {
     };
     GenCache(Context* ctx, uint64_t cap_bytes) : ctx_(ctx), cap_(cap_bytes) {}
     ~GenCache();
-    // The family for (seed, N, 2^log_n); on a miss it is expanded on `s`.  kENoMem
-    // when it does not fit under the cap or the budget (the caller expands its own).
+    // The family for (seed, N, 2^log_n); on a miss of a key seen before it is
+    // expanded on `s`.  kENoMem on a first sighting, or when it does not fit under
+    // the cap or the budget: the caller expands its own.
     int acquire(const uint8_t seed[32], uint64_t N, uint32_t log_n, cudaStream_t s, Ref* out);
     // After every reader of `r` has finished on the device.
     void release(const Ref& r);
@@ -186,6 +188,7 @@ class GenCache {
     uint64_t cap_;
     std::mutex mu_;
     std::map<std::vector<uint8_t>, Entry*> map_;
+    std::map<std::vector<uint8_t>, int> seen_;
     uint64_t clock_ = 0;
     Stats st_;
 };

@@ -75,16 +75,26 @@ def test_service_wrong_epoch_rejects(ctx):
 
 
 def test_service_cache_shares_generators(ctx):
-    """Same shape and system seed: one expansion, the rest are cache hits."""
+    """Same shape and system seed: a private expansion at the first sighting, one
+    cached expansion at the second, hits afterwards."""
     proofs = _proofs(ctx, [200_000] * 6, seed=SYSTEM_SEED, tag=2)
-    with D.VerifyService(ctx, workers=4, cache_bytes=1 << 30) as svc:
+    with D.VerifyService(ctx, workers=1, cache_bytes=1 << 30) as svc:
         assert svc.verify_batch(proofs, EPOCH) == [True] * 6
         st = svc.stats()
         # a second pass over the same shapes expands nothing
         assert svc.verify_batch(proofs, EPOCH) == [True] * 6
         st2 = svc.stats()
-    assert st["cache_misses"] == 1 and st["cache_hits"] == 5
-    assert st2["cache_misses"] == 1 and st2["cache_hits"] == 11
+    assert st["cache_misses"] == 2 and st["cache_hits"] == 4
+    assert st2["cache_misses"] == 2 and st2["cache_hits"] == 10
+
+
+def test_service_per_file_seeds_never_cache(ctx):
+    """Every proof under its own seed: no family is kept, verdicts are unchanged."""
+    proofs = _proofs(ctx, [8192, 60_000, 200_000] * 2, tag=11)
+    with D.VerifyService(ctx, workers=3, cache_bytes=1 << 30) as svc:
+        assert svc.verify_batch(proofs, EPOCH) == [True] * 6
+        st = svc.stats()
+    assert st["cache_hits"] == 0 and st["cache_misses"] == 6
 
 
 def test_service_cache_evicts_least_recently_used(ctx):
@@ -198,7 +208,9 @@ def test_service_cached_family_gives_way_to_a_job(ctx):
         p9 = _proofs(ctx, [900_000], seed=SYSTEM_SEED, tag=9)[0]
         p10 = _proofs(ctx, [4 << 20], seed=SYSTEM_SEED, tag=10)[0]
         with D.VerifyService(c, workers=2, cache_bytes=8 << 30) as svc:
-            assert svc.verify_batch([p9], EPOCH) == [True]
+            assert svc.verify_batch([p9], EPOCH) == [True]  # first sighting: private copy
+            assert svc.verify_batch([p9], EPOCH) == [True]  # second: the family stays cached
+            assert svc.stats()["cache_misses"] == 2
             assert svc.verify_batch([p10, p9], EPOCH) == [True, True]
         assert c.reserved == 0
     finally:
