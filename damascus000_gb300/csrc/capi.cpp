@@ -504,7 +504,7 @@ int damascus_ctx_flush_l2(damascus_ctx* ctx) {
 int damascus_ctx_set_generator_cache(damascus_ctx* ctx, uint64_t cap_bytes) {
     if (!ctx) return DAMASCUS_EINVAL;
     if (ctx->ctx->set_prover_cache(cap_bytes) != kOk)
-        return set_err(ctx, DAMASCUS_ESTATE, "a running prover holds a cached generator family");
+        return set_err(ctx, DAMASCUS_ESTATE, "a running prover or verifier holds a cached generator family");
     return DAMASCUS_OK;
 }
 

@@ -549,6 +549,20 @@ void ProverGenCache::release(const Ref& r) {
     }
 }
 
+bool ProverGenCache::lookup(const uint8_t g0_seed[32], uint32_t L, Ref* out) {
+    std::vector<uint8_t> key(g0_seed, g0_seed + 32);
+    key.push_back((uint8_t)L);
+    std::lock_guard<std::mutex> g(mu_);
+    auto it = map_.find(key);
+    if (it == map_.end() || !it->second->published || it->second->poisoned) return false;
+    Entry* e = it->second;
+    e->refs += 1;
+    e->last_use = ++clock_;
+    st_.hits += 1;
+    *out = Ref{static_cast<uint4*>(e->g), static_cast<uint32_t*>(e->ghat), e->ready, e, false};
+    return true;
+}
+
 void ProverGenCache::publish(const Ref& r) {
     if (!r.entry) return;
     std::lock_guard<std::mutex> g(mu_);
@@ -597,6 +611,7 @@ GpuVerifier::~GpuVerifier() {
         g_[0].reset();
         g_[1].reset();
         if (cache_ && cache_ref_.entry) cache_->release(cache_ref_);
+        if (prover_ref_.entry) ctx_->prover_cache()->release(prover_ref_);
         if (own_stream_) {
             cudaStreamSynchronize(s_);
             cudaStreamDestroy(s_);
@@ -611,6 +626,7 @@ int GpuVerifier::fail(int code, const std::string& msg) {
 }
 
 const uint4* GpuVerifier::source() const {
+    if (round_ == 0 && prover_ref_.g) return prover_ref_.g;
     return (round_ == 0 && cache_ref_.g) ? cache_ref_.g : g_[cur_].as<uint4>();
 }
 
@@ -635,6 +651,17 @@ int GpuVerifier::init(const uint8_t* statement, size_t len, const uint8_t epoch[
     uint32_t Ln = 0;
     while ((1u << Ln) < n) ++Ln;
     cur_ = 0;
+    // the provers' entry for this seed and ring holds g_0 in the verifier's layout
+    // ([N][8][n]) when the family is square, as every proof's is
+    if (N == n && ctx_->prover_cache() && ctx_->prover_cache()->lookup(st_.g_0_seed, Ln, &prover_ref_)) {
+        DM_CU(cudaStreamWaitEvent(s_, prover_ref_.ready, 0), "cudaStreamWaitEvent");
+        if (g_[1].alloc(ctx_, bytes / 2 + 16, s_) == kOk && g_[0].alloc(ctx_, bytes / 4 + 16, s_) == kOk) return kOk;
+        g_[0].reset();
+        g_[1].reset();
+        cudaStreamSynchronize(s_);
+        ctx_->prover_cache()->release(prover_ref_);
+        prover_ref_ = ProverGenCache::Ref{};
+    }
     if (cache_ && cache_->acquire(st_.g_0_seed, N, Ln, s_, &cache_ref_) == kOk) {
         // the first fold writes at most half of g_0, every later one at most a quarter
         // (both dimensions of a non-trivial family halve while above one)

@@ -223,6 +223,10 @@ class ProverGenCache {
     int acquire(const uint8_t g0_seed[32], uint32_t L, const void* plan, Ref* out);
     // After the holder's last reading stage has finished on the device.
     void release(const Ref& r);
+    // A published entry for (seed, 2^L), or false; nothing is filled or counted
+    // as a sighting.  Verifiers of the context read g_0 from it (its coefficient
+    // half is their initial family) after waiting on `ready`.
+    bool lookup(const uint8_t g0_seed[32], uint32_t L, Ref* out);
     // A fill whose stage is enqueued with `ready` recorded after it: from now on
     // the entry is handed out.  Until then other provers use their own buffers.
     void publish(const Ref& r);
@@ -250,9 +254,10 @@ class ProverGenCache {
 
 // Round-by-round verifier (src/protocol/verifier.rs:11-134): commitments and
 // challenges on the host, generator folds enqueued on the device without syncs.
-// With a stream the verifier borrows it (else it owns one); with a cache the
-// first fold reads the shared g_0 and the verifier holds half and a quarter of
-// it instead of one and a half.
+// With a stream the verifier borrows it (else it owns one).  When the context's
+// provers' cache holds g_0 (same seed, square shape), or the verifier's own cache
+// does, the first fold reads that shared copy and the verifier holds half and a
+// quarter of it instead of one and a half.
 class GpuVerifier {
    public:
     explicit GpuVerifier(Context* ctx, cudaStream_t stream = nullptr, GenCache* cache = nullptr)
@@ -264,7 +269,7 @@ class GpuVerifier {
     uint64_t round() const { return round_; }
     uint32_t vector_len() const { return N_; }
     uint32_t ring_len() const { return current_.n; }
-    bool cache_hit() const { return cache_ref_.g != nullptr; }
+    bool cache_hit() const { return cache_ref_.g != nullptr || prover_ref_.g != nullptr; }
     const std::string& error() const { return err_; }
     static uint64_t footprint(uint64_t N, uint64_t n);
 
@@ -276,6 +281,7 @@ class GpuVerifier {
     bool own_stream_ = true;
     GenCache* cache_ = nullptr;
     GenCache::Ref cache_ref_{};
+    ProverGenCache::Ref prover_ref_{};  // g_0 from the context's provers' cache
     std::string err_;
     Statement st_{};
     Transcript tr_;

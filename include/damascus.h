@@ -267,9 +267,11 @@ int damascus_file_id_noalloc(const void* d_file, size_t len, void* d_out32, void
  * context budget; requests come first and evict unreferenced entries).  The
  * reference's SystemParams::default uses one seed for every file
  * (src/utils/config.rs:19, 33-44), so a deployment expands and transforms each
- * shape once; per-file seeds only pay a lookup.  Off by default; 0 turns it off
- * (DAMASCUS_ESTATE while a running prover holds an entry).  Proof bytes never
- * depend on it. */
+ * shape once; per-file seeds only pay a lookup.  Verifiers of the context
+ * (damascus_verify, the verifier service) read a cached family's coefficients as
+ * their initial generators instead of expanding them.  Off by default; 0 turns
+ * it off (DAMASCUS_ESTATE while a running prover or verifier holds an entry).
+ * Proof bytes and verdicts never depend on it. */
 int damascus_ctx_set_generator_cache(damascus_ctx* ctx, uint64_t cap_bytes);
 int damascus_ctx_generator_cache_stats(damascus_ctx* ctx, uint64_t* hits, uint64_t* fills, uint64_t* misses,
                                        uint64_t* bytes);

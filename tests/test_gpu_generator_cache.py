@@ -185,3 +185,27 @@ def test_engine_plain_provers_and_verifier_share_one_context(reference_proofs):
         assert c.reserved == 0
     finally:
         c.close()
+
+
+def test_verifiers_read_generators_from_prover_cache():
+    """A context that proves and verifies under one seed: the verifiers (one-shot
+    and service) take g_0 from the provers' cache; verdicts are unchanged."""
+    c = D.Context(0, tuning=None)
+    try:
+        c.set_generator_cache(4 << 30)
+        files = _files(8, [200_000, 205_000, 210_000])  # all d = 7 (at most 128^2 coefficients)
+        proofs = [c.prove(d, SYSTEM_SEED, EPOCH) for d in files]  # first sighting, fill, hit
+        bad = bytearray(proofs[0])
+        bad[len(bad) // 2] ^= 2
+        bad = bytes(bad)
+        hits0 = c.generator_cache_stats()["hits"]
+        assert all(c.verify(p, EPOCH) for p in proofs)
+        assert not c.verify(bad, EPOCH)
+        assert c.generator_cache_stats()["hits"] == hits0 + 4
+        with D.VerifyService(c, workers=2, cache_bytes=0) as svc:
+            assert svc.verify_batch(proofs + [bad], EPOCH) == [True, True, True, False]
+        assert c.generator_cache_stats()["hits"] == hits0 + 8
+        c.set_generator_cache(0)
+        assert c.reserved == 0
+    finally:
+        c.close()
