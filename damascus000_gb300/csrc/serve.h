@@ -56,7 +56,12 @@ class Engine {
    private:
     struct Request;
     struct Wave;
-    int take_wave_stream();  // index of an idle wave stream (called with mu_ held)
+    // index of an idle wave stream, a high-priority one first when `high`
+    // (called with mu_ held)
+    int take_wave_stream(bool high = false);
+    // Launches the next stage of `reqs` as one wave (called with mu_ held; drops
+    // it while planning and launching).
+    void launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock<std::mutex>& lk);
     static void CUDART_CB on_wave_done(void* arg);
     void scheduler();
     void worker();
@@ -67,6 +72,13 @@ class Engine {
     cudaStream_t stream_ = nullptr;            // admission: allocations, file copies, frees
     std::vector<cudaStream_t> wave_streams_;  // one per in-flight wave, so waves overlap on the GPU
     std::vector<bool> wave_stream_busy_;
+    // The first high_streams_ wave streams run at the device's greatest stream
+    // priority; stages of requests of depth >= priority_depth_ (the longest
+    // chains of stages, 2d + 1 each) launch there in their own wave, so the end of
+    // a stream of requests is not left to the deepest ones alone.  Default 11,
+    // DM_ENGINE_PRIORITY_DEPTH overrides it; 0: one wave of everything.
+    int high_streams_ = 0;
+    uint32_t priority_depth_ = 0;
     cudaEvent_t admit_ev_ = nullptr;
     std::mutex mu_;
     std::condition_variable sched_cv_, done_cv_, work_cv_;
