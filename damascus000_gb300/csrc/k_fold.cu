@@ -26,11 +26,36 @@ unsigned grid_for(uint64_t n, unsigned bx = 256) {
 
 
 
+// acc += a * b over eight limbs (a, b below 2^112; the caller keeps the sum below 2^256).
+__device__ __forceinline__ void acc_mul(uint32_t acc[8], const fq& a, const fq& b) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        uint64_t c = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            c += (uint64_t)a.w[i] * b.w[j] + acc[i + j];
+            acc[i + j] = (uint32_t)c;
+            c >>= 32;
+        }
+#pragma unroll
+        for (int k = i + 4; k < 8; ++k) {
+            c += acc[k];
+            acc[k] = (uint32_t)c;
+            c >>= 32;
+        }
+    }
+}
+
 // Generator folds of one verifier round: vector stage g' = g_L + x^-1 g_R, then the
 // poly stage g'' = g'_e + y^-1 X g'_o.  dst is [N'][8][n'] with N' = N/2 (or N) and
-// n' = n/2 (or n).
+// n' = n/2 (or n).  With both stages an output is s0 + x^-1 s1 + y' s2 + x^-1 y' s3
+// (s0, s1 the even coefficient of both halves, s2, s3 the odd one before it, and
+// y' = -y^-1 for the coefficient that wraps around X^n = -1): the three products
+// of canonical values are summed unreduced (below 2^226) and reduced once, the
+// same canonical value as folding the stages one after the other.
 __global__ void fold_gen_round_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, uint64_t N,
-                                      uint32_t L, fq x_inv, fq y_inv, int vec_stage, int poly_stage) {
+                                      uint32_t L, fq x_inv, fq y_inv, fq xy_inv, fq neg_y_inv, fq neg_xy_inv,
+                                      int vec_stage, int poly_stage) {
     const uint64_t Nout = vec_stage ? N / 2 : N;
     const uint32_t Lout = poly_stage ? L - 1 : L;
     const uint64_t total = Nout * kRank << Lout;
@@ -45,7 +70,17 @@ __global__ void fold_gen_round_kernel(const uint4* __restrict__ src, uint4* __re
             return a;
         };
         fq out;
-        if (poly_stage) {
+        if (poly_stage && vec_stage) {
+            const uint32_t n = 1u << L;
+            const uint32_t o = j == 0 ? n - 1 : 2 * j - 1;
+            const fq s0 = ld(src, base + 2 * j), s1 = ld(src, base + 2 * j + half_elems);
+            const fq s2 = ld(src, base + o), s3 = ld(src, base + o + half_elems);
+            uint32_t acc[8] = {s0.w[0], s0.w[1], s0.w[2], s0.w[3], 0u, 0u, 0u, 0u};
+            acc_mul(acc, x_inv, s1);
+            acc_mul(acc, j == 0 ? neg_y_inv : y_inv, s2);
+            acc_mul(acc, j == 0 ? neg_xy_inv : xy_inv, s3);
+            out = fq_reduce8(acc);
+        } else if (poly_stage) {
             const uint32_t n = 1u << L;
             const fq odd = j == 0 ? fq_neg(gval(n - 1)) : gval(2 * j - 1);
             out = fq_fma(gval(2 * j), y_inv, odd);
@@ -104,8 +139,9 @@ cudaError_t launch_fold_gen_round(const uint4* d_src, uint4* d_dst, uint64_t N, 
                                   bool vec_stage, bool poly_stage, cudaStream_t s) {
     const uint64_t total = (vec_stage ? N / 2 : N) * kRank << (poly_stage ? L - 1 : L);
     if (!total) return cudaSuccess;
-    fold_gen_round_kernel<<<grid_for(total), 256, 0, s>>>(d_src, d_dst, N, L, x_inv, y_inv, vec_stage ? 1 : 0,
-                                                           poly_stage ? 1 : 0);
+    const fq xy_inv = fq_mul(x_inv, y_inv);
+    fold_gen_round_kernel<<<grid_for(total), 256, 0, s>>>(d_src, d_dst, N, L, x_inv, y_inv, xy_inv, fq_neg(y_inv),
+                                                           fq_neg(xy_inv), vec_stage ? 1 : 0, poly_stage ? 1 : 0);
     return cudaGetLastError();
 }
 
