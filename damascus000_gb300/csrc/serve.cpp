@@ -37,8 +37,8 @@ Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_w
     cudaEventCreateWithFlags(&admit_ev_, cudaEventDisableTiming);
     wave_streams_.resize(max_waves_);
     wave_stream_busy_.assign(max_waves_, false);
-    // d = 11 (16 MiB files and up): on the serving stream +1.7 % against no split
-    // (two A/B pairs on one GB300; d >= 10 measured alike and noisier)
+    // d = 11 (16 MiB files and up): on the serving stream +1.9 % against no split
+    // (five interleaved A/B pairs on GB300s; d >= 10 measured alike and noisier)
     priority_depth_ = 11;
     if (const char* v = std::getenv("DM_ENGINE_PRIORITY_DEPTH")) priority_depth_ = (uint32_t)std::atoi(v);
     int least = 0, greatest = 0;
