@@ -159,3 +159,18 @@ def test_engine_empty_and_one_byte_files(ctx, oracle_lib):
         assert p == ctx.prove(d, s, EPOCH)
         assert p == oracle_lib.prove(d, s, EPOCH)
         assert ctx.verify(p, EPOCH)
+
+
+@pytest.mark.parametrize("priority_depth", ["11", "0"])
+def test_engine_priority_split_keeps_proofs(ctx, monkeypatch, priority_depth):
+    """Stages of d = 11 requests run in their own waves on high-priority streams
+    (the default) or with everything else (0): the proofs are the same bytes as
+    the plain path's either way."""
+    monkeypatch.setenv("DM_ENGINE_PRIORITY_DEPTH", priority_depth)
+    files = _files(93, [16 << 20, 60_000, 1 << 20, 300_000, 16 << 20, 8192])
+    with D.Engine(ctx) as eng:
+        proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
+        st = eng.stats()
+    assert st["failed"] == 0
+    for (d, s), p in zip(files, proofs):
+        assert p == ctx.prove(d, s, EPOCH), len(d)
