@@ -40,6 +40,7 @@ _CODE_NAMES = {EINVAL: "EINVAL", ENOMEM_BUDGET: "ENOMEM_BUDGET", ECUDA: "ECUDA",
 EXPORTED_SYMBOLS = (
     "damascus_ctx_create", "damascus_ctx_destroy", "damascus_last_error", "damascus_create_error",
     "damascus_ctx_budget", "damascus_ctx_reserved",
+    "damascus_ctx_set_max_preprocess_bytes", "damascus_ctx_max_preprocess_bytes",
     "damascus_fp_add", "damascus_fp_sub", "damascus_fp_mul", "damascus_fp_inv",
     "damascus_fp_from_le_bytes_mod_order", "damascus_blake3", "damascus_blake3_keyed",
     "damascus_transcript_challenge", "damascus_coeff_count_for_byte_len", "damascus_layout_for_byte_len",
@@ -173,6 +174,8 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_tuning_measure", i32, vp, i32, u32, i32, u32, i32, P(ctypes.c_double))
     sig("damascus_commit_witness", i32, vp, cp, u64, u64, cp, vp)
     sig("damascus_ctx_set_generator_cache", i32, vp, u64)
+    sig("damascus_ctx_set_max_preprocess_bytes", i32, vp, u64)
+    sig("damascus_ctx_max_preprocess_bytes", u64, vp)
     sig("damascus_ctx_generator_cache_stats", i32, vp, P(u64), P(u64), P(u64), P(u64))
     sig("damascus_verify_service_create", i32, vp, i32, u64, P(vp))
     sig("damascus_verify_service_destroy", None, vp)
@@ -337,6 +340,16 @@ class Context:
     @property
     def reserved(self) -> int:
         return self._lib.damascus_ctx_reserved(self._h)
+
+    # -- RuntimeConfig.max_preprocess_bytes of prove / commit / engine submissions
+    @property
+    def max_preprocess_bytes(self) -> int:
+        return self._lib.damascus_ctx_max_preprocess_bytes(self._h)
+
+    def set_max_preprocess_bytes(self, nbytes: int) -> None:
+        """Witness-expansion limit of prove, commit and engine submissions
+        (src/utils/io.rs:42-49); 0 restores the reference default of 512 MiB."""
+        self.check(self._lib.damascus_ctx_set_max_preprocess_bytes(self._h, nbytes), "set_max_preprocess_bytes")
 
     # -- provers' generator cache (damascus_ctx_set_generator_cache)
     def set_generator_cache(self, cap_bytes: int) -> None:

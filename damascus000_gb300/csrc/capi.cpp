@@ -75,7 +75,7 @@ struct CrashTraceInstaller {
 } g_crash_trace_installer;
 
 // Reference default of RuntimeConfig.max_preprocess_bytes (src/utils/config.rs:21, 69-87).
-constexpr uint64_t kDefaultMaxPreprocess = 512ull * 1024 * 1024;
+constexpr uint64_t kDefaultMaxPreprocess = Context::kDefaultMaxPreprocess;
 
 int set_err(damascus_ctx* c, int code, const std::string& msg) {
     if (c) c->ctx->set_error(msg);
@@ -308,7 +308,7 @@ int damascus_commit(damascus_ctx* ctx, const uint8_t* file, size_t len, const ui
     if (!ctx || (!file && len) || !seed_generators) return DAMASCUS_EINVAL;
     static const uint8_t kZeroEpoch[32] = {0};
     GpuProver p(ctx->ctx);
-    int rc = p.init(file, len, false, seed_generators, kZeroEpoch, std::numeric_limits<uint64_t>::max());
+    int rc = p.init(file, len, false, seed_generators, kZeroEpoch, ctx->ctx->max_preprocess());
     if (rc != kOk) return rc;
     std::vector<uint8_t> buf;
     encode_statement(buf, p.statement());
@@ -501,6 +501,14 @@ int damascus_ctx_flush_l2(damascus_ctx* ctx) {
 }
 
 // ------------------------------------------------------------------ generator cache
+int damascus_ctx_set_max_preprocess_bytes(damascus_ctx* ctx, uint64_t max_preprocess_bytes) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    ctx->ctx->set_max_preprocess(max_preprocess_bytes);
+    return DAMASCUS_OK;
+}
+
+uint64_t damascus_ctx_max_preprocess_bytes(damascus_ctx* ctx) { return ctx ? ctx->ctx->max_preprocess() : 0; }
+
 int damascus_ctx_set_generator_cache(damascus_ctx* ctx, uint64_t cap_bytes) {
     if (!ctx) return DAMASCUS_EINVAL;
     if (ctx->ctx->set_prover_cache(cap_bytes) != kOk)
@@ -644,7 +652,10 @@ int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const u
 // ------------------------------------------------------------------ engine
 int damascus_engine_create(damascus_ctx* ctx, int host_threads, int max_waves, damascus_engine** out) {
     if (!ctx || !out) return DAMASCUS_EINVAL;
-    *out = new damascus_engine{ctx, new Engine(ctx->ctx, host_threads, max_waves > 0 ? max_waves : 3), {}, {}, {}};
+    *out = nullptr;
+    std::unique_ptr<Engine> eng(new Engine(ctx->ctx, host_threads, max_waves));
+    if (!eng->init_error().empty()) return set_err(ctx, DAMASCUS_ECUDA, eng->init_error());
+    *out = new damascus_engine{ctx, eng.release(), {}, {}, {}};
     return DAMASCUS_OK;
 }
 

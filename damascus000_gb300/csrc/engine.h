@@ -89,8 +89,18 @@ class Context {
     int set_prover_cache(uint64_t cap_bytes);
     ProverGenCache* prover_cache() const { return prover_cache_.get(); }
 
+    // RuntimeConfig.max_preprocess_bytes of the one-shot and engine entry points
+    // (src/utils/config.rs:21, 69-87; checked as src/utils/io.rs:42-49 does).
+    // Default: the reference's 512 MiB.
+    static constexpr uint64_t kDefaultMaxPreprocess = 512ull * 1024 * 1024;
+    uint64_t max_preprocess() const { return max_preprocess_.load(std::memory_order_relaxed); }
+    void set_max_preprocess(uint64_t bytes) {
+        max_preprocess_.store(bytes ? bytes : kDefaultMaxPreprocess, std::memory_order_relaxed);
+    }
+
    private:
     std::unique_ptr<ProverGenCache> prover_cache_;
+    std::atomic<uint64_t> max_preprocess_{kDefaultMaxPreprocess};
     int device_ = 0;
     int sm_count_ = 152;
     std::atomic<int> tune_[kTuneKnobs][kLogMaxProverRing + 1];

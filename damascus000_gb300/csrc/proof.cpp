@@ -622,7 +622,7 @@ double GpuProver::device_ms() const {
 int prove_all(Context* ctx, const uint8_t* file, uint64_t len, bool on_device, const uint8_t seed[32],
               const uint8_t epoch[32], std::vector<uint8_t>* proof, double* device_ms) {
     GpuProver p(ctx);
-    int rc = p.init(file, len, on_device, seed, epoch, ~0ull);
+    int rc = p.init(file, len, on_device, seed, epoch, ctx->max_preprocess());
     if (rc != kOk) return rc;
     for (uint32_t r = 0; r < p.rounds_total(); ++r) {
         rc = p.fold_round(r, nullptr);

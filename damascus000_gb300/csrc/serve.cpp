@@ -32,20 +32,31 @@ struct Engine::Wave {
 };
 
 Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_waves_(max_waves > 0 ? max_waves : 16) {
-    cudaSetDevice(ctx_->device());
-    cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
-    cudaEventCreateWithFlags(&admit_ev_, cudaEventDisableTiming);
-    wave_streams_.resize(max_waves_);
+    auto check = [this](cudaError_t e, const char* what) {
+        if (e != cudaSuccess && init_error_.empty())
+            init_error_ = std::string("engine setup, ") + what + ": " + cudaGetErrorString(e);
+        return e == cudaSuccess;
+    };
+    wave_streams_.assign(max_waves_, nullptr);
     wave_stream_busy_.assign(max_waves_, false);
     // d = 11 (16 MiB files and up): on the serving stream +1.9 % against no split
     // (five interleaved A/B pairs on GB300s; d >= 10 measured alike and noisier)
     priority_depth_ = 11;
     if (const char* v = std::getenv("DM_ENGINE_PRIORITY_DEPTH")) priority_depth_ = (uint32_t)std::atoi(v);
     int least = 0, greatest = 0;
-    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    bool ok = check(cudaSetDevice(ctx_->device()), "cudaSetDevice") &&
+              check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreateWithFlags") &&
+              check(cudaEventCreateWithFlags(&admit_ev_, cudaEventDisableTiming), "cudaEventCreateWithFlags") &&
+              check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "cudaDeviceGetStreamPriorityRange");
     high_streams_ = priority_depth_ && max_waves_ >= 4 ? max_waves_ / 4 : 0;
-    for (int i = 0; i < max_waves_; ++i)
-        cudaStreamCreateWithPriority(&wave_streams_[i], cudaStreamNonBlocking, i < high_streams_ ? greatest : least);
+    for (int i = 0; ok && i < max_waves_; ++i)
+        ok = check(cudaStreamCreateWithPriority(&wave_streams_[i], cudaStreamNonBlocking,
+                                                i < high_streams_ ? greatest : least),
+                   "cudaStreamCreateWithPriority");
+    if (!ok) {
+        cudaGetLastError();  // the failure is reported by init_error(), not by a later launch
+        return;            // no threads: the destructor frees what was created
+    }
     int n = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency() - 1;
     if (n < 1) n = 1;
     sched_thread_ = std::thread([this] { scheduler(); });
@@ -71,6 +82,7 @@ Engine::~Engine() {
     }
     all_.clear();
     for (auto& s : wave_streams_) {
+        if (!s) continue;
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
     }
@@ -152,8 +164,15 @@ void Engine::scheduler() {
             Request* r = queued_.front();
             // requests come before cached generator families: drop unreferenced
             // ones when a request does not fit
-            if (ctx_->reserved() + r->footprint > ctx_->budget() && ctx_->prover_cache())
+            if (ctx_->reserved() + r->footprint > ctx_->budget() && ctx_->prover_cache()) {
+                // The trim's cudaFree waits for the device, and every wave in flight
+                // ends in on_wave_done, which takes mu_: trim without holding it.
+                // Only this thread admits, so the queue head stays r.
+                lk.unlock();
                 ctx_->prover_cache()->trim(r->footprint);
+                lk.lock();
+                if (stop_) return;
+            }
             const uint64_t reserved = ctx_->reserved();
             if (reserved + r->footprint > ctx_->budget()) {
                 const bool idle = ready_.empty() && host_q_.empty() && inflight_waves_ == 0 && reserved == 0;
@@ -166,7 +185,7 @@ void Engine::scheduler() {
             lk.unlock();
             const bool dev = r->device_file != nullptr;
             const int rc = r->ps->setup(dev ? r->device_file : r->pinned_file, r->len, dev, r->seed, r->epoch,
-                                        std::numeric_limits<uint64_t>::max(), stream_);
+                                        ctx_->max_preprocess(), stream_);
             lk.lock();
             if (rc != kOk) {
                 r->err = r->ps->error();

@@ -40,6 +40,9 @@ class Engine {
    public:
     Engine(Context* ctx, int host_threads, int max_waves);
     ~Engine();
+    // Empty when the streams and events were created; otherwise the failed call
+    // (the engine then runs nothing and must be destroyed).
+    const std::string& init_error() const { return init_error_; }
 
     // Copies the file; returns a ticket.  Never blocks on the GPU.  With
     // on_device the file is a device pointer that must stay valid until the
@@ -92,6 +95,7 @@ class Engine {
     std::chrono::steady_clock::time_point idle_since_{}, active_since_{};
     bool admit_blocked_ = false;  // the queue head waits for memory; cleared when a request finishes
     bool stop_ = false;
+    std::string init_error_;
     EngineStats stats_;
     std::thread sched_thread_;
     std::vector<std::thread> workers_;

@@ -56,6 +56,16 @@ const char* damascus_last_error(damascus_ctx* ctx);
 const char* damascus_create_error(void);
 uint64_t damascus_ctx_budget(damascus_ctx* ctx);
 uint64_t damascus_ctx_reserved(damascus_ctx* ctx);
+/* RuntimeConfig.max_preprocess_bytes (src/utils/config.rs:21, 69-87) of the
+ * context's file entry points that take no limit of their own: damascus_prove,
+ * damascus_prove_device(_timed), damascus_commit and engine submissions.  A file
+ * whose witness expansion (2 x 16 bytes per coefficient of the square layout)
+ * exceeds it fails with DAMASCUS_EINVAL and the reference's message
+ * (src/utils/io.rs:42-49), as DamascusProver::initialize_with_config does.
+ * 0 restores the reference default of 512 MiB (depth <= 12); a new context
+ * starts there.  damascus_prover_new keeps its own argument. */
+int damascus_ctx_set_max_preprocess_bytes(damascus_ctx* ctx, uint64_t max_preprocess_bytes);
+uint64_t damascus_ctx_max_preprocess_bytes(damascus_ctx* ctx);
 
 /* ------------------------------------------------------------------ field */
 /* src/algebra/field.rs:137-198, 45-63, 106-109 */
@@ -105,7 +115,8 @@ int damascus_commit_with_generators(damascus_ctx* ctx, const uint8_t* witness, c
 int damascus_commit_witness(damascus_ctx* ctx, const uint8_t* witness, uint64_t vector_len, uint64_t ring_len,
                             const uint8_t seed_generators[32], uint8_t* com_out);
 /* ModuleSisCommitter::new + register_with_ntt (src/commitment/sis.rs:68-70, 179-195)
- * via expand_file_to_square_polys (src/utils/io.rs:29-70): writes bincode(Statement). */
+ * via expand_file_to_square_polys (src/utils/io.rs:29-70): writes bincode(Statement).
+ * The context's max_preprocess_bytes applies, as the expansion's limit. */
 int damascus_commit(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
                     uint8_t* statement_out, size_t cap, size_t* statement_len);
 /* negacyclic_multiply (src/algebra/ntt.rs:112-195), batched: out_i = a_i * b_i in
@@ -139,7 +150,8 @@ int damascus_prover_fold_round(damascus_prover* p, uint64_t round, uint8_t* reco
 int damascus_prover_final_opening(const damascus_prover* p, uint8_t out[16]);
 
 /* One-shot commit + d fold rounds + opening: writes
- * bincode((Statement, Vec<RoundRecord>, Fp)); capacity from damascus_proof_size(). */
+ * bincode((Statement, Vec<RoundRecord>, Fp)); capacity from damascus_proof_size().
+ * The context's max_preprocess_bytes applies (damascus_ctx_set_max_preprocess_bytes). */
 int damascus_prove(damascus_ctx* ctx, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
                    const uint8_t epoch_seed[32], uint8_t* proof_out, size_t cap, size_t* proof_len);
 /* Same with the file already in device memory. */
@@ -178,7 +190,9 @@ int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const u
 typedef struct damascus_engine damascus_engine;
 int damascus_engine_create(damascus_ctx* ctx, int host_threads, int max_waves, damascus_engine** out);
 void damascus_engine_destroy(damascus_engine* e);
-/* Copies the file and returns at once with a ticket. */
+/* Copies the file and returns at once with a ticket.  The context's
+ * max_preprocess_bytes applies at admission: a larger file's request fails with
+ * DAMASCUS_EINVAL (from poll / wait) and leaves the others undisturbed. */
 int damascus_engine_submit(damascus_engine* e, const uint8_t* file, size_t len, const uint8_t seed_generators[32],
                            const uint8_t epoch_seed[32], uint64_t* ticket);
 /* Same with the file already in device memory; d_file must stay valid until the
@@ -243,20 +257,22 @@ int damascus_cuda_ntt_batch(const uint64_t* host_a, const uint64_t* host_b, uint
                             const uint64_t* primes, const uint64_t* stage_roots, const uint64_t* inv_roots,
                             const uint64_t* inv_sizes);
 
-/* BLAKE3 file id (the blake3::hash of src/utils/io.rs:33) of a file that is
- * already in device memory, for callers that cannot allocate device memory --
- * code running while a CUDA graph is being captured, serving loops confined to
- * a pre-reserved budget, hosts whose allocator belongs to another framework.
- * No counterpart in the reference, which hashes on the host.
+/* BLAKE3 hash of len bytes already in device memory -- the same 32 bytes
+ * damascus_file_id returns for them -- for callers that cannot allocate device
+ * memory: serving loops confined to a pre-reserved budget, and hosts whose
+ * device allocator belongs to another framework.  It has no counterpart in the
+ * reference.
  * d_file: len bytes of device memory; d_out32: 32 bytes of device memory; the
  * kernels run asynchronously on `stream` (a cudaStream_t, 0 for the default
  * stream) on the current device.  The call makes no device allocation: its
  * scratch is a 4 MiB static device array that every device loading this library
- * holds until exit, so len is limited to 64 MiB (larger returns DAMASCUS_ESIZE).
+ * holds until exit, so len is limited to 64 MiB (larger returns DAMASCUS_ESIZE):
+ * files of depth <= 11 fit, those of depth 12 and 13 do not.
  * The first call on a device resolves that array's address (cudaGetSymbolAddress)
- * and should come before any stream capture.  All calls share the array and
- * nothing in it needs clearing between calls; calls that overlap on the GPU
- * (other streams, or other threads) race on it and must be serialised. */
+ * and should come before any stream capture; a failed resolution is retried by
+ * the next call.  All calls share the array and nothing in it needs clearing
+ * between calls; calls that overlap on the GPU (other streams, or other threads)
+ * race on it and must be serialised. */
 int damascus_file_id_noalloc(const void* d_file, size_t len, void* d_out32, void* stream);
 
 /* ------------------------------------------------------------------ generator cache */

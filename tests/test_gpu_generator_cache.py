@@ -209,3 +209,35 @@ def test_verifiers_read_generators_from_prover_cache():
         assert c.reserved == 0
     finally:
         c.close()
+
+
+def test_engine_trims_cached_family_while_waves_in_flight(reference_proofs):
+    """An unreferenced cached d = 9 family must give way to a request while a
+    different request's waves run.  The eviction frees device memory, which waits
+    for the device; the engine therefore trims outside its scheduler lock, so the
+    running waves' completion callbacks are not blocked behind it."""
+    f10 = D.prover_footprint(4 << 20)
+    f8 = D.prover_footprint(600_000)
+    assert f8 < _entry_bytes(9)
+    c = D.Context(0, hbm_budget_bytes=f10 + _entry_bytes(9) + (1 << 20), tuning=None)
+    try:
+        c.set_generator_cache(64 << 30)
+        d9 = _files(7, [900_000, 950_000])
+        for d in d9:  # first sighting, then a fill that stays cached and unreferenced
+            assert c.prove(d, SYSTEM_SEED, EPOCH) == reference_proofs(d)
+        assert c.generator_cache_stats()["bytes"] == _entry_bytes(9)
+        a10, s10 = synth.random_file(808, 4 << 20, 0)  # per-file seeds: neither request uses the cache
+        b8, s8 = synth.random_file(808, 600_000, 1)
+        with D.Engine(c) as eng:
+            ta = eng.submit(a10, s10, EPOCH)
+            for _ in range(20000):  # until the d = 10 request's first wave is on the GPU
+                if eng.stats()["waves"] >= 1:
+                    break
+            tb = eng.submit(b8, s8, EPOCH)  # does not fit beside the cached family: trimmed
+            pa, pb = eng.wait(ta)[0], eng.wait(tb)[0]
+            st = eng.stats()
+        assert pa == reference_proofs(a10, s10) and pb == reference_proofs(b8, s8)
+        assert st["failed"] == 0 and st["peak_reserved"] <= c.budget
+        assert c.generator_cache_stats()["bytes"] == 0
+    finally:
+        c.close()

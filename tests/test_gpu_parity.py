@@ -127,9 +127,13 @@ def test_commit_witness_empty_is_zero_module(ctx):
     assert ctx.commit_witness(b"", 0, 64) == bytes(8 * 16)  # ModuleElement::zero(1), sis.rs:120-122
 
 
-@pytest.mark.parametrize("N,n", [(64, 64), (512, 512), (2048, 2048)])
+@pytest.mark.parametrize("N,n", [(64, 64), (512, 512), (2048, 2048), (4096, 4096),
+                                 pytest.param(8192, 8192, marks=pytest.mark.slow)])
 def test_commit_worst_case_crt_headroom(ctx, N, n):
-    """All coefficients q-1: sum_i (-1)(-1) products = N * (2j + 2 - n) (mod q) per slot j."""
+    """All coefficients q-1: sum_i (-1)(-1) products = N * (2j + 2 - n) (mod q) per slot j.
+    The exact sum at slot n-1 is N * n * (q-1)^2: 2^246 at 2048, 2^248 at 4096 and
+    2^250 at 8192 (d = 13, 8 GiB of generators), against P / 2 > 2^250.98 of the
+    nine CRT primes."""
     w = D.fe_vec([Q - 1]) * (N * n)
     g = D.fe_vec([Q - 1]) * (N * 8 * n)
     out = D.unfe_vec(ctx.commit_with_generators(w, g, N, n))
@@ -254,6 +258,41 @@ def test_round_index_mismatch_and_early_opening(ctx):
     assert e.value.code == D.ESTATE
 
 
+def test_default_memory_limit_rejects_depth13_on_every_file_path(ctx):
+    """RuntimeConfig::default's 512 MiB expansion limit (src/utils/config.rs:21,
+    src/utils/io.rs:42-49): a depth-13 file (2 GiB estimate) fails with EINVAL and
+    the reference's message through the one-shot prover, the commitment, the
+    engine and DamascusProver; a depth-12 file (exactly 512 MiB) passes."""
+    assert ctx.max_preprocess_bytes == D.DEFAULT_MEMORY_LIMIT_BYTES
+    d13 = b"\x5a" * (4096 * 4096 * 13 + 1)
+    assert D.layout_for_byte_len(len(d13))[0] == 13
+    calls = [lambda: ctx.prove(d13, SEED7, EPOCH), lambda: ctx.commit(d13, SEED7),
+             lambda: D.DamascusProver(ctx, d13, SEED7, EPOCH)]
+    for call in calls:
+        with pytest.raises(D.DamascusError) as e:
+            call()
+        assert e.value.code == D.EINVAL and "above max_preprocess_bytes=536870912" in str(e.value)
+    with D.Engine(ctx, host_threads=2) as eng:
+        small = synth.random_file(31, 60_000, 0)[0]
+        t_bad, t_ok = eng.submit(d13, SEED7, EPOCH), eng.submit(small, SEED7, EPOCH)
+        with pytest.raises(D.DamascusError) as e:
+            eng.wait(t_bad)
+        assert e.value.code == D.EINVAL and "split the file" in str(e.value)
+        assert eng.wait(t_ok)[0] == ctx.prove(small, SEED7, EPOCH)
+    d12 = b"\x5a" * (2048 * 2048 * 13 + 1)
+    assert D.layout_for_byte_len(len(d12))[0] == 12
+    stmt = ctx.commit(d12, SEED7)
+    assert len(stmt) == D.load().damascus_statement_size(4096)
+    ctx.set_max_preprocess_bytes(256 << 20)
+    try:
+        with pytest.raises(D.DamascusError) as e:
+            ctx.commit(d12, SEED7)
+        assert e.value.code == D.EINVAL
+    finally:
+        ctx.set_max_preprocess_bytes(0)
+    assert ctx.max_preprocess_bytes == D.DEFAULT_MEMORY_LIMIT_BYTES
+
+
 def test_memory_limit_error_path(ctx):
     with pytest.raises(D.DamascusError) as e:
         D.DamascusProver(ctx, write_pattern(1 << 20, 7), SEED7, EPOCH, max_preprocess_bytes=1024)
@@ -309,8 +348,12 @@ def test_d13_prove_verifies_on_gpu(ctx):
     nbytes = 4096 * 4096 * 13 + 1  # just above the depth-12 capacity
     data, seed = synth.random_file(13, nbytes, 0)
     assert D.layout_for_byte_len(nbytes)[0] == 13
-    with D.Engine(ctx, host_threads=4) as eng:
-        proof = eng.prove_batch([(data, seed, EPOCH)])[0]
+    ctx.set_max_preprocess_bytes(4 << 30)  # the expansion needs 2 GiB
+    try:
+        with D.Engine(ctx, host_threads=4) as eng:
+            proof = eng.prove_batch([(data, seed, EPOCH)])[0]
+    finally:
+        ctx.set_max_preprocess_bytes(0)
     assert len(proof) == D.proof_size(nbytes)
     assert ctx.verify(proof, EPOCH)
     bad = bytearray(proof)
