@@ -1,9 +1,11 @@
 """The allocation-free file-id entry point, for callers that cannot allocate
-device memory (graph capture, fixed-budget serving loops, foreign allocators).
+device memory: serving loops confined to a fixed, pre-reserved budget, and hosts
+whose device allocator belongs to another framework.
 
 Checks damascus_file_id_noalloc through the C ABI against the allocating
 damascus_file_id, bit-exact, on two calls in a row per input (the static
-scratch keeps the previous call's contents).  Collected last on purpose."""
+scratch keeps the previous call's contents), that a call leaves the device's
+free memory unchanged, and the size limit.  Collected last on purpose."""
 import ctypes
 
 import pytest
@@ -14,6 +16,11 @@ from damascus000_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 MAX_BYTES = 64 << 20
+
+
+def _call(lib, dev, n, out, stream):
+    return lib.damascus_file_id_noalloc(ctypes.c_void_p(dev.data_ptr()), n, ctypes.c_void_p(out.data_ptr()),
+                                        ctypes.c_void_p(stream.cuda_stream))
 
 
 def test_file_id_noalloc_matches_allocating_entry_point(ctx):
@@ -27,11 +34,27 @@ def test_file_id_noalloc_matches_allocating_entry_point(ctx):
         dev = torch.frombuffer(bytearray(data if n else b"\0"), dtype=torch.uint8).cuda()
         for _ in range(2):
             out.fill_(0xEE)
-            rc = lib.damascus_file_id_noalloc(ctypes.c_void_p(dev.data_ptr()), n, ctypes.c_void_p(out.data_ptr()),
-                                              ctypes.c_void_p(stream.cuda_stream))
-            assert rc == D.OK
+            assert _call(lib, dev, n, out, stream) == D.OK
             stream.synchronize()
             assert bytes(out.cpu().tolist()) == want, n
+
+
+def test_file_id_noalloc_leaves_free_memory_unchanged(ctx):
+    torch = pytest.importorskip("torch")
+    lib = D.load()
+    stream = torch.cuda.current_stream()
+    data, _ = synth.random_file(78, 3 << 20, 0)
+    dev = torch.frombuffer(bytearray(data), dtype=torch.uint8).cuda()
+    out = torch.zeros(32, dtype=torch.uint8, device="cuda")
+    assert _call(lib, dev, len(data), out, stream) == D.OK  # the array exists once the module is loaded
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert _call(lib, dev, len(data), out, stream) == D.OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert bytes(out.cpu().tolist()) == ctx.file_id(data)
 
 
 def test_file_id_noalloc_rejects_oversized_input():
