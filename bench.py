@@ -136,14 +136,11 @@ def workload_files(wl, rank: int = 0):
         return [(synth.random_file(base, wl["file_bytes"], 40_000 + i)[0], SYSTEM_SEED, i / wl["rate"])
                 for i in range(wl["requests"])]
     if wl["kind"] in ("serve", "verify"):
-        reqs = synth.serving_stream(base, wl["requests"], wl["rate"])
-        files = [synth.random_file(base, r.size, 10_000 + r.index) + (r.arrival_s,) for r in reqs]
-        if wl["kind"] == "verify" or wl.get("system_seed"):  # one seed for every file, as SystemParams::default
-            files = [(d, SYSTEM_SEED, a) for d, _, a in files]
-        return files
+        # one seed for every file in the verify and system-seed forms, as SystemParams::default
+        one_seed = SYSTEM_SEED if wl["kind"] == "verify" or wl.get("system_seed") else None
+        return synth.serving_files(base, wl["requests"], wl["rate"], one_seed)
     if wl["kind"] == "batched":
-        sizes = synth.log_uniform_sizes(base, wl["files"], wl["lo"], wl["hi"])
-        return [synth.random_file(base, n, 20_000 + i) + (0.0,) for i, n in enumerate(sizes)]
+        return synth.batched_files(base, wl["files"], wl["lo"], wl["hi"])
     return None
 
 
@@ -271,14 +268,12 @@ def cpu_baseline(wl, budget_s: float = 15.0, threads: int = 0, proofs=None):
         return {"value": submitted / el, "unit": "proofs/s", "cores": threads, "kind": "port",
                 "sample": f"{submitted} verifications by the oracle restatement (generator expansion, transcript replay, "
                           f"module folds) of {what}, {threads} at a time on {threads} threads, in {el:.1f} s"}
-    if wl["kind"] == "plain":
-        items = ((synth.random_file(MASTER_SEED, wl["file_bytes"], 1000 + i)) for i in range(64))
-        what = f"full commit+prove of {wl['file_bytes']}-byte files"
-    else:
-        files = workload_files(wl)
-        small = [(d, s) for d, s, _ in files if len(d) <= (1 << 20)]
-        items = iter(small)
-        what = "full commit+prove of the workload's files <= 1 MiB, in stream order"
+    if wl["kind"] != "plain":
+        r = StratifiedOracle(wl, threads).step(0, max_full_depth=10)
+        return {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port", "sample": r["sample"],
+                "per_depth": r["per_depth"]}
+    items = ((synth.random_file(MASTER_SEED, wl["file_bytes"], 1000 + i)) for i in range(64))
+    what = f"full commit+prove of {wl['file_bytes']}-byte files"
     done = nbytes = 0
     t0 = time.perf_counter()
     for data, seed in items:
@@ -293,20 +288,91 @@ def cpu_baseline(wl, budget_s: float = 15.0, threads: int = 0, proofs=None):
                       f"CRT, commitment columns over {threads} threads); {nbytes} bytes in {el:.1f} s"}
 
 
+class StratifiedOracle:
+    """The oracle's MiB/s on a workload of mixed depths, stratified by depth.
+
+    Every depth present is timed on full commit+prove runs of the workload's own
+    files, and the workload's rate is its bytes over the sum, per depth, of its
+    bytes of that depth at the rate measured there.  Depths up to 9 take seconds
+    and are re-sampled every step on the next file of that depth; deeper ones
+    (d = 10: tens of seconds, d = 11: minutes) are timed once, on the first file
+    of that depth, and reused."""
+
+    def __init__(self, wl, threads):
+        import oracle as O
+        O.build()
+        self.O, self.threads = O, threads
+        self.by_depth = {}
+        for d, s, _ in workload_files(wl):
+            self.by_depth.setdefault(O.layout_for_byte_len(len(d))[0], []).append((d, s))
+        self.once = {}
+
+    def _time(self, data, seed):
+        t0 = time.perf_counter()
+        self.O.prove(data, seed, EPOCH, use_ntt=True, threads=self.threads)
+        return time.perf_counter() - t0
+
+    def step(self, k, max_full_depth=11, resample_depth=9):
+        per, proj_s, total, sampled = {}, 0.0, 0, 0
+        for depth in sorted(self.by_depth):
+            files = self.by_depth[depth]
+            dbytes = sum(len(d) for d, _ in files)
+            total += dbytes
+            if depth > max_full_depth:
+                continue
+            if depth <= resample_depth:
+                data, seed = files[k % len(files)]
+                n, secs = len(data), self._time(data, seed)
+            else:
+                if depth not in self.once:
+                    data, seed = files[0]
+                    self.once[depth] = (len(data), self._time(data, seed))
+                n, secs = self.once[depth]
+            rate = n / MIB / secs
+            per[depth] = {"files_in_workload": len(files), "workload_bytes": dbytes, "sampled_bytes": n,
+                          "seconds": round(secs, 3), "mib_s": rate}
+            proj_s += dbytes / MIB / rate
+            sampled += dbytes
+        value = sampled / MIB / proj_s
+        skipped = [d for d in self.by_depth if d > max_full_depth]
+        sample = (f"oracle restatement (per-product 2n-point NTT over 8 CRT primes + Garner CRT, commitment columns "
+                  f"over {self.threads} threads), one full commit+prove per depth of the workload's own files "
+                  f"(d <= {resample_depth}: the next file of that depth each step; deeper: the first, timed once); "
+                  "value = the workload's bytes / sum over depths of its bytes there at the measured rate; "
+                  "per depth: " + "; ".join(f"d{d}: {v['sampled_bytes']} B in {v['seconds']} s"
+                                            for d, v in per.items()))
+        if skipped:
+            sample += (f"; depths {skipped} ({total - sampled} of {total} bytes) not sampled in this bounded leg, "
+                       "the value covers the rest of the workload")
+        return {"value": value, "per_depth": per, "sample": sample}
+
+
 def run_reference(args, wl):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    vals = []
-    base = None
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline(wl, budget_s=4.0 if i else 10.0)
-        if r["value"] is None:
-            print(json.dumps({"impl": "reference", "unavailable": r["sample"]}))
-            return 0
-        base = base or r
-        if i >= args.warmup:
+    threads = os.cpu_count() or 1
+    vals, base, per_depth = [], None, None
+    if wl["kind"] in ("serve", "batched"):
+        strat = StratifiedOracle(wl, threads)
+        import oracle as O
+        d6 = min(strat.by_depth)
+        for i in range(args.warmup):  # warm-up: one proof of the shallowest depth
+            O.prove(*strat.by_depth[d6][i % len(strat.by_depth[d6])], EPOCH, use_ntt=True, threads=threads)
+        for k in range(args.steps):
+            r = strat.step(k)
             vals.append(r["value"])
+            base, per_depth = base or r, r["per_depth"]
+        base = {"value": base["value"], "cores": threads, "sample": base["sample"]}
+    else:
+        for i in range(args.warmup + args.steps):
+            r = cpu_baseline(wl, budget_s=4.0 if i else 10.0)
+            if r["value"] is None:
+                print(json.dumps({"impl": "reference", "unavailable": r["sample"]}))
+                return 0
+            base = base or r
+            if i >= args.warmup:
+                vals.append(r["value"])
     value = statistics.median(vals) if vals else base["value"]
     # one step of the GPU arm's workload at the sampled rate (the sample itself is bounded)
     if wl["kind"] == "ringmul":
@@ -325,32 +391,58 @@ def run_reference(args, wl):
             "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32/u128 integer", "data": "synthetic",
             "config": {"workload": wl["desc"], "impl_note": "CPU restatement of the reference algorithm; the Rust "
-                       "reference cannot be built here (no cargo/rustc on either machine)"},
+                       "reference cannot be built here (no cargo/rustc on either machine)",
+                       "step_values": vals},
             "cpu_baseline": {"value": value, "unit": unit, "cores": base["cores"], "kind": "port",
                              "sample": base["sample"]},
             "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if per_depth:
+        line["cpu_baseline"]["per_depth_last_step"] = per_depth
     print(json.dumps(line))
     return 0
 
 
 # ------------------------------------------------------------------ GPU
-# DRAM bytes per algorithmic byte of the forward transform: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum over 1200 transform launches of the
-# serving stream (0.94-0.99 for the rings that dominate its time, below 1 for
-# small rings that stay in L2).
-NTT_TRAFFIC_RATIO = 0.950
-# The transform and the generator expansion are integer-bound: the busy fraction
-# of the pipe that limits each, from ncu --set full on a d = 11 proof (FMA-heavy,
-# which runs the integer multiplies, for the transform; the ALU for BLAKE3).
-INT_PIPE = {
-    "ntt_fwd": {"pipe": "FMA-heavy (integer multiply)", "ncu_frac": 0.698,
-                "unit_rate": "butterflies/s"},
-    "gen_generators": {"pipe": "ALU (XOR / rotate)", "ncu_frac": 0.885, "unit_rate": "BLAKE3 compressions/s"},
+# DRAM bytes per algorithmic byte of a kernel, from ncu captures of small cases
+# (dram__bytes_read.sum + dram__bytes_write.sum over the captured launches ÷ the
+# same launches' algorithmic bytes).  Used to state `traffic` per launch of this
+# run; the capture, not this run, measured it.
+DRAM_PER_ALGO_BYTE = {
+    "ntt_fwd": (0.95, "ncu of the transform, per ring size (profiles/ntt_fwd_traffic_by_ring.txt)"),
 }
-INT_PIPE_SOURCE = "profiles/kernels_d11_full.md"
+# The transform is bound by the integer multiplier, not by HBM.  Its multiplies,
+# counted from the kernel's code (dm_ntt.cuh, dm_field.cuh): a butterfly is one
+# Shoup product (one mul.hi, two mul.lo); the input residue of a 112-bit
+# coefficient under one prime is three 32x32->64 multiply-adds and a Shoup
+# product (residue_fwd), and the output's reduction a mul.hi and a mul.lo
+# (shoup_one).  Each form is weighted by its issue cost relative to mul.lo, and
+# the peak is mul.lo's rate: all three rates measured on this device in this run
+# (damascus_measure_int_multiply).
+N_PRIMES = 9
+NTT_MULS = {"butterfly": {"mul.hi": 1, "mul.lo": 2},
+            "residue": {"mad.wide": 3, "mul.hi": 2, "mul.lo": 3}}  # per coefficient and prime
 
 
-def roofline(stats, measured_on="the timed steps"):
+def int_pipe(dom, n, ms, byts, ops, rates):
+    """Integer-multiplier fraction of the transform from counted multiplies."""
+    if dom != "ntt_fwd" or not rates or not all(rates.values()):
+        return None
+    weight = {k: rates["mul.lo"] / v for k, v in rates.items()}  # mul.lo issue slots per instruction
+    per = {u: sum(c * weight[k] for k, c in f.items()) for u, f in NTT_MULS.items()}
+    coeffs = byts / (16 + 4 * N_PRIMES)  # each coefficient: 16 B read, nine 4-byte residues written
+    slots = ops * per["butterfly"] + coeffs * N_PRIMES * per["residue"]
+    rate = slots / (ms / 1000.0)
+    return {"pipe": "integer multiplier (FMA-heavy)", "achieved": rate, "peak": rates["mul.lo"],
+            "unit": "mul.lo-equivalent multiplies/s", "frac": rate / rates["mul.lo"],
+            "counted_per_launch": slots / n, "multiplies": NTT_MULS,
+            "measured_rates_ops_per_s": rates, "issue_weight_vs_mul_lo": weight,
+            "butterflies_per_s": ops / (ms / 1000.0),
+            "note": "peak and weights measured in this run on this GPU (independent chains of each form); counts "
+                    "only the arithmetic's multiplies, while ncu's FMA-heavy busy % also includes the compiler's "
+                    "integer moves and address arithmetic on that pipe"}
+
+
+def roofline(stats, measured_on, rates=None):
     peak, src = read_peaks()
     live = {k: v for k, v in stats.items() if v}
     if not live:
@@ -359,21 +451,87 @@ def roofline(stats, measured_on="the timed steps"):
     n, ms, byts, ops = live[dom]
     achieved = byts / n / (ms / n / 1000.0) / 1e9
     total_ms = sum(v[1] for v in live.values())
-    traffic = byts / n * NTT_TRAFFIC_RATIO if dom == "ntt_fwd" else None
+    ratio = DRAM_PER_ALGO_BYTE.get(dom)
     out = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-           "frac": achieved / peak, "peak_source": src, "traffic": traffic,
-           "traffic_source": "ncu DRAM bytes / algorithmic bytes of this kernel" if traffic else None,
+           "frac": achieved / peak, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured"
+           else src, "traffic": byts / n * ratio[0] if ratio else None,
+           "traffic_source": (f"not measured in this run: algorithmic bytes per launch x {ratio[0]} DRAM bytes "
+                              f"per algorithmic byte from {ratio[1]}") if ratio else None,
            "algo_bytes_per_launch": byts / n, "avg_launch_ms": ms / n, "share_of_kernel_time": ms / total_ms,
            "measured_on": measured_on,
-           "kernels": {k: {"launches": v[0], "ms": round(v[1], 4), "algo_bytes": v[2], "algo_ops": v[3]}
+           "kernels": {k: {"launches": v[0], "ms": round(v[1], 4), "algo_bytes": v[2], "algo_ops": v[3],
+                           "achieved_gbs": v[2] / (v[1] / 1000.0) / 1e9}
                        for k, v in live.items()}}
-    if dom in INT_PIPE:
-        # the kernel's own limit is an integer pipe; the HBM fraction above is the share of
-        # the copy bandwidth it uses, the pipe fraction below how close it runs to its limit
-        out["int_pipe"] = dict(INT_PIPE[dom], achieved_rate=ops / (ms / 1000.0), source=INT_PIPE_SOURCE)
+    ip = int_pipe(dom, n, ms, byts, ops, rates)
+    if ip:
+        out["int_pipe"] = ip
         out["note"] = ("integer-bound kernel: frac is its share of the HBM copy peak; its own limit is the "
-                       "int_pipe fraction (ncu)")
+                       "integer multiplier, int_pipe.frac")
     return out
+
+
+def workload_digests(name, rank):
+    """The oracle's proof digests for this workload's files (rank 0's files only)."""
+    sets = {"serve": "serving", "serve_seed": "serving_system_seed", "batched": "batched", "d9": "d9",
+            "d11": "d11"}
+    p = ROOT / "tests" / "golden" / "workload_digests.json"
+    if rank != 0 or name not in sets or not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    if d.get("master_seed") != MASTER_SEED or sets[name] not in d:
+        return None
+    return d[sets[name]]
+
+
+def check_digests(entries, proofs, lengths, indices=None):
+    """(proofs equal to the oracle's, proofs checked) by SHA-256."""
+    import hashlib
+    by_index = {e["index"]: e for e in entries}
+    ok = checked = 0
+    for k, (p, ln) in enumerate(zip(proofs, lengths)):
+        e = by_index.get(indices[k] if indices else k)
+        if e is None or e["file_len"] != ln:
+            continue
+        checked += 1
+        ok += hashlib.sha256(p).hexdigest() == e["proof_sha256"]
+    return ok, checked
+
+
+def measure_batched(ctx, D, torch, args, rank, world, ranks):
+    """The 64-file batched set (log-uniform 50 KB - 4 MiB, d 6-10): one engine batch
+    per step against the plain one-at-a-time path, every proof checked against the
+    oracle's digests.  Reported beside the serving stream's line."""
+    wl = dict(WORKLOADS["batched"], name="batched")
+    files = workload_files(wl, rank)
+    total = sum(len(d) for d, _, _ in files)
+    dev = [torch.frombuffer(bytearray(d), dtype=torch.uint8).cuda() for d, _, _ in files]
+    torch.cuda.synchronize()
+    with D.Engine(ctx) as eng:
+        def batch():
+            return [eng.wait(t)[0] for t in
+                    [eng.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]]
+        for _ in range(args.warmup):
+            batch()
+        ranks.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            proofs = batch()
+        torch.cuda.synchronize()
+        step_s = ranks.max(time.perf_counter() - t0) / args.steps
+    ranks.barrier()
+    t0 = time.perf_counter()
+    for t, (d, s, _) in zip(dev, files):
+        ctx.prove_device(t.data_ptr(), len(d), s, EPOCH)
+    torch.cuda.synchronize()
+    plain_s = ranks.max(time.perf_counter() - t0)
+    digests = workload_digests("batched", rank)
+    exact = check_digests(digests, proofs, [len(d) for d, _, _ in files]) if digests else None
+    return {"workload": wl["desc"], "value": world * total / MIB / step_s, "unit": UNIT,
+            "ms_per_step": step_s * 1000.0, "total_bytes": total, "steps": args.steps,
+            "plain_mib_s": world * total / MIB / plain_s, "batched_vs_plain": plain_s / step_s,
+            "bit_exact_vs_oracle": f"{exact[0]}/{exact[1]}" if exact else None,
+            "note": "files resident in HBM; wall time of the whole batch (host challenges included)"}
 
 
 def percentile(xs, q):
@@ -399,6 +557,7 @@ def run_gpu(args, wl):
     barrier, max_over_ranks = ranks.barrier, ranks.max
 
     ctx = D.Context(local, hbm_budget_bytes=SERVE_BUDGET if wl["kind"] != "plain" else 0)
+    int_rates = ctx.measure_int_multiply()  # the integer-multiplier peaks of the transform's roofline
     if wl.get("generator_cache"):
         ctx.set_generator_cache(wl["generator_cache"])
     cpu_inputs = None  # the verify workloads time the oracle verifier on their own proofs
@@ -464,7 +623,9 @@ def run_gpu(args, wl):
                      "e2e": {"value": world * args.steps * pairs / e2e_s, "unit": "products/s",
                              "h2d_bytes_per_step": 2 * len(a), "d2h_bytes_per_step": len(a)},
                      "gpu_launches": int(sum(s[0] for s in stats.values() if s)),
-                     "roofline": roofline({k: v for k, v in stats.items() if k != "ring_mul"}), "clocks": clk})
+                     "roofline": roofline({k: v for k, v in stats.items() if k != "ring_mul"},
+                                          "the timed steps (one launch at a time on the context stream, per-kernel "
+                                          "CUDA events)", int_rates), "clocks": clk})
     elif wl["kind"] == "plain":
         file_bytes = wl["file_bytes"]
         nsteps = args.warmup + args.steps
@@ -516,13 +677,24 @@ def run_gpu(args, wl):
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(max(ev0.elapsed_time(ev1) / 1000.0, time.perf_counter() - t0))
         ok = ctx.verify(out.raw[:n_out.value], EPOCH)
+        # the files the oracle's digests cover, proven again through the same path
+        digests = workload_digests(wl["name"], rank)
+        exact = None
+        if digests:
+            idx = [e["index"] for e in digests if e["index"] < nsteps]
+            exact = check_digests(digests, [ctx.prove(files[i][0], files[i][1], EPOCH) for i in idx],
+                                  [file_bytes] * len(idx), idx)
         line.update({"value": value, "ms_per_step": total_ms / args.steps,
                      "config": {"workload": wl["desc"], "file_bytes": file_bytes, "parallelism": f"replicas x{world}",
-                                "l2": "flushed (256 MiB write) between timed steps", "verified": bool(ok)},
+                                "l2": "flushed (256 MiB write) between timed steps", "verified": bool(ok),
+                                "bit_exact_vs_oracle": f"{exact[0]}/{exact[1]} proofs of this workload's files equal "
+                                                       "the CPU oracle's (SHA-256)" if exact else None},
                      "e2e": {"value": world * args.steps * file_bytes / MIB / e2e_s, "unit": UNIT,
                              "h2d_bytes_per_step": file_bytes, "d2h_bytes_per_step": n_out.value},
                      "gpu_launches": int(sum(s[0] for s in stats.values() if s)),
-                     "roofline": roofline(stats, "the same K steps rerun with per-kernel CUDA events"),
+                     "roofline": roofline(stats, "the same K steps rerun with per-kernel CUDA events (one proof at a "
+                                                 "time: launches serialised on the prover's stream)",
+                                          int_rates),
                      "clocks": clk})
     elif wl["kind"] == "verify":
         files = workload_files(wl, rank)
@@ -667,15 +839,22 @@ def run_gpu(args, wl):
         st1 = eng.stats()
         step_s = max_over_ranks(max(ev0.elapsed_time(ev1) / 1000.0, wall)) / args.steps
         value = world * total / MIB / step_s
+        # every proof of the last timed replay against the oracle's digests
+        digests = workload_digests(wl["name"], rank)
+        exact = check_digests(digests, [r[0] for r in res], [len(d) for d, _, _ in files]) if digests else None
 
-        # kernel breakdown: the same K replays again with per-kernel CUDA events
+        # kernel rates: one more replay with a single wave in flight, so the launches
+        # run one after another on one stream and each kernel's CUDA events time it
+        # alone (the timed replays overlap up to 16 waves)
         ctx.set_profiling(True)
         ctx.reset_stats()
-        for _ in range(args.steps):
-            replay_device()
+        with D.Engine(ctx, max_waves=1) as eng1:
+            serial = [eng1.wait(t)[0] for t in
+                      [eng1.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]]
         torch.cuda.synchronize()
         stats = {k: ctx.kernel_stat(k) for k in KERNELS}
         ctx.set_profiling(False)
+        serial_same = sum(a == b[0] for a, b in zip(serial, res))
 
         # end to end from pinned host memory
         lib = D.load()
@@ -690,6 +869,7 @@ def run_gpu(args, wl):
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(time.perf_counter() - t0) / args.steps
         verified = all(ctx.verify(o[0], EPOCH) for o in outs[:: max(1, len(outs) // 4)])
+        e2e_exact = check_digests(digests, [o[0] for o in outs], [len(d) for d, _, _ in files]) if digests else None
 
         # plain one-request-at-a-time GPU path on the same files
         barrier()
@@ -717,11 +897,20 @@ def run_gpu(args, wl):
                    "rate_per_s": wl["rate"], "requests": len(lats),
                    "offered_mib_s": total / MIB / files[-1][2]}
         eng.close()
+        if wl["name"] == "serve" and not args.no_batched:
+            line["batched"] = measure_batched(ctx, D, torch, args, rank, world, ranks)
         line.update({"value": value, "ms_per_step": step_s * 1000.0,
                      "config": {"workload": wl["desc"], "requests": len(files), "total_bytes": total,
                                 "parallelism": f"replicas x{world}", "hbm_budget_bytes": SERVE_BUDGET,
                                 "l2": "working set (>= 1 GiB per step) exceeds the 129 MB L2",
                                 "verified": bool(verified),
+                                "bit_exact_vs_oracle": (f"{exact[0]}/{exact[1]} proofs of the last timed replay and "
+                                                        f"{e2e_exact[0]}/{e2e_exact[1]} of the last e2e replay equal "
+                                                        "the CPU oracle's (SHA-256, tests/golden/"
+                                                        "workload_digests.json)") if exact else
+                                "no oracle digests for this rank's files",
+                                "proofs_exact": exact[0] if exact else None,
+                                "proofs_checked": exact[1] if exact else None,
                                 "waves_per_step": (st1["waves"] - st0["waves"]) / args.steps,
                                 "launches_per_step": (st1["launches"] - st0["launches"]) / args.steps,
                                 "gpu_idle_ms_per_step": (st1["gpu_idle_ms"] - st0["gpu_idle_ms"]) / args.steps,
@@ -731,7 +920,10 @@ def run_gpu(args, wl):
                              "d2h_bytes_per_step": d2h},
                      "plain_mib_s": plain, "serving_vs_plain": value / plain,
                      "gpu_launches": int(st1["launches"] - st0["launches"]),
-                     "roofline": roofline(stats, "the same K steps rerun with per-kernel CUDA events"),
+                     "roofline": roofline(stats, "one more replay of the workload with a single stage wave in "
+                                                 "flight: launches serialised on one stream, per-kernel CUDA "
+                                                 f"events ({serial_same}/{len(files)} proofs identical to the "
+                                                 "timed replay's)", int_rates),
                      "clocks": clk})
         if lat:
             line["latency_ms"] = lat
@@ -752,9 +944,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="serve", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched set measured beside the serving "
+                    "stream")
     ap.add_argument("--waves", type=int, default=0, help="engine stage waves in flight (0: library default)")
     args = ap.parse_args()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload], name=args.workload)
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_gpu(args, wl)

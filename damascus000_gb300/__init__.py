@@ -40,7 +40,7 @@ _CODE_NAMES = {EINVAL: "EINVAL", ENOMEM_BUDGET: "ENOMEM_BUDGET", ECUDA: "ECUDA",
 EXPORTED_SYMBOLS = (
     "damascus_ctx_create", "damascus_ctx_destroy", "damascus_last_error", "damascus_create_error",
     "damascus_ctx_budget", "damascus_ctx_reserved",
-    "damascus_ctx_set_max_preprocess_bytes", "damascus_ctx_max_preprocess_bytes",
+    "damascus_ctx_set_max_preprocess_bytes", "damascus_ctx_max_preprocess_bytes", "damascus_measure_int_multiply",
     "damascus_fp_add", "damascus_fp_sub", "damascus_fp_mul", "damascus_fp_inv",
     "damascus_fp_from_le_bytes_mod_order", "damascus_blake3", "damascus_blake3_keyed",
     "damascus_transcript_challenge", "damascus_coeff_count_for_byte_len", "damascus_layout_for_byte_len",
@@ -176,6 +176,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_ctx_set_generator_cache", i32, vp, u64)
     sig("damascus_ctx_set_max_preprocess_bytes", i32, vp, u64)
     sig("damascus_ctx_max_preprocess_bytes", u64, vp)
+    sig("damascus_measure_int_multiply", i32, vp, P(ctypes.c_double))
     sig("damascus_ctx_generator_cache_stats", i32, vp, P(u64), P(u64), P(u64), P(u64))
     sig("damascus_verify_service_create", i32, vp, i32, u64, P(vp))
     sig("damascus_verify_service_destroy", None, vp)
@@ -380,6 +381,12 @@ class Context:
         return ms.value
 
     # -- profiling
+    def measure_int_multiply(self) -> dict:
+        """Measured ops/s of 32-bit multiply-add, mul.hi and 32x32->64 multiply-add."""
+        v = (ctypes.c_double * 3)()
+        self.check(self._lib.damascus_measure_int_multiply(self._h, v), "measure_int_multiply")
+        return {"mul.lo": v[0], "mul.hi": v[1], "mad.wide": v[2]}
+
     def set_profiling(self, on: bool) -> None:
         self.check(self._lib.damascus_ctx_set_profiling(self._h, int(on)), "set_profiling")
 

@@ -543,6 +543,38 @@ int damascus_tuning_get(damascus_ctx* ctx, int knob, uint32_t log_ring, int* val
     return DAMASCUS_OK;
 }
 
+int damascus_measure_int_multiply(damascus_ctx* ctx, double ops_per_s[3]) {
+    if (!ctx || !ops_per_s) return DAMASCUS_EINVAL;
+    Context* C = ctx->ctx;
+    std::lock_guard<std::mutex> g(C->mutex());
+    cudaSetDevice(C->device());
+    cudaStream_t st = C->stream();
+    Scratch sink;
+    if (sink.alloc(C, 256)) return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
+    const int blocks = 4 * C->sm_count(), iters = 4096;
+    const double ops = (double)int_mul_probe_ops(blocks, iters);
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    for (int kind = 0; kind < 3 && e == cudaSuccess; ++kind) {
+        double best = 0;
+        for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {  // the first launch warms up
+            e = cudaEventRecord(a, st);
+            if (e == cudaSuccess) e = launch_int_mul_probe(kind, sink.m.as<uint32_t>(), blocks, 3u + rep, iters, st);
+            if (e == cudaSuccess) e = cudaEventRecord(b, st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            if (e == cudaSuccess && rep > 0 && ms > 0 && ops / (ms * 1e-3) > best) best = ops / (ms * 1e-3);
+        }
+        ops_per_s[kind] = best;
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (e != cudaSuccess) return set_err(ctx, DAMASCUS_ECUDA, std::string("integer multiply probe: ") + cudaGetErrorString(e));
+    return DAMASCUS_OK;
+}
+
 int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int value, uint32_t count, int reps,
                             double* ms_per_launch) {
     if (!ctx || !ms_per_launch || count == 0 || reps <= 0 || log_ring > (uint32_t)kLogMaxProverRing)

@@ -49,4 +49,11 @@ cudaError_t launch_fold_gen_round(const uint4* d_src, uint4* d_dst, uint64_t N, 
 // a[i] = a[i] mod q for arbitrary 128-bit words
 cudaError_t launch_canon(uint4* d_a, uint64_t n, cudaStream_t st);
 
+// ---- measurement (k_probe.cu) ----
+// Issue-rate probe of one integer multiply form (0: 32-bit multiply-add, 1: high
+// half of a 32 x 32 product, 2: 32 x 32 -> 64 multiply-add): `blocks` blocks of
+// independent chains, int_mul_probe_ops(blocks, iters) operations per launch.
+cudaError_t launch_int_mul_probe(int kind, uint32_t* d_sink, int blocks, uint32_t seed, int iters, cudaStream_t st);
+uint64_t int_mul_probe_ops(int blocks, int iters);
+
 }  // namespace dm

@@ -19,6 +19,161 @@ const uint32_t kIV[8] = {DM_B3_IV0, DM_B3_IV1, DM_B3_IV2, DM_B3_IV3, DM_B3_IV4, 
 void words16(const uint8_t* p, uint32_t m[16]) {
     for (int i = 0; i < 16; ++i) m[i] = b3_load_le32(p + 4 * i);
 }
+
+// ---- lane-parallel compressions ----
+//
+// kLanes independent compressions at once in generic vector types (one lane per
+// chunk, or per parent node): the compiler maps them to the host's SIMD unit
+// (NEON on aarch64, SSE on x86-64) without architecture intrinsics, so the same
+// code builds and gives the same digests on both.
+constexpr int kLanes = 4;
+typedef uint32_t LaneVec __attribute__((vector_size(4 * kLanes)));
+
+inline LaneVec b3_rotr(LaneVec x, uint32_t n) { return (x >> n) | (x << (32u - n)); }
+inline LaneVec splat(uint32_t s) {
+    LaneVec v = {};
+    return v + s;
+}
+
+// The chaining value half of kLanes compressions: cv (per lane) is replaced by
+// the output words 0..7.
+inline void compress_lanes(LaneVec cv[8], const LaneVec m[16], const LaneVec& ctr_lo, const LaneVec& ctr_hi,
+                           uint32_t block_len, uint32_t flags) {
+    LaneVec v0 = cv[0], v1 = cv[1], v2 = cv[2], v3 = cv[3], v4 = cv[4], v5 = cv[5], v6 = cv[6], v7 = cv[7];
+    LaneVec v8 = splat(DM_B3_IV0), v9 = splat(DM_B3_IV1), v10 = splat(DM_B3_IV2), v11 = splat(DM_B3_IV3);
+    LaneVec v12 = ctr_lo, v13 = ctr_hi, v14 = splat(block_len), v15 = splat(flags);
+    DM_B3_ROUND(m, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15);
+    DM_B3_ROUND(m, 2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8);
+    DM_B3_ROUND(m, 3, 4, 10, 12, 13, 2, 7, 14, 6, 5, 9, 0, 11, 15, 8, 1);
+    DM_B3_ROUND(m, 10, 7, 12, 9, 14, 3, 13, 15, 4, 0, 11, 2, 5, 8, 1, 6);
+    DM_B3_ROUND(m, 12, 13, 9, 11, 15, 10, 14, 8, 7, 2, 5, 3, 0, 1, 6, 4);
+    DM_B3_ROUND(m, 9, 14, 11, 5, 8, 12, 15, 1, 13, 3, 0, 10, 2, 6, 4, 7);
+    DM_B3_ROUND(m, 11, 15, 5, 0, 1, 9, 8, 6, 14, 10, 2, 12, 3, 4, 7, 13);
+    cv[0] = v0 ^ v8;
+    cv[1] = v1 ^ v9;
+    cv[2] = v2 ^ v10;
+    cv[3] = v3 ^ v11;
+    cv[4] = v4 ^ v12;
+    cv[5] = v5 ^ v13;
+    cv[6] = v6 ^ v14;
+    cv[7] = v7 ^ v15;
+}
+
+// Message words i of kLanes 64-byte blocks that start `stride` bytes apart.
+inline void load_lanes(const uint8_t* p, size_t stride, LaneVec m[16]) {
+    alignas(64) uint32_t t[16][kLanes];
+    for (int l = 0; l < kLanes; ++l)
+        for (int i = 0; i < 16; ++i) t[i][l] = b3_load_le32(p + l * stride + 4 * i);
+    for (int i = 0; i < 16; ++i) std::memcpy(&m[i], t[i], sizeof(LaneVec));
+}
+
+inline void store_lanes(const LaneVec cv[8], uint32_t* out) {  // out: kLanes x 8 words
+    alignas(64) uint32_t t[8][kLanes];
+    for (int i = 0; i < 8; ++i) std::memcpy(t[i], &cv[i], sizeof(LaneVec));
+    for (int l = 0; l < kLanes; ++l)
+        for (int i = 0; i < 8; ++i) out[8 * l + i] = t[i][l];
+}
+
+// Chaining values of kLanes full (1024-byte, non-root) chunks first .. first + kLanes - 1.
+void full_chunk_cvs_lanes(const uint8_t* data, uint64_t first, const uint32_t key[8], uint32_t flags,
+                          uint32_t* out) {
+    LaneVec cv[8], m[16];
+    for (int i = 0; i < 8; ++i) cv[i] = splat(key[i]);
+    alignas(64) uint32_t lo[kLanes], hi[kLanes];
+    for (int l = 0; l < kLanes; ++l) {
+        lo[l] = (uint32_t)(first + l);
+        hi[l] = (uint32_t)((first + l) >> 32);
+    }
+    LaneVec ctr_lo, ctr_hi;
+    std::memcpy(&ctr_lo, lo, sizeof(LaneVec));
+    std::memcpy(&ctr_hi, hi, sizeof(LaneVec));
+    const uint8_t* base = data + first * kB3ChunkLen;
+    for (uint32_t b = 0; b < kB3ChunkLen / kB3BlockLen; ++b) {
+        load_lanes(base + b * kB3BlockLen, kB3ChunkLen, m);
+        const uint32_t f = flags | (b == 0 ? kB3ChunkStart : 0u) | (b + 1 == kB3ChunkLen / kB3BlockLen ? kB3ChunkEnd : 0u);
+        compress_lanes(cv, m, ctr_lo, ctr_hi, kB3BlockLen, f);
+    }
+    store_lanes(cv, out);
+}
+
+// Chaining value of chunk c (any length, never the root).
+void one_chunk_cv(const uint8_t* data, size_t len, uint64_t c, const uint32_t key[8], uint32_t flags, uint32_t out[8]) {
+    const size_t off = c * kB3ChunkLen;
+    const size_t clen = len - off < kB3ChunkLen ? len - off : kB3ChunkLen;
+    const size_t nblocks = clen ? (clen + 63) / 64 : 1;
+    uint32_t cv[8];
+    std::memcpy(cv, key, 32);
+    for (size_t b = 0; b < nblocks; ++b) {
+        uint8_t block[64];
+        const size_t bl = clen - b * 64 < 64 ? clen - b * 64 : 64;
+        std::memset(block, 0, 64);
+        std::memcpy(block, data + off + b * 64, bl);
+        uint32_t m[16], o[16];
+        words16(block, m);
+        const uint32_t f = flags | (b == 0 ? kB3ChunkStart : 0u) | (b + 1 == nblocks ? kB3ChunkEnd : 0u);
+        b3_compress(cv, m, c, (uint32_t)bl, f, o);
+        std::memcpy(cv, o, 32);
+    }
+    std::memcpy(out, cv, 32);
+}
+
+// Chaining values of chunks [begin, end) of a message of len bytes into cvs
+// (8 words per chunk): groups of kLanes full chunks in the lanes, the rest one by one.
+void chunk_cvs_range(const uint8_t* data, size_t len, size_t begin, size_t end, const uint32_t key[8],
+                     uint32_t flags, uint32_t* cvs) {
+    const size_t full = len / kB3ChunkLen;  // chunks with all 1024 bytes
+    size_t c = begin;
+    for (; c + kLanes <= end && c + kLanes <= full; c += kLanes) full_chunk_cvs_lanes(data, c, key, flags, cvs + 8 * c);
+    for (; c < end; ++c) one_chunk_cv(data, len, c, key, flags, cvs + 8 * c);
+}
+
+// Parents of one tree level: n nodes (8 words each) in src -> (n + 1) / 2 in dst,
+// an odd last node carried up unchanged; with n == 2 the one parent is the root.
+void merge_level(const uint32_t* src, size_t n, const uint32_t key[8], uint32_t flags, uint32_t* dst) {
+    const size_t pairs = n / 2;
+    const uint32_t pf = flags | kB3Parent | (n == 2 ? kB3Root : 0u);
+    size_t j = 0;
+    if (n > 2) {
+        const LaneVec zero = {};
+        for (; j + kLanes <= pairs; j += kLanes) {
+            LaneVec cv[8], m[16];
+            for (int i = 0; i < 8; ++i) cv[i] = splat(key[i]);
+            load_lanes(reinterpret_cast<const uint8_t*>(src + 16 * j), 64, m);
+            compress_lanes(cv, m, zero, zero, kB3BlockLen, pf);
+            store_lanes(cv, dst + 8 * j);
+        }
+    }
+    for (; j < pairs; ++j) {
+        uint32_t o[16];
+        b3_compress(key, src + 16 * j, 0, kB3BlockLen, pf, o);
+        std::memcpy(dst + 8 * j, o, 32);
+    }
+    if (n & 1) std::memcpy(dst + 8 * pairs, src + 8 * (n - 1), 32);
+}
+
+void words_to_bytes(const uint32_t w[8], uint8_t out[32]) {
+    for (int i = 0; i < 8; ++i) {
+        out[4 * i] = (uint8_t)w[i];
+        out[4 * i + 1] = (uint8_t)(w[i] >> 8);
+        out[4 * i + 2] = (uint8_t)(w[i] >> 16);
+        out[4 * i + 3] = (uint8_t)(w[i] >> 24);
+    }
+}
+
+// Root of the tree over nchunks >= 2 chunk chaining values (the tree is left
+// complete, which pairing level by level with the odd node carried up reproduces).
+void tree_root(std::vector<uint32_t>& a, size_t nchunks, const uint32_t key[8], uint32_t flags, uint8_t out[32]) {
+    std::vector<uint32_t> b(8 * ((nchunks + 1) / 2));
+    uint32_t* src = a.data();
+    uint32_t* dst = b.data();
+    size_t n = nchunks;
+    while (n > 1) {
+        merge_level(src, n, key, flags, dst);
+        n = (n + 1) / 2;
+        std::swap(src, dst);
+    }
+    words_to_bytes(src, out);
+}
 }  // namespace
 
 Blake3Hasher::Blake3Hasher() : flags_(0) {
@@ -120,16 +275,33 @@ void Blake3Hasher::finalize(uint8_t out[32]) const {
     }
 }
 
-void blake3_hash(const void* data, size_t len, uint8_t out[32]) {
-    Blake3Hasher h;
-    h.update(data, len);
-    h.finalize(out);
+namespace {
+// One-shot hash: a single chunk through the incremental hasher (its last block is
+// the root), longer inputs as chunk chaining values in the lanes plus the tree.
+void hash_oneshot(const uint8_t* key_bytes, const void* data, size_t len, uint8_t out[32]) {
+    if (len <= kB3ChunkLen) {
+        Blake3Hasher h = key_bytes ? Blake3Hasher(key_bytes) : Blake3Hasher();
+        h.update(data, len);
+        h.finalize(out);
+        return;
+    }
+    uint32_t key[8];
+    if (key_bytes)
+        for (int i = 0; i < 8; ++i) key[i] = b3_load_le32(key_bytes + 4 * i);
+    else
+        std::memcpy(key, kIV, 32);
+    const uint32_t flags = key_bytes ? kB3Keyed : 0u;
+    const size_t nchunks = (len + kB3ChunkLen - 1) / kB3ChunkLen;
+    std::vector<uint32_t> cvs(8 * nchunks);
+    chunk_cvs_range(static_cast<const uint8_t*>(data), len, 0, nchunks, key, flags, cvs.data());
+    tree_root(cvs, nchunks, key, flags, out);
 }
+}  // namespace
+
+void blake3_hash(const void* data, size_t len, uint8_t out[32]) { hash_oneshot(nullptr, data, len, out); }
 
 void blake3_keyed_hash(const uint8_t key[32], const void* data, size_t len, uint8_t out[32]) {
-    Blake3Hasher h(key);
-    h.update(data, len);
-    h.finalize(out);
+    hash_oneshot(key, data, len, out);
 }
 
 // ============================================================== host pool
@@ -197,27 +369,13 @@ struct ChunkArgs {
     uint32_t* cvs;
 };
 
+// Task bounds are rounded to whole lane groups, so every group but the last runs in the lanes.
 void chunk_cvs(void* a, size_t begin, size_t end) {
     const ChunkArgs* A = static_cast<const ChunkArgs*>(a);
-    for (size_t c = begin; c < end; ++c) {
-        const size_t off = c * kB3ChunkLen;
-        const size_t clen = A->len - off < kB3ChunkLen ? A->len - off : kB3ChunkLen;
-        const size_t nblocks = (clen + 63) / 64;
-        uint32_t cv[8];
-        std::memcpy(cv, kIV, 32);
-        for (size_t b = 0; b < nblocks; ++b) {
-            uint8_t block[64];
-            const size_t bl = clen - b * 64 < 64 ? clen - b * 64 : 64;
-            std::memset(block, 0, 64);
-            std::memcpy(block, A->data + off + b * 64, bl);
-            uint32_t m[16], out[16];
-            words16(block, m);
-            uint32_t f = (b == 0 ? kB3ChunkStart : 0u) | (b + 1 == nblocks ? kB3ChunkEnd : 0u);
-            b3_compress(cv, m, c, (uint32_t)bl, f, out);
-            std::memcpy(cv, out, 32);
-        }
-        std::memcpy(A->cvs + 8 * c, cv, 32);
-    }
+    const size_t nchunks = (A->len + kB3ChunkLen - 1) / kB3ChunkLen;
+    begin *= kLanes;
+    end = end * kLanes < nchunks ? end * kLanes : nchunks;
+    chunk_cvs_range(A->data, A->len, begin, end, kIV, 0u, A->cvs);
 }
 
 }  // namespace
@@ -255,33 +413,10 @@ void blake3_hash_parallel(const void* data, size_t len, uint8_t out[32]) {
         blake3_hash(data, len, out);
         return;
     }
-    std::vector<uint32_t> a(8 * nchunks), b(8 * nchunks);
+    std::vector<uint32_t> a(8 * nchunks);
     ChunkArgs args{static_cast<const uint8_t*>(data), len, a.data()};
-    host_parallel_for(nchunks, 16, chunk_cvs, &args);
-    // pairwise merge with carry; the final merge is the root
-    size_t n = nchunks;
-    uint32_t* src = a.data();
-    uint32_t* dst = b.data();
-    uint32_t outw[16];
-    while (n > 1) {
-        const size_t pairs = n / 2;
-        for (size_t j = 0; j < pairs; ++j) {
-            uint32_t m[16];
-            std::memcpy(m, src + 16 * j, 64);
-            const bool root = (n == 2);
-            b3_compress(kIV, m, 0, kB3BlockLen, kB3Parent | (root ? kB3Root : 0u), outw);
-            std::memcpy(dst + 8 * j, outw, 32);
-        }
-        if (n & 1) std::memcpy(dst + 8 * pairs, src + 8 * (n - 1), 32);
-        n = pairs + (n & 1);
-        std::swap(src, dst);
-    }
-    for (int i = 0; i < 8; ++i) {
-        out[4 * i] = (uint8_t)src[i];
-        out[4 * i + 1] = (uint8_t)(src[i] >> 8);
-        out[4 * i + 2] = (uint8_t)(src[i] >> 16);
-        out[4 * i + 3] = (uint8_t)(src[i] >> 24);
-    }
+    host_parallel_for((nchunks + kLanes - 1) / kLanes, 4, chunk_cvs, &args);
+    tree_root(a, nchunks, kIV, 0u, out);
 }
 
 }  // namespace dm

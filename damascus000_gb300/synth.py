@@ -108,3 +108,23 @@ def serving_stream(master_seed: int, count: int, rate_per_s: float = 200.0) -> L
         size = int(round(math.exp(math.log(lo) + r * (math.log(hi) - math.log(lo)))))
         out.append(Request(i, t, size))
     return out
+
+
+def serving_files(master_seed: int, count: int, rate_per_s: float = 200.0, seed_generators: bytes = None):
+    """[(file bytes, seed_generators, arrival_s)] of the serving stream.
+
+    File ``i`` is ``random_file(master_seed, size_i, 10_000 + i)``; with
+    ``seed_generators`` given, every file uses that one system seed instead of
+    its own (SystemParams::default, src/utils/config.rs:19, 33-44)."""
+    out = []
+    for r in serving_stream(master_seed, count, rate_per_s):
+        data, seed = random_file(master_seed, r.size, 10_000 + r.index)
+        out.append((data, seed_generators if seed_generators is not None else seed, r.arrival_s))
+    return out
+
+
+def batched_files(master_seed: int, count: int, lo: int, hi: int):
+    """[(file bytes, seed_generators, 0.0)] of the batched set: log-uniform sizes in
+    [lo, hi], file ``i`` = ``random_file(master_seed, size_i, 20_000 + i)``."""
+    sizes = log_uniform_sizes(master_seed, count, lo, hi)
+    return [random_file(master_seed, n, 20_000 + i) + (0.0,) for i, n in enumerate(sizes)]

@@ -303,6 +303,12 @@ int damascus_ctx_kernel_stat(damascus_ctx* ctx, const char* name, uint64_t* laun
 int damascus_ctx_synchronize(damascus_ctx* ctx);
 /* Writes 256 MiB (more than the 129 MB L2) on the context stream and waits. */
 int damascus_ctx_flush_l2(damascus_ctx* ctx);
+/* Measured issue rates (operations per second, best of three launches after a
+ * warm-up) of the three integer multiply forms the forward transform spends its
+ * multiplier on: [0] 32-bit multiply-add, [1] high half of a 32 x 32 product,
+ * [2] 32 x 32 -> 64 multiply-add.  The peaks against which bench.py states the
+ * transform's counted multiplies (no reference counterpart). */
+int damascus_measure_int_multiply(damascus_ctx* ctx, double ops_per_s[3]);
 
 /* ------------------------------------------------------------------ launch-shape tuning */
 /* Knobs of the kernels' launch shapes per ring size 2^log_ring (no reference

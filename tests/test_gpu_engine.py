@@ -67,18 +67,25 @@ def test_engine_admission_respects_budget():
         c.close()
 
 
-def test_engine_failure_is_isolated(ctx):
+@pytest.mark.parametrize("limit,code", [(0, D.EINVAL), (1 << 40, D.EUNSUPPORTED)])
+def test_engine_failure_is_isolated(ctx, limit, code):
+    """872 MB + 1 byte lands on depth 14: above the reference's default expansion
+    limit (EINVAL, as src/utils/io.rs:42-49), and with the limit raised above the
+    supported maximum depth (13: the CRT range).  The requests around it finish."""
     good = _files(92, [40_000, 70_000])
-    with D.Engine(ctx) as eng:
-        t0 = eng.submit(*good[0], EPOCH)
-        # 872 MB + 1 byte lands on depth 14, above the supported maximum (13: the CRT range)
-        bad = eng.submit(bytes(8192 * 8192 * 13 + 1), bytes(32), EPOCH)
-        t1 = eng.submit(*good[1], EPOCH)
-        p0 = eng.wait(t0)[0]
-        with pytest.raises(D.DamascusError) as e:
-            eng.wait(bad)
-        p1 = eng.wait(t1)[0]
-    assert e.value.code == D.EUNSUPPORTED
+    ctx.set_max_preprocess_bytes(limit)
+    try:
+        with D.Engine(ctx) as eng:
+            t0 = eng.submit(*good[0], EPOCH)
+            bad = eng.submit(bytes(8192 * 8192 * 13 + 1), bytes(32), EPOCH)
+            t1 = eng.submit(*good[1], EPOCH)
+            p0 = eng.wait(t0)[0]
+            with pytest.raises(D.DamascusError) as e:
+                eng.wait(bad)
+            p1 = eng.wait(t1)[0]
+    finally:
+        ctx.set_max_preprocess_bytes(0)
+    assert e.value.code == code
     assert p0 == ctx.prove(*good[0], EPOCH)
     assert p1 == ctx.prove(*good[1], EPOCH)
 
