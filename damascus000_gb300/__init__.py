@@ -302,6 +302,7 @@ class Context:
             raise DamascusError(rc, L.damascus_create_error().decode())
         self._h = h
         self._lib = L
+        self.engine_waves = 0  # stage waves an Engine keeps in flight when none is given (0: the library's 16)
         if tuning is not None:
             from . import autotune
             autotune.apply(self, table=None if tuning == "auto" else tuning)
@@ -604,6 +605,7 @@ class Engine:
     def __init__(self, ctx: Context, host_threads: int = 0, max_waves: int = 0):
         self._ctx = ctx
         self._lib = ctx._lib
+        max_waves = max_waves or getattr(ctx, "engine_waves", 0)
         h = ctypes.c_void_p()
         ctx.check(self._lib.damascus_engine_create(ctx.handle, host_threads, max_waves, ctypes.byref(h)),
                   "engine create")

@@ -9,7 +9,13 @@ writes a table that `apply()` loads into a context:
   (32 or 64: how many small polynomials share a block);
 * `MAC_TRIPLE`, `MAC_SPLIT`, `MAC_PLAIN` — the resident blocks per SM that a
   multiply-accumulate's column split fills (its part count; more parts mean more
-  blocks in flight but more partial sums for the finish to add).
+  blocks in flight but more partial sums for the finish to add);
+* `SPLIT_COORDS` — commitment coordinates per thread of the split MAC (1, 2, 4
+  or 8: each witness slot pair loaded once for that many generator rows, at the
+  cost of registers).  It is tuned jointly with `MAC_SPLIT`: every pair is timed;
+* `engine_waves` — stage waves the serving engine keeps in flight (one stream
+  each), timed end to end on a replay of a serving-stream mix; `Engine(ctx)`
+  takes it when no count is given.
 
 Results never depend on the table; only launch shapes do.  The table committed
 beside this file (`tuning_gb300.json`) came from `python -m damascus000_gb300.autotune`
@@ -23,13 +29,15 @@ import time
 from pathlib import Path
 from typing import Dict, List, Optional
 
-NTT_GROUP, MAC_TRIPLE, MAC_SPLIT, MAC_PLAIN = 0, 1, 2, 3
-KNOB_NAMES = {NTT_GROUP: "ntt_group", MAC_TRIPLE: "mac_triple", MAC_SPLIT: "mac_split", MAC_PLAIN: "mac_plain"}
+NTT_GROUP, MAC_TRIPLE, MAC_SPLIT, MAC_PLAIN, SPLIT_COORDS = 0, 1, 2, 3, 4
+KNOB_NAMES = {NTT_GROUP: "ntt_group", MAC_TRIPLE: "mac_triple", MAC_SPLIT: "mac_split", MAC_PLAIN: "mac_plain",
+              SPLIT_COORDS: "split_coords"}
 CANDIDATES = {
     NTT_GROUP: [32, 64],
     MAC_TRIPLE: [2, 4, 8, 12, 16, 24],
     MAC_SPLIT: [2, 4, 8, 12, 16, 24],
     MAC_PLAIN: [2, 4, 8, 16],
+    SPLIT_COORDS: [1, 2, 4, 8],
 }
 DEFAULT_TABLE = Path(__file__).resolve().parent / "tuning_gb300.json"
 
@@ -52,7 +60,10 @@ def ring_sizes(knob: int) -> List[int]:
     return list(range(4, 13))
 
 
-DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8}  # the library's built-in values
+DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1}  # the library's built-ins
+ENGINE_WAVES = "engine_waves"
+WAVE_CANDIDATES = [4, 8, 12, 16, 24, 32]
+DEFAULT_WAVES = 16
 
 
 def choose(times: Dict[int, float], default: int, margin: float = 0.03, min_gain_ms: float = 0.001) -> int:
@@ -71,10 +82,15 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
     """Measures every candidate and sets the chosen value on `ctx`; returns the table."""
     entries = []
     for knob in knobs if knobs is not None else list(CANDIDATES):
+        if knob == SPLIT_COORDS:
+            continue  # tuned with MAC_SPLIT
         for L in ring_sizes(knob):
             if L > max_L:
                 continue
             count = work_size(knob, L)
+            if knob == MAC_SPLIT:
+                entries += tune_split(ctx, L, count, reps, margin, log)
+                continue
             times = {}
             for v in CANDIDATES[knob]:
                 times[v] = ctx.tuning_measure(knob, L, v, count, reps)
@@ -88,6 +104,49 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
             "margin": margin, "min_gain_ms": 0.001, "entries": entries}
 
 
+def tune_split(ctx, L: int, count: int, reps: int, margin: float, log=print) -> List[Dict]:
+    """The split MAC's (coordinates per thread, blocks per SM) pair at ring 2^L:
+    every pair timed, the built-in pair kept unless beaten as `choose` requires."""
+    times = {}
+    for kc in CANDIDATES[SPLIT_COORDS]:
+        ctx.tuning_set(SPLIT_COORDS, L, kc)
+        for v in CANDIDATES[MAC_SPLIT]:
+            times[(kc, v)] = ctx.tuning_measure(MAC_SPLIT, L, v, count, reps)
+    kc, v = choose(times, (DEFAULTS[SPLIT_COORDS], DEFAULTS[MAC_SPLIT]), margin)
+    ctx.tuning_set(SPLIT_COORDS, L, kc)
+    ctx.tuning_set(MAC_SPLIT, L, v)
+    ms = {f"{a}x{b}": round(t, 5) for (a, b), t in times.items()}
+    log(f"split      L={L:2d} count={count:6d} best={kc}x{v} " + " ".join(f"{k}:{t:.4f}" for k, t in ms.items()))
+    return [{"knob": KNOB_NAMES[MAC_SPLIT], "log_ring": L, "value": v, "count": count, "ms": ms},
+            {"knob": KNOB_NAMES[SPLIT_COORDS], "log_ring": L, "value": kc, "count": count}]
+
+
+def tune_waves(ctx, requests: int = 48, reps: int = 3, margin: float = 0.03, log=print) -> Dict:
+    """Stage waves in flight of the serving engine: end-to-end MiB/s of `reps`
+    replays (after one warm-up) of a serving-stream mix of `requests` files
+    (host buffers, copies included), per candidate."""
+    import damascus000_gb300 as D
+    from damascus000_gb300 import synth
+    files = synth.serving_files(0x7E57, requests, 200.0)
+    total = sum(len(d) for d, _, _ in files)
+    epoch = D.DEFAULT_EPOCH_SEED
+    rates = {}
+    for w in WAVE_CANDIDATES:
+        with D.Engine(ctx, max_waves=w) as eng:
+            eng.prove_batch([(d, s, epoch) for d, s, _ in files])
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                eng.prove_batch([(d, s, epoch) for d, s, _ in files])
+            rates[w] = reps * total / (1 << 20) / (time.perf_counter() - t0)
+    best = max(rates, key=rates.get)
+    if rates[best] < (1.0 + margin) * rates[DEFAULT_WAVES]:
+        best = DEFAULT_WAVES
+    ctx.engine_waves = best
+    log(f"engine_waves best={best} " + " ".join(f"{w}:{r:.0f}MiB/s" for w, r in rates.items()))
+    return {"knob": ENGINE_WAVES, "value": best, "requests": requests, "total_bytes": total,
+            "mib_s": {str(w): round(r, 1) for w, r in rates.items()}}
+
+
 def apply(ctx, table: Optional[Dict] = None, path: Optional[Path] = None) -> int:
     """Sets a table's values on `ctx` (the packaged GB300 table by default); returns how many."""
     if table is None:
@@ -98,7 +157,10 @@ def apply(ctx, table: Optional[Dict] = None, path: Optional[Path] = None) -> int
     names = {v: k for k, v in KNOB_NAMES.items()}
     n = 0
     for e in table.get("entries", []):
-        ctx.tuning_set(names[e["knob"]], int(e["log_ring"]), int(e["value"]))
+        if e["knob"] == ENGINE_WAVES:
+            ctx.engine_waves = int(e["value"])
+        else:
+            ctx.tuning_set(names[e["knob"]], int(e["log_ring"]), int(e["value"]))
         n += 1
     return n
 
@@ -108,10 +170,13 @@ def main() -> None:
     ap.add_argument("--out", default=str(DEFAULT_TABLE))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--max-L", type=int, default=12)
+    ap.add_argument("--no-waves", action="store_true", help="skip the engine's waves-in-flight sweep")
     args = ap.parse_args()
     import damascus000_gb300 as D
-    ctx = D.Context(0)
+    ctx = D.Context(0, tuning=None)
     table = tune(ctx, reps=args.reps, max_L=args.max_L)
+    if not args.no_waves:
+        table["entries"].append(tune_waves(ctx))
     Path(args.out).write_text(json.dumps(table, indent=1) + "\n")
     print(f"wrote {args.out} ({len(table['entries'])} entries)")
 

@@ -21,9 +21,10 @@ enum TuneKnob : int {
     kTuneMacTriple = 1,  // resident blocks per SM a triple MAC's column split fills: 1..32
     kTuneMacSplit = 2,   // the same for the split MAC
     kTuneMacPlain = 3,   // the same for the single-sum MAC
-    kTuneKnobs = 4,
+    kTuneSplitCoords = 4,  // commitment coordinates per thread of the split MAC: 1, 2, 4 or 8
+    kTuneKnobs = 5,
 };
-constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8};
+constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8, 1};
 static_assert((uint64_t)kMaxMacParts * ((1u << 28) - 1) < (1ull << 32), "part sums fit 32 bits");
 
 // ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][9][2^L] ----
@@ -50,6 +51,10 @@ struct MacJobX {
     // on zero, so the witness is read at i only and R is zero.
     uint32_t pair;
     uint32_t L;  // ring size 2^L of this job (jobs of any sizes share a launch)
+    // Split MAC only: commitment coordinates per thread, 1, 2, 4 or 8 (0 reads
+    // as 1).  A thread then loads each witness slot pair once for kc generator
+    // rows, and a part covers kRows / kc rows.
+    uint32_t kc;
 };
 
 // ---- sum partials, inverse NTT, CRT to Z_q, optional compare (all jobs share L) ----
@@ -119,7 +124,10 @@ struct HashJob {
 
 // group: threads per block for rings below 2^10 (32 or 64, kTuneNttGroup)
 cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group = 64);
-cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st);
+// kernels (optional): how many kernels it launched (the split MAC launches one
+// per coordinates-per-thread value among the jobs)
+cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st,
+                            int* kernels = nullptr);
 // Triple MAC (count = h column pairs): out0 = full sum, out1 = L, out2 = R.
 cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, cudaStream_t st);
 cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);  // 2 launches

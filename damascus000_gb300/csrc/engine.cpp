@@ -63,7 +63,10 @@ int Context::create(int device, uint64_t hbm_budget, Context** out, std::string*
 
 int Context::set_tuning(int knob, uint32_t L, int value) {
     if (knob < 0 || knob >= kTuneKnobs || L > (uint32_t)kLogMaxProverRing) return kEInval;
-    if (knob == kTuneNttGroup ? (value != 32 && value != 64) : (value < 1 || value > 32)) return kEInval;
+    if (knob == kTuneNttGroup ? (value != 32 && value != 64)
+        : knob == kTuneSplitCoords ? (value != 1 && value != 2 && value != 4 && value != 8)
+                                   : (value < 1 || value > 32))
+        return kEInval;
     tune_[knob][L].store(value, std::memory_order_relaxed);
     return kOk;
 }
@@ -72,8 +75,8 @@ uint32_t Context::mac_parts(int knob, uint32_t L, uint32_t threads_per_row, uint
     return mac_parts_for(tuning(knob, L), threads_per_row, count);
 }
 
-uint32_t Context::mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uint32_t count) const {
-    const uint32_t per_part = ((threads_per_row + 127) / 128) * (uint32_t)(kRank * kPrimes);
+uint32_t Context::mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uint32_t count, uint32_t rows) const {
+    const uint32_t per_part = ((threads_per_row + 127) / 128) * rows;
     uint32_t parts = (uint32_t)sm_count_ * (uint32_t)blocks_per_sm / per_part;
     if (parts > kMaxMacParts) parts = kMaxMacParts;
 #ifndef DM_MIN_PART_COLS

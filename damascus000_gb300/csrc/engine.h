@@ -82,7 +82,9 @@ class Context {
     // fewer partial rows for the finish; measured +2 % on the serving stream),
     // at least one part.
     uint32_t mac_parts(int knob, uint32_t L, uint32_t threads_per_row, uint32_t count) const;
-    uint32_t mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uint32_t count) const;
+    // rows: the thread rows one part launches (kRows; kRows / kc for the split MAC)
+    uint32_t mac_parts_for(int blocks_per_sm, uint32_t threads_per_row, uint32_t count,
+                           uint32_t rows = kRank * kPrimes) const;
 
     // Provers' generator cache (off until a capacity is set; 0 turns it off and
     // frees it once no prover holds an entry).  Set it before proving starts.

@@ -303,54 +303,81 @@ __global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<Ma
     *reinterpret_cast<uint2*>(jb.out2 + o) = make_uint2(red96(hi[4], lo[4], pc, pi), red96(hi[5], lo[5], pc, pi));
 }
 
-// Split MAC: thread per slot pair (2 i2, 2 i2 + 1) of ring 2^L (L >= 1): the
-// recompute check over all slots and the even/odd cross terms
-// (g(w) - g(-w)) (m(w) + m(-w)) and (g(w) + g(-w)) (m(w) - m(-w)) at 2^(L-1).
-__global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
-    const MacJobX jb = J.j[find_job(J)];
+// Split MAC: thread per slot pair (2 i2, 2 i2 + 1) of ring 2^L (L >= 1) and KC
+// commitment coordinates of one prime: the recompute check over all slots and
+// the even/odd cross terms (g(w) - g(-w)) (m(w) + m(-w)) and
+// (g(w) + g(-w)) (m(w) - m(-w)) at 2^(L-1).  Each column's witness slot pair is
+// loaded once for the KC generator rows (and its sum and difference formed once).
+template <int KC>
+DM_D void split_rows(const MacJobX& jb, uint32_t kg, uint32_t pi, uint32_t part, uint32_t i2, const PrimeConsts& pc) {
     const uint32_t L = jb.L;
-    const uint32_t hs = 1u << (L - 1);
-    const uint32_t nblk = slot_block_count(hs);
-    uint32_t c = blockIdx.x - jb.cta0;
-    const uint32_t blk = c % nblk;
-    c /= nblk;
-    const uint32_t kp = c % kRows;
-    const uint32_t part = c / kRows;
-    const uint32_t i2 = blk * kMacThreads + threadIdx.x;
-    if (i2 >= hs) return;
-    const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
     const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
     const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
     const uint32_t p = pc.p[pi];
     const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
     const uint64_t mstride = (uint64_t)kPrimes << L;
-    const uint32_t* g = jb.G + ((((uint64_t)jb.g_base * kRank + k) * kPrimes + pi) << L) + 2 * i2;
+    const uint64_t kstride = (uint64_t)kPrimes << L;  // the next coordinate's row, same prime
+    const uint32_t* g = jb.G + ((((uint64_t)jb.g_base * kRank + kg * KC) * kPrimes + pi) << L) + 2 * i2;
     const uint32_t* m = jb.M + (((uint64_t)jb.m_base * kPrimes + pi) << L) + 2 * i2;
-    uint64_t l0 = 0, l1 = 0, ll = 0, lr = 0;
-    uint32_t h0 = 0, h1 = 0, hl = 0, hr = 0;
+    uint64_t l0[KC], l1[KC], ll[KC], lr[KC];
+    uint32_t h0[KC], h1[KC], hl[KC], hr[KC];
+#pragma unroll
+    for (int j = 0; j < KC; ++j) l0[j] = l1[j] = ll[j] = lr[j] = 0, h0[j] = h1[j] = hl[j] = hr[j] = 0;
+    constexpr int kUnroll = KC >= 4 ? 2 : 8 / KC;
     uint32_t i = i0;
     while (i < i1) {
         const uint32_t e = i + 16 < i1 ? i + 16 : i1;
-        uint64_t b0 = 0, b1 = 0, bl = 0, br = 0;
-#pragma unroll 8
+        uint64_t b0[KC], b1[KC], bl[KC], br[KC];
+#pragma unroll
+        for (int j = 0; j < KC; ++j) b0[j] = b1[j] = bl[j] = br[j] = 0;
+#pragma unroll kUnroll
         for (; i < e; ++i) {
-            const uint2 gv = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
             const uint2 mv = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
-            b0 += mul64(gv.x, mv.x);
-            b1 += mul64(gv.y, mv.y);
             // sums and differences below 2p: products below 4p^2 < 2^58, 16 of them fit
-            bl += mul64(gv.x + p - gv.y, mv.x + mv.y);
-            br += mul64(gv.x + gv.y, mv.x + p - mv.y);
+            const uint32_t msum = mv.x + mv.y, mdif = mv.x + p - mv.y;
+#pragma unroll
+            for (int j = 0; j < KC; ++j) {
+                const uint2 gv = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + j * kstride));
+                b0[j] += mul64(gv.x, mv.x);
+                b1[j] += mul64(gv.y, mv.y);
+                bl[j] += mul64(gv.x + p - gv.y, msum);
+                br[j] += mul64(gv.x + gv.y, mdif);
+            }
         }
-        acc96(l0, h0, b0);
-        acc96(l1, h1, b1);
-        acc96(ll, hl, bl);
-        acc96(lr, hr, br);
+#pragma unroll
+        for (int j = 0; j < KC; ++j) {
+            acc96(l0[j], h0[j], b0[j]);
+            acc96(l1[j], h1[j], b1[j]);
+            acc96(ll[j], hl[j], bl[j]);
+            acc96(lr[j], hr[j], br[j]);
+        }
     }
-    *reinterpret_cast<uint2*>(jb.out0 + (((uint64_t)part * kRows + kp) << L) + 2 * i2) =
-        make_uint2(red96(h0, l0, pc, pi), red96(h1, l1, pc, pi));
-    jb.out1[(((uint64_t)part * kRows + kp) << (L - 1)) + i2] = red96(hl, ll, pc, pi);
-    jb.out2[(((uint64_t)part * kRows + kp) << (L - 1)) + i2] = red96(hr, lr, pc, pi);
+#pragma unroll
+    for (int j = 0; j < KC; ++j) {
+        const uint64_t row = (uint64_t)part * kRows + (kg * KC + j) * kPrimes + pi;
+        *reinterpret_cast<uint2*>(jb.out0 + (row << L) + 2 * i2) =
+            make_uint2(red96(h0[j], l0[j], pc, pi), red96(h1[j], l1[j], pc, pi));
+        jb.out1[(row << (L - 1)) + i2] = red96(hl[j], ll[j], pc, pi);
+        jb.out2[(row << (L - 1)) + i2] = red96(hr[j], lr[j], pc, pi);
+    }
+}
+
+// grid: per job, nblk * (72 / KC) * parts blocks; block -> (part, coordinate group x prime, slot block).
+// Every job of a launch has kc == KC (the launcher groups them).
+template <int KC>
+__global__ void __launch_bounds__(kMacThreads) mac_split_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
+    const MacJobX jb = J.j[find_job(J)];
+    const uint32_t hs = 1u << (jb.L - 1);
+    const uint32_t nblk = slot_block_count(hs);
+    constexpr uint32_t rows = kRows / KC;
+    uint32_t c = blockIdx.x - jb.cta0;
+    const uint32_t blk = c % nblk;
+    c /= nblk;
+    const uint32_t kp = c % rows;
+    const uint32_t part = c / rows;
+    const uint32_t i2 = blk * kMacThreads + threadIdx.x;
+    if (i2 >= hs) return;
+    split_rows<KC>(jb, kp / kPrimes, kp % kPrimes, part, i2, pc);
 }
 
 // ================================================================ finish
@@ -735,7 +762,7 @@ cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t
 namespace {
 template <class Slots>
 cudaError_t mac_launch_common(MacJobX* jobs, int n, Slots slots_of, JobList<MacJobX>& JL, uint64_t* total,
-                              unsigned* bx) {
+                              unsigned* bx, bool split = false) {
     uint32_t widest = 1;
     *total = 0;
     JL.n = n;
@@ -743,9 +770,11 @@ cudaError_t mac_launch_common(MacJobX* jobs, int n, Slots slots_of, JobList<MacJ
         if (jobs[i].L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
         const uint32_t slots = slots_of(jobs[i]);
         if (slots == 0) return cudaErrorInvalidValue;
+        const uint32_t kc = split && jobs[i].kc ? jobs[i].kc : 1u;
+        if (kc != 1 && kc != 2 && kc != 4 && kc != 8) return cudaErrorInvalidValue;
         jobs[i].cta0 = (uint32_t)*total;
         JL.j[i] = jobs[i];
-        *total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * kRows * jobs[i].parts;
+        *total += (uint64_t)((slots + kMacThreads - 1) / kMacThreads) * (kRows / kc) * jobs[i].parts;
         widest = slots > widest ? slots : widest;
     }
     *bx = widest < (uint32_t)kMacThreads ? widest : kMacThreads;
@@ -767,22 +796,45 @@ cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st) {
+cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st, int* kernels) {
+    if (kernels) *kernels = 0;
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs) return cudaErrorInvalidValue;
     JobList<MacJobX> JL;
     uint64_t total;
     unsigned bx;
-    cudaError_t e = split ? mac_launch_common(jobs, n, [](const MacJobX& j) { return j.L ? 1u << (j.L - 1) : 0u; },
-                                              JL, &total, &bx)
-                          : mac_launch_common(jobs, n, [](const MacJobX& j) { return 1u << j.L; }, JL, &total, &bx);
-    if (e != cudaSuccess) return e;
-    if (!total) return cudaSuccess;
-    if (split)
-        mac_split_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, T.pc);
-    else
+    if (!split) {
+        cudaError_t e = mac_launch_common(jobs, n, [](const MacJobX& j) { return 1u << j.L; }, JL, &total, &bx);
+        if (e != cudaSuccess || !total) return e;
         mac_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, T.pc);
-    return cudaGetLastError();
+        if (kernels) *kernels = 1;
+        return cudaGetLastError();
+    }
+    // one launch per coordinates-per-thread value present
+    for (uint32_t kc : {1u, 2u, 4u, 8u}) {
+        MacJobX group[kMaxJobs];
+        int m = 0;
+        for (int i = 0; i < n; ++i) {
+            const uint32_t jkc = jobs[i].kc ? jobs[i].kc : 1u;
+            if (jkc != 1 && jkc != 2 && jkc != 4 && jkc != 8) return cudaErrorInvalidValue;
+            if (jkc == kc) group[m++] = jobs[i];
+        }
+        if (!m) continue;
+        cudaError_t e = mac_launch_common(group, m, [](const MacJobX& j) { return j.L ? 1u << (j.L - 1) : 0u; }, JL,
+                                          &total, &bx, true);
+        if (e != cudaSuccess) return e;
+        if (!total) continue;
+        switch (kc) {
+            case 1: mac_split_jobs_kernel<1><<<(unsigned)total, bx, 0, st>>>(JL, T.pc); break;
+            case 2: mac_split_jobs_kernel<2><<<(unsigned)total, bx, 0, st>>>(JL, T.pc); break;
+            case 4: mac_split_jobs_kernel<4><<<(unsigned)total, bx, 0, st>>>(JL, T.pc); break;
+            default: mac_split_jobs_kernel<8><<<(unsigned)total, bx, 0, st>>>(JL, T.pc); break;
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        if (kernels) ++*kernels;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st) {

@@ -173,10 +173,11 @@ int Plan::launch_all(Context* ctx, cudaStream_t st, std::string* err) {
         if ((rc = timed(name, bytes, macs, [&] {
                  for (size_t i = 0; i < v.size(); i += kMaxJobs) {
                      const int n = (int)std::min<size_t>(kMaxJobs, v.size() - i);
+                     int k = 1;
                      cudaError_t e = pass == 2 ? launch_mac_triple_jobs(T, v.data() + i, n, st)
-                                               : launch_mac_jobs(T, v.data() + i, n, pass == 1, st);
+                                               : launch_mac_jobs(T, v.data() + i, n, pass == 1, st, &k);
                      if (e != cudaSuccess) return (int)e;
-                     ++launches;
+                     launches += k;
                  }
                  return 0;
              })))
@@ -436,11 +437,13 @@ void ProofState::plan_stage(Plan& P) {
             P.ntt[L].push_back(NttJob{m_b_.as<uint4>(), mhat_.as<uint32_t>(), c, 0});
             P.ntt[L].push_back(NttJob{g_b_.as<uint4>(), ghat_.as<uint32_t>(), 8ull * c, 0});
         }
-        parts_ = ctx_->mac_parts(kTuneMacSplit, L, h, c);
+        const uint32_t kc = (uint32_t)ctx_->tuning(kTuneSplitCoords, L);
+        parts_ = ctx_->mac_parts_for(ctx_->tuning(kTuneMacSplit, L), h, c, kRows / kc);
         uint32_t* pchk = part;
         uint32_t* plp = part + (size_t)parts_ * kRows * s;
         uint32_t* prp = plp + (size_t)parts_ * kRows * h;
-        P.split.push_back(MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, c, parts_, 0, 0, L});
+        P.split.push_back(
+            MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, c, parts_, 0, 0, L, kc});
         P.finish[L].push_back(FinishJobX{pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain, kRows, 0});
         P.finish[L - 1].push_back(FinishJobX{plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL, kRows, 0});
         P.finish[L - 1].push_back(FinishJobX{prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR, kRows, 0});
