@@ -291,12 +291,15 @@ def cpu_baseline(wl, budget_s: float = 15.0, threads: int = 0, proofs=None):
 class StratifiedOracle:
     """The oracle's MiB/s on a workload of mixed depths, stratified by depth.
 
-    Every depth present is timed on full commit+prove runs of the workload's own
-    files, and the workload's rate is its bytes over the sum, per depth, of its
-    bytes of that depth at the rate measured there.  Depths up to 9 take seconds
-    and are re-sampled every step on the next file of that depth; deeper ones
-    (d = 10: tens of seconds, d = 11: minutes) are timed once, on the first file
-    of that depth, and reused."""
+    Every depth present is timed on a full commit+prove of one of the workload's
+    own files.  The oracle, like the reference, transforms every column of the
+    square witness, zero padding included, so a proof's CPU time depends on its
+    depth and not on how full the file is: the workload's time is the sum over
+    depths of its proofs of that depth times the seconds measured there, and its
+    rate its bytes over that time.  Depths up to 9 take seconds and are
+    re-sampled every step on the next file of that depth; deeper ones (d = 10:
+    tens of seconds, d = 11: minutes) are timed once, on the first file of that
+    depth, and reused."""
 
     def __init__(self, wl, threads):
         import oracle as O
@@ -328,19 +331,19 @@ class StratifiedOracle:
                     data, seed = files[0]
                     self.once[depth] = (len(data), self._time(data, seed))
                 n, secs = self.once[depth]
-            rate = n / MIB / secs
             per[depth] = {"files_in_workload": len(files), "workload_bytes": dbytes, "sampled_bytes": n,
-                          "seconds": round(secs, 3), "mib_s": rate}
-            proj_s += dbytes / MIB / rate
+                          "seconds_per_proof": round(secs, 3)}
+            proj_s += len(files) * secs
             sampled += dbytes
         value = sampled / MIB / proj_s
         skipped = [d for d in self.by_depth if d > max_full_depth]
         sample = (f"oracle restatement (per-product 2n-point NTT over 8 CRT primes + Garner CRT, commitment columns "
                   f"over {self.threads} threads), one full commit+prove per depth of the workload's own files "
                   f"(d <= {resample_depth}: the next file of that depth each step; deeper: the first, timed once); "
-                  "value = the workload's bytes / sum over depths of its bytes there at the measured rate; "
-                  "per depth: " + "; ".join(f"d{d}: {v['sampled_bytes']} B in {v['seconds']} s"
-                                            for d, v in per.items()))
+                  "value = the workload's bytes / sum over depths of (its proofs there x the measured seconds "
+                  "per proof); per depth: " + "; ".join(f"d{d}: {v['files_in_workload']} proofs, one of "
+                                                        f"{v['sampled_bytes']} B in {v['seconds_per_proof']} s"
+                                                        for d, v in per.items()))
         if skipped:
             sample += (f"; depths {skipped} ({total - sampled} of {total} bytes) not sampled in this bounded leg, "
                        "the value covers the rest of the workload")
@@ -495,6 +498,20 @@ def check_digests(entries, proofs, lengths, indices=None):
         checked += 1
         ok += hashlib.sha256(p).hexdigest() == e["proof_sha256"]
     return ok, checked
+
+
+def host_hash_rate(D, nbytes: int = 64 << 20, reps: int = 5):
+    """GB/s of the host BLAKE3 on one core (the keyed entry point hashes on the
+    calling thread; its chunks run in vector lanes), the transcript's hash."""
+    import ctypes
+    L = D.load()
+    data = bytes(range(256)) * (nbytes // 256)
+    out = ctypes.create_string_buffer(32)
+    L.damascus_blake3_keyed(b"\x07" * 32, data, len(data), out)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        L.damascus_blake3_keyed(b"\x07" * 32, data, len(data), out)
+    return reps * len(data) / (time.perf_counter() - t0) / 1e9
 
 
 def measure_batched(ctx, D, torch, args, rank, world, ranks):
@@ -899,6 +916,7 @@ def run_gpu(args, wl):
         eng.close()
         if wl["name"] == "serve" and not args.no_batched:
             line["batched"] = measure_batched(ctx, D, torch, args, rank, world, ranks)
+        line["host_blake3_gbs_per_core"] = host_hash_rate(D)
         line.update({"value": value, "ms_per_step": step_s * 1000.0,
                      "config": {"workload": wl["desc"], "requests": len(files), "total_bytes": total,
                                 "parallelism": f"replicas x{world}", "hbm_budget_bytes": SERVE_BUDGET,

@@ -60,7 +60,9 @@ def ring_sizes(knob: int) -> List[int]:
     return list(range(4, 13))
 
 
-DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1}  # the library's built-ins
+# the library's built-in values (the split's coordinates per thread: 4 from rings of 2^9 on); the autotuner
+# reads them from a context made without a table
+DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1}
 ENGINE_WAVES = "engine_waves"
 WAVE_CANDIDATES = [4, 8, 12, 16, 24, 32]
 DEFAULT_WAVES = 16
@@ -91,10 +93,11 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
             if knob == MAC_SPLIT:
                 entries += tune_split(ctx, L, count, reps, margin, log)
                 continue
+            default = ctx.tuning_get(knob, L)  # the library's built-in value
             times = {}
             for v in CANDIDATES[knob]:
                 times[v] = ctx.tuning_measure(knob, L, v, count, reps)
-            best = choose(times, DEFAULTS[knob], margin)
+            best = choose(times, default, margin)
             ctx.tuning_set(knob, L, best)
             entries.append({"knob": KNOB_NAMES[knob], "log_ring": L, "value": best, "count": count,
                             "ms": {str(k): round(t, 5) for k, t in times.items()}})
@@ -107,12 +110,13 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
 def tune_split(ctx, L: int, count: int, reps: int, margin: float, log=print) -> List[Dict]:
     """The split MAC's (coordinates per thread, blocks per SM) pair at ring 2^L:
     every pair timed, the built-in pair kept unless beaten as `choose` requires."""
+    default = (ctx.tuning_get(SPLIT_COORDS, L), ctx.tuning_get(MAC_SPLIT, L))  # the library's built-in pair
     times = {}
     for kc in CANDIDATES[SPLIT_COORDS]:
         ctx.tuning_set(SPLIT_COORDS, L, kc)
         for v in CANDIDATES[MAC_SPLIT]:
             times[(kc, v)] = ctx.tuning_measure(MAC_SPLIT, L, v, count, reps)
-    kc, v = choose(times, (DEFAULTS[SPLIT_COORDS], DEFAULTS[MAC_SPLIT]), margin)
+    kc, v = choose(times, default, margin)
     ctx.tuning_set(SPLIT_COORDS, L, kc)
     ctx.tuning_set(MAC_SPLIT, L, v)
     ms = {f"{a}x{b}": round(t, 5) for (a, b), t in times.items()}

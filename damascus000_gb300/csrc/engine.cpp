@@ -39,7 +39,7 @@ int Context::create(int device, uint64_t hbm_budget, Context** out, std::string*
     c->device_ = device;
     c->sm_count_ = prop.multiProcessorCount > 0 ? prop.multiProcessorCount : 152;
     for (int k = 0; k < kTuneKnobs; ++k)
-        for (int L = 0; L <= kLogMaxProverRing; ++L) c->tune_[k][L].store(kTuneDefault[k]);
+        for (int L = 0; L <= kLogMaxProverRing; ++L) c->tune_[k][L].store(tune_default(k, L));
     if ((e = cudaStreamCreateWithFlags(&c->stream_, cudaStreamNonBlocking)) != cudaSuccess) {
         *err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
         return kECuda;

@@ -60,11 +60,23 @@ inline void compress_lanes(LaneVec cv[8], const LaneVec m[16], const LaneVec& ct
 }
 
 // Message words i of kLanes 64-byte blocks that start `stride` bytes apart.
+// Four lanes: each lane's 16 words are four vectors (little-endian hosts: the
+// byte order of the words is the memory order), transposed in 4 x 4 tiles.
+static_assert(kLanes == 4, "the transpose below is for four lanes");
+static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "message words are loaded in memory order");
 inline void load_lanes(const uint8_t* p, size_t stride, LaneVec m[16]) {
-    alignas(64) uint32_t t[16][kLanes];
-    for (int l = 0; l < kLanes; ++l)
-        for (int i = 0; i < 16; ++i) t[i][l] = b3_load_le32(p + l * stride + 4 * i);
-    for (int i = 0; i < 16; ++i) std::memcpy(&m[i], t[i], sizeof(LaneVec));
+    typedef uint32_t Idx __attribute__((vector_size(4 * kLanes)));
+    const Idx lo = {0, 4, 1, 5}, hi = {2, 6, 3, 7}, first = {0, 1, 4, 5}, second = {2, 3, 6, 7};
+    for (int j = 0; j < 4; ++j) {
+        LaneVec q[4];
+        for (int l = 0; l < 4; ++l) std::memcpy(&q[l], p + l * stride + 16 * j, 16);
+        const LaneVec t0 = __builtin_shuffle(q[0], q[1], lo), t1 = __builtin_shuffle(q[0], q[1], hi);
+        const LaneVec t2 = __builtin_shuffle(q[2], q[3], lo), t3 = __builtin_shuffle(q[2], q[3], hi);
+        m[4 * j + 0] = __builtin_shuffle(t0, t2, first);
+        m[4 * j + 1] = __builtin_shuffle(t0, t2, second);
+        m[4 * j + 2] = __builtin_shuffle(t1, t3, first);
+        m[4 * j + 3] = __builtin_shuffle(t1, t3, second);
+    }
 }
 
 inline void store_lanes(const LaneVec cv[8], uint32_t* out) {  // out: kLanes x 8 words
