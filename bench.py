@@ -866,8 +866,10 @@ def run_gpu(args, wl):
         ctx.set_profiling(True)
         ctx.reset_stats()
         with D.Engine(ctx, max_waves=1) as eng1:
+            t_serial = time.perf_counter()
             serial = [eng1.wait(t)[0] for t in
                       [eng1.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]]
+            serial_s = time.perf_counter() - t_serial
         torch.cuda.synchronize()
         stats = {k: ctx.kernel_stat(k) for k in KERNELS}
         ctx.set_profiling(False)
@@ -937,6 +939,10 @@ def run_gpu(args, wl):
                      "e2e": {"value": world * total / MIB / e2e_s, "unit": UNIT, "h2d_bytes_per_step": total,
                              "d2h_bytes_per_step": d2h},
                      "plain_mib_s": plain, "serving_vs_plain": value / plain,
+                     "single_wave_replay": {"mib_s": total / MIB / serial_s,
+                                            "kernel_ms": sum(v[1] for v in stats.values() if v),
+                                            "note": "one stage wave in flight, per-kernel events on: the kernels "
+                                                    "one after another, host stages not overlapped"},
                      "gpu_launches": int(st1["launches"] - st0["launches"]),
                      "roofline": roofline(stats, "one more replay of the workload with a single stage wave in "
                                                  "flight: launches serialised on one stream, per-kernel CUDA "

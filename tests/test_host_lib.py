@@ -51,8 +51,11 @@ def test_from_le_bytes_mod_order(oracle_lib, n):
         int.from_bytes(b, "little") % Q
 
 
-@pytest.mark.parametrize("n", [0, 1, 63, 64, 65, 1023, 1024, 1025, 2048, 3073, 16385, 70000, 1 << 20])
+@pytest.mark.parametrize("n", [0, 1, 63, 64, 65, 1023, 1024, 1025, 2048, 3073, 4096, 4097, 5 * 1024, 8 * 1024 - 1,
+                               8 * 1024, 9 * 1024 + 3, 16385, 33 * 1024, 70000, 1 << 20, (1 << 20) + 4 * 1024 + 1])
 def test_host_blake3_matches_oracle(oracle_lib, n):
+    """Lengths around the host hash's lane groups (four whole chunks at a time),
+    its parent levels in lanes (four pairs at a time) and the parallel split."""
     data = bytes((i * 131 + n) & 0xFF for i in range(n))
     key = bytes(range(32))
     assert D.blake3(data) == oracle_lib.blake3(data)
