@@ -411,7 +411,9 @@ def run_reference(args, wl):
 # same launches' algorithmic bytes).  Used to state `traffic` per launch of this
 # run; the capture, not this run, measured it.
 DRAM_PER_ALGO_BYTE = {
-    "ntt_fwd": (0.95, "ncu of the transform, per ring size (profiles/ntt_fwd_traffic_by_ring.txt)"),
+    "ntt_fwd": (0.93, "ncu of the transform at ring 2^11, the ring most of its bytes run at (0.90-0.95; rings "
+                      "of 2^7-2^9 stay in L2 at 0.31-0.34: an upper estimate for a mixed workload), "
+                      "profiles/ntt_fwd_traffic_by_ring.txt"),
 }
 # The transform is bound by the integer multiplier, not by HBM.  Its multiplies,
 # counted from the kernel's code (dm_ntt.cuh, dm_field.cuh): a butterfly is one
