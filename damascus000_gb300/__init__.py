@@ -32,9 +32,10 @@ DEFAULT_MEMORY_LIMIT_BYTES = 512 * 1024 * 1024
 OK = 0
 EINVAL, ENOMEM_BUDGET, ECUDA, ETIMEOUT, EVERIFY, EINVARIANT, ESTATE, ESIZE, EDESERIALIZE, EUNSUPPORTED = \
     -1, -2, -3, -4, -5, -6, -7, -8, -9, -10
+ECANCELED = -11
 _CODE_NAMES = {EINVAL: "EINVAL", ENOMEM_BUDGET: "ENOMEM_BUDGET", ECUDA: "ECUDA", ETIMEOUT: "ETIMEOUT",
                EVERIFY: "EVERIFY", EINVARIANT: "EINVARIANT", ESTATE: "ESTATE", ESIZE: "ESIZE",
-               EDESERIALIZE: "EDESERIALIZE", EUNSUPPORTED: "EUNSUPPORTED"}
+               EDESERIALIZE: "EDESERIALIZE", EUNSUPPORTED: "EUNSUPPORTED", ECANCELED: "ECANCELED"}
 
 #: every symbol include/damascus.h declares
 EXPORTED_SYMBOLS = (
@@ -59,6 +60,8 @@ EXPORTED_SYMBOLS = (
     "damascus_engine_create", "damascus_engine_destroy", "damascus_engine_submit", "damascus_engine_submit_device",
     "damascus_engine_poll",
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
+    "damascus_engine_wait_timeout", "damascus_engine_cancel", "damascus_engine_set_request_timeout",
+    "damascus_engine_health",
     "damascus_tuning_set", "damascus_tuning_get", "damascus_tuning_measure",
     "damascus_verify_service_create", "damascus_verify_service_destroy", "damascus_verify_service_submit",
     "damascus_verify_service_poll", "damascus_verify_service_wait", "damascus_verify_service_drain",
@@ -166,6 +169,10 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_poll", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_wait", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_take", i32, vp, u64, vp, sz)
+    sig("damascus_engine_wait_timeout", i32, vp, u64, ctypes.c_double, P(sz), P(ctypes.c_double))
+    sig("damascus_engine_cancel", i32, vp, u64)
+    sig("damascus_engine_set_request_timeout", i32, vp, ctypes.c_double)
+    sig("damascus_engine_health", i32, vp, P(u64), P(ctypes.c_double))
     sig("damascus_engine_drain", i32, vp)
     sig("damascus_engine_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64))
     sig("damascus_engine_profile", i32, vp, P(ctypes.c_double), P(ctypes.c_double))
@@ -651,11 +658,17 @@ class Engine:
                                                          epoch_seed, ctypes.byref(t)), "engine submit")
         return t.value
 
-    def _result(self, ticket: int, block: bool):
+    def _result(self, ticket: int, block: bool, timeout_ms: Optional[float] = None):
         n = ctypes.c_size_t()
         lat = ctypes.c_double()
-        fn = self._lib.damascus_engine_wait if block else self._lib.damascus_engine_poll
-        rc = fn(self._h, ticket, ctypes.byref(n), ctypes.byref(lat))
+        if timeout_ms is not None:
+            rc = self._lib.damascus_engine_wait_timeout(self._h, ticket, float(timeout_ms), ctypes.byref(n),
+                                                        ctypes.byref(lat))
+            if rc == ETIMEOUT:
+                return None
+        else:
+            fn = self._lib.damascus_engine_wait if block else self._lib.damascus_engine_poll
+            rc = fn(self._h, ticket, ctypes.byref(n), ctypes.byref(lat))
         if rc == 0:
             return None
         if rc < 0:
@@ -664,9 +677,27 @@ class Engine:
         self._ctx.check(self._lib.damascus_engine_take(self._h, ticket, buf, n.value), "engine take")
         return buf.raw, lat.value
 
-    def wait(self, ticket: int):
-        """(proof bytes, latency ms) once the request finished."""
-        return self._result(ticket, True)
+    def wait(self, ticket: int, timeout_ms: Optional[float] = None):
+        """(proof bytes, latency ms) once the request finished; with timeout_ms,
+        None when it has not finished by then (it keeps running)."""
+        return self._result(ticket, True, timeout_ms)
+
+    def cancel(self, ticket: int) -> None:
+        """Ends the request early (queued: at once; admitted: at its next stage
+        boundary); its wait then raises ECANCELED."""
+        self._ctx.check(self._lib.damascus_engine_cancel(self._h, ticket), "engine cancel")
+
+    def set_request_timeout(self, timeout_ms: float) -> None:
+        """Requests submitted from now on fail with ETIMEOUT when unfinished after
+        timeout_ms (0: no limit)."""
+        self._ctx.check(self._lib.damascus_engine_set_request_timeout(self._h, float(timeout_ms)),
+                        "engine set_request_timeout")
+
+    def health(self) -> dict:
+        """Unfinished requests and milliseconds since any stage finished."""
+        u, ms = ctypes.c_uint64(), ctypes.c_double()
+        self._ctx.check(self._lib.damascus_engine_health(self._h, ctypes.byref(u), ctypes.byref(ms)), "engine health")
+        return {"unfinished": u.value, "ms_since_progress": ms.value}
 
     def poll(self, ticket: int):
         """(proof bytes, latency ms), or None while running."""

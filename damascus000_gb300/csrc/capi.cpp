@@ -751,6 +751,51 @@ int damascus_engine_wait(damascus_engine* e, uint64_t ticket, size_t* proof_len,
     return engine_result(e, ticket, true, proof_len, latency_ms);
 }
 
+int damascus_engine_wait_timeout(damascus_engine* e, uint64_t ticket, double timeout_ms, size_t* proof_len,
+                                 double* latency_ms) {
+    if (!e) return DAMASCUS_EINVAL;
+    bool known;
+    {
+        std::lock_guard<std::mutex> g(e->mu);
+        known = e->status.count(ticket) != 0;
+    }
+    if (known) return engine_result(e, ticket, false, proof_len, latency_ms);  // finished earlier
+    std::vector<uint8_t> proof;
+    double lat = 0;
+    std::string err;
+    const int rc = e->e->wait_for(ticket, timeout_ms, &proof, &lat, &err);
+    if (rc == kETimeout || rc == 0) return rc == 0 ? 0 : DAMASCUS_ETIMEOUT;
+    if (rc < 0 && rc == DAMASCUS_EINVAL && err.empty()) return rc;
+    std::lock_guard<std::mutex> g(e->mu);
+    if (rc < 0) e->owner->ctx->set_error(err);
+    e->status[ticket] = {rc, lat};
+    if (proof_len) *proof_len = proof.size();
+    if (latency_ms) *latency_ms = lat;
+    e->results[ticket] = std::move(proof);
+    return rc;
+}
+
+int damascus_engine_cancel(damascus_engine* e, uint64_t ticket) {
+    if (!e) return DAMASCUS_EINVAL;
+    {
+        std::lock_guard<std::mutex> g(e->mu);
+        if (e->status.count(ticket)) return DAMASCUS_ESTATE;  // finished, result not taken yet
+    }
+    return e->e->cancel(ticket);
+}
+
+int damascus_engine_set_request_timeout(damascus_engine* e, double timeout_ms) {
+    if (!e || timeout_ms < 0) return DAMASCUS_EINVAL;
+    e->e->set_request_timeout(timeout_ms);
+    return DAMASCUS_OK;
+}
+
+int damascus_engine_health(damascus_engine* e, uint64_t* unfinished, double* ms_since_progress) {
+    if (!e) return DAMASCUS_EINVAL;
+    e->e->health(unfinished, ms_since_progress);
+    return DAMASCUS_OK;
+}
+
 int damascus_engine_take(damascus_engine* e, uint64_t ticket, uint8_t* proof_out, size_t cap) {
     if (!e) return DAMASCUS_EINVAL;
     std::lock_guard<std::mutex> g(e->mu);

@@ -31,6 +31,7 @@ enum Status : int {
     kESize = -8,        // output buffer too small
     kEDeserialize = -9,
     kEUnsupported = -10,
+    kECanceled = -11,   // the caller cancelled the request
 };
 
 struct KernelStat {

@@ -1,5 +1,6 @@
 #include "serve.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
@@ -23,6 +24,9 @@ struct Engine::Request {
     int err_code = 0;
     uint64_t footprint = 0;
     Clock::time_point t_submit, t_done;
+    bool cancel = false;          // the caller cancelled it
+    bool has_deadline = false;    // the engine's request timeout applies
+    Clock::time_point deadline{};
 };
 
 struct Engine::Wave {
@@ -126,6 +130,10 @@ int Engine::submit(const uint8_t* file, uint64_t len, const uint8_t seed[32], co
     r->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> g(mu_);
+        if (request_timeout_ms_ > 0) {
+            r->has_deadline = true;
+            r->deadline = r->t_submit + std::chrono::microseconds((int64_t)(request_timeout_ms_ * 1000.0));
+        }
         r->ticket = next_ticket_++;
         *ticket = r->ticket;
         queued_.push_back(r.get());
@@ -142,6 +150,7 @@ void CUDART_CB Engine::on_wave_done(void* arg) {
     {
         std::lock_guard<std::mutex> g(e->mu_);
         for (Request* r : w->reqs) e->host_q_.push_back(r);
+        e->last_progress_ = Clock::now();
         if (--e->inflight_waves_ == 0) e->idle_since_ = Clock::now();
         e->wave_stream_busy_[w->stream_idx] = false;
     }
@@ -162,6 +171,15 @@ void Engine::scheduler() {
         // Admission in arrival order while the HBM budget holds the request's footprint.
         while (!queued_.empty()) {
             Request* r = queued_.front();
+            if (const int code = abort_code(r, Clock::now())) {  // cancelled or expired while queued
+                queued_.pop_front();
+                r->err_code = code;
+                r->err = code == kECanceled ? "request cancelled" : "request timed out while queued";
+                lk.unlock();
+                finish_request(r);
+                lk.lock();
+                continue;
+            }
             // requests come before cached generator families: drop unreferenced
             // ones when a request does not fit
             if (ctx_->reserved() + r->footprint > ctx_->budget() && ctx_->prover_cache()) {
@@ -203,6 +221,29 @@ void Engine::scheduler() {
         if (ready_.empty() || inflight_waves_ >= max_waves_) continue;
         std::vector<Request*> rest;
         rest.swap(ready_);
+        {
+            // requests cancelled or expired between stages end here: their last
+            // stage has completed on the device
+            std::vector<Request*> ended;
+            const Clock::time_point now = Clock::now();
+            size_t k = 0;
+            for (Request* r : rest) {
+                if (const int code = abort_code(r, now)) {
+                    r->err_code = code;
+                    r->err = code == kECanceled ? "request cancelled" : "request timed out";
+                    ended.push_back(r);
+                } else {
+                    rest[k++] = r;
+                }
+            }
+            rest.resize(k);
+            if (!ended.empty()) {
+                lk.unlock();
+                for (Request* r : ended) finish_request(r);
+                lk.lock();
+            }
+            if (rest.empty()) continue;
+        }
         std::vector<Request*> deep;
         if (priority_depth_ && inflight_waves_ + 1 < max_waves_) {
             // the deepest requests' stages in a wave of their own on a high-priority stream
@@ -270,6 +311,14 @@ void Engine::worker() {
             if (host_q_.empty()) return;
             r = host_q_.front();
             host_q_.pop_front();
+            if (const int code = abort_code(r, Clock::now())) {  // its stage landed: end it here
+                r->err_code = code;
+                r->err = code == kECanceled ? "request cancelled" : "request timed out";
+            }
+        }
+        if (r->err_code) {
+            finish_request(r);
+            continue;
         }
         const Clock::time_point t0 = Clock::now();
         const int rc = r->ps->complete_stage();
@@ -307,11 +356,14 @@ void Engine::finish_request(Request* r) {
         if (r->state == Request::Active) --active_;
         r->state = ok ? Request::Done : Request::Failed;
         admit_blocked_ = false;
+        last_progress_ = Clock::now();
         if (ok) {
             stats_.completed++;
             stats_.bytes_done += r->len;
         } else {
             stats_.failed++;
+            if (r->err_code == kECanceled) stats_.cancelled++;
+            if (r->err_code == kETimeout) stats_.timed_out++;
         }
     }
     done_cv_.notify_all();
@@ -341,6 +393,66 @@ int Engine::wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_m
         done_cv_.wait(lk, [&] { return r->state == Request::Done || r->state == Request::Failed; });
     }
     return poll(ticket, proof, latency_ms, err);
+}
+
+int Engine::wait_for(uint64_t ticket, double timeout_ms, std::vector<uint8_t>* proof, double* latency_ms,
+                     std::string* err) {
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        auto it = all_.find(ticket);
+        if (it == all_.end()) return kEInval;
+        Request* r = it->second.get();
+        const bool done = done_cv_.wait_for(
+            lk, std::chrono::microseconds((int64_t)(timeout_ms > 0 ? timeout_ms * 1000.0 : 0)),
+            [&] { return r->state == Request::Done || r->state == Request::Failed; });
+        if (!done) return kETimeout;
+    }
+    return poll(ticket, proof, latency_ms, err);
+}
+
+int Engine::abort_code(const Request* r, Clock::time_point now) const {
+    if (r->cancel) return kECanceled;
+    if (r->has_deadline && now >= r->deadline) return kETimeout;
+    return 0;
+}
+
+int Engine::cancel(uint64_t ticket) {
+    Request* now = nullptr;  // a queued request ends here; an admitted one at its next stage boundary
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        auto it = all_.find(ticket);
+        if (it == all_.end()) return kEInval;
+        Request* r = it->second.get();
+        if (r->state == Request::Done || r->state == Request::Failed) return kEState;
+        r->cancel = true;
+        if (r->state == Request::Queued) {
+            auto q = std::find(queued_.begin(), queued_.end(), r);
+            if (q != queued_.end()) {  // not being admitted right now: nothing of it is on the device
+                queued_.erase(q);
+                r->err_code = kECanceled;
+                r->err = "request cancelled";
+                now = r;
+            }
+        }
+    }
+    if (now) finish_request(now);
+    sched_cv_.notify_one();
+    return kOk;
+}
+
+void Engine::set_request_timeout(double timeout_ms) {
+    std::lock_guard<std::mutex> g(mu_);
+    request_timeout_ms_ = timeout_ms > 0 ? timeout_ms : 0;
+}
+
+void Engine::health(uint64_t* unfinished, double* ms_since_progress) {
+    std::lock_guard<std::mutex> g(mu_);
+    const uint64_t open = stats_.submitted - stats_.completed - stats_.failed;
+    if (unfinished) *unfinished = open;
+    if (ms_since_progress) {
+        const Clock::time_point from = last_progress_ > Clock::time_point{} ? last_progress_ : Clock::now();
+        *ms_since_progress = open ? std::chrono::duration<double, std::milli>(Clock::now() - from).count() : 0.0;
+    }
 }
 
 void Engine::drain() {

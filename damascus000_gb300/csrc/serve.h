@@ -34,6 +34,7 @@ struct EngineStats {
     uint64_t peak_reserved = 0;
     double host_stage_ms = 0;  // summed time of the host part of stages (all workers)
     double gpu_idle_ms = 0;    // wall time with no wave in flight while requests were admitted
+    uint64_t cancelled = 0, timed_out = 0;
 };
 
 class Engine {
@@ -53,6 +54,24 @@ class Engine {
     int poll(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err);
     // Blocks until the ticket finishes; same results as poll.
     int wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err);
+    // wait with a limit: kETimeout when the request has not finished within
+    // timeout_ms (it keeps running; the ticket stays valid).
+    int wait_for(uint64_t ticket, double timeout_ms, std::vector<uint8_t>* proof, double* latency_ms,
+                 std::string* err);
+    // Ends a request early: a queued one at once, an admitted one at its next
+    // stage boundary (a stage already on the GPU completes first, so no kernel is
+    // interrupted and no buffer freed under it).  It then finishes with
+    // kECanceled and releases its memory.  kEState if it had already finished.
+    int cancel(uint64_t ticket);
+    // Requests submitted from now on fail with kETimeout when they are still
+    // unfinished timeout_ms after submission (checked at admission and at stage
+    // boundaries, as cancel is).  0: no limit.
+    void set_request_timeout(double timeout_ms);
+    // Watchdog reading: unfinished requests and the milliseconds since any
+    // stage finished (0 when nothing is unfinished).  The GPU kernels wait on
+    // nothing, so a growing age with requests unfinished means the host side
+    // (or the device) stopped making progress.
+    void health(uint64_t* unfinished, double* ms_since_progress);
     void drain();  // blocks until every submitted request has finished
     EngineStats stats();
 
@@ -69,6 +88,8 @@ class Engine {
     void scheduler();
     void worker();
     void finish_request(Request* r);
+    // kECanceled / kETimeout when r must end at this boundary, else 0 (mu_ held).
+    int abort_code(const Request* r, std::chrono::steady_clock::time_point now) const;
 
     Context* ctx_;
     int max_waves_;
@@ -95,6 +116,8 @@ class Engine {
     std::chrono::steady_clock::time_point idle_since_{}, active_since_{};
     bool admit_blocked_ = false;  // the queue head waits for memory; cleared when a request finishes
     bool stop_ = false;
+    double request_timeout_ms_ = 0;
+    std::chrono::steady_clock::time_point last_progress_{};
     std::string init_error_;
     EngineStats stats_;
     std::thread sched_thread_;

@@ -41,6 +41,7 @@ extern "C" {
 #define DAMASCUS_ESIZE (-8)
 #define DAMASCUS_EDESERIALIZE (-9)
 #define DAMASCUS_EUNSUPPORTED (-10)
+#define DAMASCUS_ECANCELED (-11)
 
 typedef struct damascus_ctx damascus_ctx;
 typedef struct damascus_prover damascus_prover;
@@ -203,6 +204,26 @@ int damascus_engine_submit_device(damascus_engine* e, const void* d_file, size_t
 int damascus_engine_poll(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms);
 /* Blocks until the ticket finishes; same results as poll. */
 int damascus_engine_wait(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms);
+/* wait with a limit: DAMASCUS_ETIMEOUT when the request has not finished within
+ * timeout_ms; it keeps running and the ticket stays valid. */
+int damascus_engine_wait_timeout(damascus_engine* e, uint64_t ticket, double timeout_ms, size_t* proof_len,
+                                 double* latency_ms);
+/* Ends a request early.  A queued request ends at once; an admitted one at its
+ * next stage boundary: a stage already on the GPU completes first, so no kernel
+ * is interrupted.  The request then finishes with DAMASCUS_ECANCELED (from poll
+ * or wait) and releases its memory; the others are undisturbed.
+ * DAMASCUS_ESTATE when it had already finished, DAMASCUS_EINVAL for an unknown
+ * ticket. */
+int damascus_engine_cancel(damascus_engine* e, uint64_t ticket);
+/* Requests submitted from now on fail with DAMASCUS_ETIMEOUT when still
+ * unfinished timeout_ms after their submission (checked at admission and at
+ * stage boundaries, as cancel is).  0 removes the limit. */
+int damascus_engine_set_request_timeout(damascus_engine* e, double timeout_ms);
+/* Watchdog reading: unfinished requests and the milliseconds since any stage
+ * (or request) finished, 0 while nothing is unfinished.  No kernel of the engine
+ * waits on a flag, so an age that keeps growing with requests unfinished points
+ * at the host side or a stalled device; the caller decides what to do. */
+int damascus_engine_health(damascus_engine* e, uint64_t* unfinished, double* ms_since_progress);
 /* Copies a finished proof out and forgets it (DAMASCUS_ESIZE keeps it). */
 int damascus_engine_take(damascus_engine* e, uint64_t ticket, uint8_t* proof_out, size_t cap);
 int damascus_engine_drain(damascus_engine* e);

@@ -19,6 +19,7 @@ pub const DAMASCUS_ESTATE: c_int = -7;
 pub const DAMASCUS_ESIZE: c_int = -8;
 pub const DAMASCUS_EDESERIALIZE: c_int = -9;
 pub const DAMASCUS_EUNSUPPORTED: c_int = -10;
+pub const DAMASCUS_ECANCELED: c_int = -11;
 
 pub const DAMASCUS_TUNE_NTT_GROUP: c_int = 0;
 pub const DAMASCUS_TUNE_MAC_TRIPLE: c_int = 1;
@@ -103,6 +104,10 @@ extern "C" {
     pub fn damascus_engine_submit_device(e: *mut Engine, d_file: *const c_void, len: usize, seed_generators: *const u8, epoch_seed: *const u8, ticket: *mut u64) -> c_int;
     pub fn damascus_engine_poll(e: *mut Engine, ticket: u64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
     pub fn damascus_engine_wait(e: *mut Engine, ticket: u64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
+    pub fn damascus_engine_wait_timeout(e: *mut Engine, ticket: u64, timeout_ms: f64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
+    pub fn damascus_engine_cancel(e: *mut Engine, ticket: u64) -> c_int;
+    pub fn damascus_engine_set_request_timeout(e: *mut Engine, timeout_ms: f64) -> c_int;
+    pub fn damascus_engine_health(e: *mut Engine, unfinished: *mut u64, ms_since_progress: *mut f64) -> c_int;
     pub fn damascus_engine_take(e: *mut Engine, ticket: u64, proof_out: *mut u8, cap: usize) -> c_int;
     pub fn damascus_engine_drain(e: *mut Engine) -> c_int;
     pub fn damascus_engine_stats(e: *mut Engine, completed: *mut u64, failed: *mut u64, waves: *mut u64, launches: *mut u64, peak_reserved_bytes: *mut u64) -> c_int;

@@ -181,3 +181,60 @@ def test_engine_priority_split_keeps_proofs(ctx, monkeypatch, priority_depth):
     assert st["failed"] == 0
     for (d, s), p in zip(files, proofs):
         assert p == ctx.prove(d, s, EPOCH), len(d)
+
+
+def test_engine_cancel_queued_and_admitted_requests(ctx):
+    """Two 16 MiB requests under a budget that admits one: the second waits in the
+    queue and is cancelled there, the first is cancelled between two of its
+    stages.  Both end with ECANCELED and leave no memory behind, and the small
+    request queued behind them finishes with the plain path's bytes."""
+    a = synth.random_file(95, 16 << 20, 0)
+    b = synth.random_file(95, 16 << 20, 1)
+    small = _files(96, [60_000])[0]
+    budget = D.prover_footprint(16 << 20) + D.prover_footprint(60_000) + (64 << 20)
+    c = D.Context(0, hbm_budget_bytes=budget, tuning=None)
+    try:
+        with D.Engine(c) as eng:
+            ta = eng.submit(*a, EPOCH)
+            for _ in range(200000):  # until the first request's first stage is on the GPU
+                if eng.stats()["waves"] >= 1:
+                    break
+            tb = eng.submit(*b, EPOCH)  # cannot be admitted beside the first
+            ts = eng.submit(*small, EPOCH)  # behind it in arrival order
+            eng.cancel(tb)
+            eng.cancel(ta)
+            for t in (ta, tb):
+                with pytest.raises(D.DamascusError) as e:
+                    eng.wait(t)
+                assert e.value.code == D.ECANCELED
+            proof = eng.wait(ts)[0]
+            with pytest.raises(D.DamascusError) as e:
+                eng.cancel(ts)  # already finished
+            assert e.value.code == D.ESTATE
+            assert eng.health()["unfinished"] == 0
+        assert c.reserved == 0
+    finally:
+        c.close()
+    assert proof == ctx.prove(*small, EPOCH)
+
+
+def test_engine_request_timeout_and_bounded_wait(ctx):
+    big = synth.random_file(97, 16 << 20, 0)
+    small = _files(98, [80_000])[0]
+    with D.Engine(ctx) as eng:
+        eng.set_request_timeout(0.5)  # a 16 MiB proof takes milliseconds
+        t = eng.submit(*big, EPOCH)
+        with pytest.raises(D.DamascusError) as e:
+            eng.wait(t)
+        assert e.value.code == D.ETIMEOUT
+        eng.set_request_timeout(0)
+        t = eng.submit(*big, EPOCH)
+        assert eng.wait(t, timeout_ms=0.01) is None  # still running: the ticket stays valid
+        h = eng.health()
+        assert h["unfinished"] >= 1 and h["ms_since_progress"] >= 0.0
+        proof = eng.wait(t)[0]
+        assert eng.wait(eng.submit(*small, EPOCH), timeout_ms=60_000)[0] == ctx.prove(*small, EPOCH)
+        assert eng.health() == {"unfinished": 0, "ms_since_progress": 0.0}
+        st = eng.stats()
+    assert proof == ctx.prove(*big, EPOCH)
+    assert st["failed"] == 1
