@@ -13,6 +13,8 @@ writes a table that `apply()` loads into a context:
 * `SPLIT_COORDS` — commitment coordinates per thread of the split MAC (1, 2, 4
   or 8: each witness slot pair loaded once for that many generator rows, at the
   cost of registers).  It is tuned jointly with `MAC_SPLIT`: every pair is timed;
+* `TRIPLE_COORDS` — the same for the triple MAC (1, 2 or 4), tuned jointly with
+  `MAC_TRIPLE`;
 * `engine_waves` — stage waves the serving engine keeps in flight (one stream
   each), timed end to end on a replay of a serving-stream mix; `Engine(ctx)`
   takes it when no count is given.
@@ -29,15 +31,16 @@ import time
 from pathlib import Path
 from typing import Dict, List, Optional
 
-NTT_GROUP, MAC_TRIPLE, MAC_SPLIT, MAC_PLAIN, SPLIT_COORDS = 0, 1, 2, 3, 4
+NTT_GROUP, MAC_TRIPLE, MAC_SPLIT, MAC_PLAIN, SPLIT_COORDS, TRIPLE_COORDS = 0, 1, 2, 3, 4, 5
 KNOB_NAMES = {NTT_GROUP: "ntt_group", MAC_TRIPLE: "mac_triple", MAC_SPLIT: "mac_split", MAC_PLAIN: "mac_plain",
-              SPLIT_COORDS: "split_coords"}
+              SPLIT_COORDS: "split_coords", TRIPLE_COORDS: "triple_coords"}
 CANDIDATES = {
     NTT_GROUP: [32, 64],
     MAC_TRIPLE: [2, 4, 8, 12, 16, 24],
     MAC_SPLIT: [2, 4, 8, 12, 16, 24],
     MAC_PLAIN: [2, 4, 8, 16],
     SPLIT_COORDS: [1, 2, 4, 8],
+    TRIPLE_COORDS: [1, 2, 4],
 }
 DEFAULT_TABLE = Path(__file__).resolve().parent / "tuning_gb300.json"
 
@@ -62,7 +65,7 @@ def ring_sizes(knob: int) -> List[int]:
 
 # the library's built-in values (the split's coordinates per thread: 4 from rings of 2^9 on); the autotuner
 # reads them from a context made without a table
-DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1}
+DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1, TRIPLE_COORDS: 1}
 ENGINE_WAVES = "engine_waves"
 WAVE_CANDIDATES = [4, 8, 12, 16, 24, 32]
 DEFAULT_WAVES = 16
@@ -84,14 +87,14 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
     """Measures every candidate and sets the chosen value on `ctx`; returns the table."""
     entries = []
     for knob in knobs if knobs is not None else list(CANDIDATES):
-        if knob == SPLIT_COORDS:
-            continue  # tuned with MAC_SPLIT
+        if knob in (SPLIT_COORDS, TRIPLE_COORDS):
+            continue  # tuned with MAC_SPLIT / MAC_TRIPLE
         for L in ring_sizes(knob):
             if L > max_L:
                 continue
             count = work_size(knob, L)
-            if knob == MAC_SPLIT:
-                entries += tune_split(ctx, L, count, reps, margin, log)
+            if knob in (MAC_SPLIT, MAC_TRIPLE):
+                entries += tune_coords(ctx, knob, L, count, reps, margin, log)
                 continue
             default = ctx.tuning_get(knob, L)  # the library's built-in value
             times = {}
@@ -107,22 +110,25 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
             "margin": margin, "min_gain_ms": 0.001, "entries": entries}
 
 
-def tune_split(ctx, L: int, count: int, reps: int, margin: float, log=print) -> List[Dict]:
-    """The split MAC's (coordinates per thread, blocks per SM) pair at ring 2^L:
-    every pair timed, the built-in pair kept unless beaten as `choose` requires."""
-    default = (ctx.tuning_get(SPLIT_COORDS, L), ctx.tuning_get(MAC_SPLIT, L))  # the library's built-in pair
+def tune_coords(ctx, knob: int, L: int, count: int, reps: int, margin: float, log=print) -> List[Dict]:
+    """A MAC's (coordinates per thread, blocks per SM) pair at ring 2^L (knob is
+    MAC_SPLIT or MAC_TRIPLE): every pair timed, the built-in pair kept unless
+    beaten as `choose` requires."""
+    coords = SPLIT_COORDS if knob == MAC_SPLIT else TRIPLE_COORDS
+    default = (ctx.tuning_get(coords, L), ctx.tuning_get(knob, L))  # the library's built-in pair
     times = {}
-    for kc in CANDIDATES[SPLIT_COORDS]:
-        ctx.tuning_set(SPLIT_COORDS, L, kc)
-        for v in CANDIDATES[MAC_SPLIT]:
-            times[(kc, v)] = ctx.tuning_measure(MAC_SPLIT, L, v, count, reps)
+    for kc in CANDIDATES[coords]:
+        ctx.tuning_set(coords, L, kc)
+        for v in CANDIDATES[knob]:
+            times[(kc, v)] = ctx.tuning_measure(knob, L, v, count, reps)
     kc, v = choose(times, default, margin)
-    ctx.tuning_set(SPLIT_COORDS, L, kc)
-    ctx.tuning_set(MAC_SPLIT, L, v)
+    ctx.tuning_set(coords, L, kc)
+    ctx.tuning_set(knob, L, v)
     ms = {f"{a}x{b}": round(t, 5) for (a, b), t in times.items()}
-    log(f"split      L={L:2d} count={count:6d} best={kc}x{v} " + " ".join(f"{k}:{t:.4f}" for k, t in ms.items()))
-    return [{"knob": KNOB_NAMES[MAC_SPLIT], "log_ring": L, "value": v, "count": count, "ms": ms},
-            {"knob": KNOB_NAMES[SPLIT_COORDS], "log_ring": L, "value": kc, "count": count}]
+    log(f"{KNOB_NAMES[knob]:10s} L={L:2d} count={count:6d} best={kc}x{v} "
+        + " ".join(f"{k}:{t:.4f}" for k, t in ms.items()))
+    return [{"knob": KNOB_NAMES[knob], "log_ring": L, "value": v, "count": count, "ms": ms},
+            {"knob": KNOB_NAMES[coords], "log_ring": L, "value": kc, "count": count}]
 
 
 def tune_waves(ctx, requests: int = 48, reps: int = 3, margin: float = 0.03, log=print) -> Dict:

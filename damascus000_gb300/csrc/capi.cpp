@@ -581,9 +581,10 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
         return DAMASCUS_EINVAL;
     const uint32_t L = log_ring;
     const uint64_t s = 1ull << L;
-    const bool bad = knob == kTuneNttGroup      ? (L < 4 || (value != 32 && value != 64))
-                     : knob == kTuneSplitCoords ? (L < 1 || (value != 1 && value != 2 && value != 4 && value != 8))
-                                                : (knob <= 0 || knob >= kTuneKnobs || L < 1 || value < 1 || value > 32);
+    const bool bad = knob == kTuneNttGroup       ? (L < 4 || (value != 32 && value != 64))
+                     : knob == kTuneSplitCoords  ? (L < 1 || (value != 1 && value != 2 && value != 4 && value != 8))
+                     : knob == kTuneTripleCoords ? (L < 1 || (value != 1 && value != 2 && value != 4))
+                                                 : (knob <= 0 || knob >= kTuneKnobs || L < 1 || value < 1 || value > 32);
     if (bad) return set_err(ctx, DAMASCUS_EINVAL, "tuning knob, ring size or value out of range");
     Context* C = ctx->ctx;
     std::lock_guard<std::mutex> g(C->mutex());
@@ -604,14 +605,17 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
         launch = [&] { return launch_ntt_jobs(T, &nj, 1, L, st, value); };
     } else {
         // generator / witness residues (all 0x01010101 < p) over `count` columns (pairs for the triple MAC);
-        // the split coordinates knob measures the split MAC with its blocks-per-SM knob as set
-        const uint64_t cols = knob == kTuneMacTriple ? 2ull * count : count;
+        // a coordinates knob measures its MAC with that MAC's blocks-per-SM knob as set
+        const bool triple = knob == kTuneMacTriple || knob == kTuneTripleCoords;
+        const bool split = knob == kTuneMacSplit || knob == kTuneSplitCoords;
+        const bool coords = knob == kTuneSplitCoords || knob == kTuneTripleCoords;
+        const int coords_knob = triple ? kTuneTripleCoords : kTuneSplitCoords;
+        const int bps_knob = triple ? kTuneMacTriple : kTuneMacSplit;
+        const uint64_t cols = triple ? 2ull * count : count;
         const uint32_t tpr = knob == kTuneMacPlain ? (uint32_t)s : (uint32_t)(s / 2);
-        const bool coords = knob == kTuneSplitCoords;
-        const uint32_t kc = coords ? (uint32_t)value : (uint32_t)C->tuning(kTuneSplitCoords, L);
-        const bool split = coords || knob == kTuneMacSplit;
-        const uint32_t parts = C->mac_parts_for(coords ? C->tuning(kTuneMacSplit, L) : value, tpr, count,
-                                                split ? rows / kc : rows);
+        const uint32_t kc = coords ? (uint32_t)value : (uint32_t)C->tuning(coords_knob, L);
+        const uint32_t parts = C->mac_parts_for(coords ? C->tuning(bps_knob, L) : value, tpr, count,
+                                                (split || triple) ? rows / kc : rows);
         if (a.alloc(C, cols * rows * s * 4) || b.alloc(C, cols * kPrimes * s * 4) ||
             part.alloc(C, 3ull * parts * rows * s * 4))
             return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
@@ -620,8 +624,8 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
         uint32_t* P = part.m.as<uint32_t>();
         const uint64_t ps = (uint64_t)parts * rows * s;
         mj = MacJobX{a.m.as<uint32_t>(), b.m.as<uint32_t>(), P, P + ps, P + 2 * ps, 0, 0, count, parts, 0, 0, L,
-                     split ? kc : 0u};
-        if (knob == kTuneMacTriple)
+                     (split || triple) ? kc : 0u};
+        if (triple)
             launch = [&] { return launch_mac_triple_jobs(T, &mj, 1, st); };
         else
             launch = [&, split] { return launch_mac_jobs(T, &mj, 1, split, st); };

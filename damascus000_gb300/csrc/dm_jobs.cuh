@@ -21,10 +21,11 @@ enum TuneKnob : int {
     kTuneMacTriple = 1,  // resident blocks per SM a triple MAC's column split fills: 1..32
     kTuneMacSplit = 2,   // the same for the split MAC
     kTuneMacPlain = 3,   // the same for the single-sum MAC
-    kTuneSplitCoords = 4,  // commitment coordinates per thread of the split MAC: 1, 2, 4 or 8
-    kTuneKnobs = 5,
+    kTuneSplitCoords = 4,   // commitment coordinates per thread of the split MAC: 1, 2, 4 or 8
+    kTuneTripleCoords = 5,  // the same for the triple MAC: 1, 2 or 4
+    kTuneKnobs = 6,
 };
-constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8, 1};
+constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8, 1, 1};
 // Built-in value of a knob at ring 2^L: kTuneDefault, except four coordinates per
 // thread for the split MAC from rings of 2^9 on (measured 16-21 % faster there on
 // GB300, within noise below).
@@ -55,9 +56,9 @@ struct MacJobX {
     // on zero, so the witness is read at i only and R is zero.
     uint32_t pair;
     uint32_t L;  // ring size 2^L of this job (jobs of any sizes share a launch)
-    // Split MAC only: commitment coordinates per thread, 1, 2, 4 or 8 (0 reads
-    // as 1).  A thread then loads each witness slot pair once for kc generator
-    // rows, and a part covers kRows / kc rows.
+    // Split and triple MACs: commitment coordinates per thread, 1, 2, 4 (or 8,
+    // split only); 0 reads as 1.  A thread then loads each witness slot pair
+    // once for kc generator rows, and a part covers kRows / kc rows.
     uint32_t kc;
 };
 
@@ -133,7 +134,9 @@ cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st,
                             int* kernels = nullptr);
 // Triple MAC (count = h column pairs): out0 = full sum, out1 = L, out2 = R.
-cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, cudaStream_t st);
+// kernels (optional): how many kernels it launched (one per kc value among the jobs)
+cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, cudaStream_t st,
+                                   int* kernels = nullptr);
 cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, uint32_t L, cudaStream_t st);  // 2 launches
 cudaError_t launch_fold_jobs(FoldJob* jobs, int n, cudaStream_t st);
 cudaError_t launch_gen_jobs(GenJob* jobs, int n, cudaStream_t st);

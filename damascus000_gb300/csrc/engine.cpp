@@ -64,7 +64,8 @@ int Context::create(int device, uint64_t hbm_budget, Context** out, std::string*
 int Context::set_tuning(int knob, uint32_t L, int value) {
     if (knob < 0 || knob >= kTuneKnobs || L > (uint32_t)kLogMaxProverRing) return kEInval;
     if (knob == kTuneNttGroup ? (value != 32 && value != 64)
-        : knob == kTuneSplitCoords ? (value != 1 && value != 2 && value != 4 && value != 8)
+        : knob == kTuneSplitCoords  ? (value != 1 && value != 2 && value != 4 && value != 8)
+        : knob == kTuneTripleCoords ? (value != 1 && value != 2 && value != 4)
                                    : (value < 1 || value > 32))
         return kEInval;
     tune_[knob][L].store(value, std::memory_order_relaxed);

@@ -234,73 +234,100 @@ __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> 
 // gives the full sum (out0), L = sum G[i+h] M[i] (out1) and R = sum G[i] M[i+h]
 // (out2).  h = count, or h = pair when the witness columns from h on are known
 // zero: then i runs over the count < h leading columns only, the witness is read
-// at i alone and R is zero.  Thread per slot pair (8-byte loads), L >= 1.
-__global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
-    const MacJobX jb = J.j[find_job(J)];
+// at i alone and R is zero.  Thread per slot pair (8-byte loads), L >= 1, and KC
+// commitment coordinates of one prime: each column's witness slot pairs are
+// loaded once for the KC generator rows.
+template <int KC, bool PAIR>
+DM_D void triple_rows(const MacJobX& jb, uint32_t kg, uint32_t pi, uint32_t part, uint32_t i2, const PrimeConsts& pc) {
     const uint32_t L = jb.L;
-    const uint32_t sp = 1u << (L - 1);
-    const uint32_t nblk = slot_block_count(sp);
-    uint32_t c = blockIdx.x - jb.cta0;
-    const uint32_t blk = c % nblk;
-    c /= nblk;
-    const uint32_t kp = c % kRows;
-    const uint32_t part = c / kRows;
-    const uint32_t i2 = blk * kMacThreads + threadIdx.x;
-    if (i2 >= sp) return;
-    const uint32_t k = kp / kPrimes, pi = kp % kPrimes;
-    const uint32_t h = jb.pair ? jb.pair : jb.count;
+    const uint32_t h = PAIR ? jb.pair : jb.count;
     const uint32_t i0 = (uint32_t)((uint64_t)jb.count * part / jb.parts);
     const uint32_t i1 = (uint32_t)((uint64_t)jb.count * (part + 1) / jb.parts);
     const uint64_t gstride = (uint64_t)kRank * kPrimes << L;
     const uint64_t mstride = (uint64_t)kPrimes << L;
-    const uint32_t* g = jb.G + ((((uint64_t)k) * kPrimes + pi) << L) + 2 * i2;
+    const uint64_t kstride = (uint64_t)kPrimes << L;  // the next coordinate's row, same prime
+    const uint32_t* g = jb.G + ((((uint64_t)kg * KC) * kPrimes + pi) << L) + 2 * i2;
     const uint32_t* m = jb.M + (((uint64_t)pi) << L) + 2 * i2;
     const uint64_t gh = (uint64_t)h * gstride, mh = (uint64_t)h * mstride;
-    uint64_t lo[6] = {0, 0, 0, 0, 0, 0};  // (full, L, R) x (even, odd slot)
-    uint32_t hi[6] = {0, 0, 0, 0, 0, 0};
+    constexpr int NS = PAIR ? 4 : 6;  // sums per coordinate: (full, L[, R]) x (even, odd slot)
+    uint64_t lo[KC][NS];
+    uint32_t hi[KC][NS];
+#pragma unroll
+    for (int j = 0; j < KC; ++j)
+#pragma unroll
+        for (int q = 0; q < NS; ++q) lo[j][q] = 0, hi[j][q] = 0;
+    // products below 2^56: a block sum of 16 (pair) or 8 (full: two products per sum) fits 64 bits
+    constexpr uint32_t kBlock = PAIR ? 16 : 8;
+    constexpr int kUnroll = KC >= 4 ? 2 : (KC == 2 ? 2 : 4);
     uint32_t i = i0;
-    if (jb.pair) {
-        while (i < i1) {
-            const uint32_t e = i + 16 < i1 ? i + 16 : i1;  // <= 16 products per block sum
-            uint64_t b[4] = {0, 0, 0, 0};
-#pragma unroll 4
-            for (; i < e; ++i) {
-                const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
-                const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
-                const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
-                b[0] += mul64(gl.x, ml.x);
-                b[1] += mul64(gl.y, ml.y);
-                b[2] += mul64(gr.x, ml.x);
-                b[3] += mul64(gr.y, ml.y);
-            }
+    while (i < i1) {
+        const uint32_t e = i + kBlock < i1 ? i + kBlock : i1;
+        uint64_t b[KC][NS];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc96(lo[q], hi[q], b[q]);
-        }
-    } else {
-        while (i < i1) {
-            const uint32_t e = i + 8 < i1 ? i + 8 : i1;  // <= 16 products per block sum
-            uint64_t b[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll 4
-            for (; i < e; ++i) {
-                const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride));
-                const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + gh));
-                const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
-                const uint2 mr = __ldg(reinterpret_cast<const uint2*>(m + i * mstride + mh));
-                b[0] += mul64(gl.x, ml.x) + mul64(gr.x, mr.x);
-                b[1] += mul64(gl.y, ml.y) + mul64(gr.y, mr.y);
-                b[2] += mul64(gr.x, ml.x);
-                b[3] += mul64(gr.y, ml.y);
-                b[4] += mul64(gl.x, mr.x);
-                b[5] += mul64(gl.y, mr.y);
-            }
+        for (int j = 0; j < KC; ++j)
 #pragma unroll
-            for (int q = 0; q < 6; ++q) acc96(lo[q], hi[q], b[q]);
+            for (int q = 0; q < NS; ++q) b[j][q] = 0;
+#pragma unroll kUnroll
+        for (; i < e; ++i) {
+            const uint2 ml = __ldg(reinterpret_cast<const uint2*>(m + i * mstride));
+            uint2 mr = make_uint2(0u, 0u);
+            if (!PAIR) mr = __ldg(reinterpret_cast<const uint2*>(m + i * mstride + mh));
+#pragma unroll
+            for (int j = 0; j < KC; ++j) {
+                const uint2 gl = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + j * kstride));
+                const uint2 gr = __ldg(reinterpret_cast<const uint2*>(g + i * gstride + j * kstride + gh));
+                if (PAIR) {
+                    b[j][0] += mul64(gl.x, ml.x);
+                    b[j][1] += mul64(gl.y, ml.y);
+                    b[j][2] += mul64(gr.x, ml.x);
+                    b[j][3] += mul64(gr.y, ml.y);
+                } else {
+                    b[j][0] += mul64(gl.x, ml.x) + mul64(gr.x, mr.x);
+                    b[j][1] += mul64(gl.y, ml.y) + mul64(gr.y, mr.y);
+                    b[j][2] += mul64(gr.x, ml.x);
+                    b[j][3] += mul64(gr.y, ml.y);
+                    b[j][4] += mul64(gl.x, mr.x);
+                    b[j][5] += mul64(gl.y, mr.y);
+                }
+            }
         }
+#pragma unroll
+        for (int j = 0; j < KC; ++j)
+#pragma unroll
+            for (int q = 0; q < NS; ++q) acc96(lo[j][q], hi[j][q], b[j][q]);
     }
-    const uint64_t o = (((uint64_t)part * kRows + kp) << L) + 2 * i2;
-    *reinterpret_cast<uint2*>(jb.out0 + o) = make_uint2(red96(hi[0], lo[0], pc, pi), red96(hi[1], lo[1], pc, pi));
-    *reinterpret_cast<uint2*>(jb.out1 + o) = make_uint2(red96(hi[2], lo[2], pc, pi), red96(hi[3], lo[3], pc, pi));
-    *reinterpret_cast<uint2*>(jb.out2 + o) = make_uint2(red96(hi[4], lo[4], pc, pi), red96(hi[5], lo[5], pc, pi));
+#pragma unroll
+    for (int j = 0; j < KC; ++j) {
+        const uint64_t row = (uint64_t)part * kRows + (kg * KC + j) * kPrimes + pi;
+        const uint64_t o = (row << L) + 2 * i2;
+        *reinterpret_cast<uint2*>(jb.out0 + o) =
+            make_uint2(red96(hi[j][0], lo[j][0], pc, pi), red96(hi[j][1], lo[j][1], pc, pi));
+        *reinterpret_cast<uint2*>(jb.out1 + o) =
+            make_uint2(red96(hi[j][2], lo[j][2], pc, pi), red96(hi[j][3], lo[j][3], pc, pi));
+        *reinterpret_cast<uint2*>(jb.out2 + o) =
+            PAIR ? make_uint2(0u, 0u)
+                 : make_uint2(red96(hi[j][NS - 2], lo[j][NS - 2], pc, pi), red96(hi[j][NS - 1], lo[j][NS - 1], pc, pi));
+    }
+}
+
+// grid: per job, nblk * (72 / KC) * parts blocks; every job of a launch has kc == KC.
+template <int KC>
+__global__ void __launch_bounds__(kMacThreads) mac_triple_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
+    const MacJobX jb = J.j[find_job(J)];
+    const uint32_t sp = 1u << (jb.L - 1);
+    const uint32_t nblk = slot_block_count(sp);
+    constexpr uint32_t rows = kRows / KC;
+    uint32_t c = blockIdx.x - jb.cta0;
+    const uint32_t blk = c % nblk;
+    c /= nblk;
+    const uint32_t kp = c % rows;
+    const uint32_t part = c / rows;
+    const uint32_t i2 = blk * kMacThreads + threadIdx.x;
+    if (i2 >= sp) return;
+    if (jb.pair)
+        triple_rows<KC, true>(jb, kp / kPrimes, kp % kPrimes, part, i2, pc);
+    else
+        triple_rows<KC, false>(jb, kp / kPrimes, kp % kPrimes, part, i2, pc);
 }
 
 // Split MAC: thread per slot pair (2 i2, 2 i2 + 1) of ring 2^L (L >= 1) and KC
@@ -762,7 +789,7 @@ cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t
 namespace {
 template <class Slots>
 cudaError_t mac_launch_common(MacJobX* jobs, int n, Slots slots_of, JobList<MacJobX>& JL, uint64_t* total,
-                              unsigned* bx, bool split = false) {
+                              unsigned* bx, bool coords = false) {
     uint32_t widest = 1;
     *total = 0;
     JL.n = n;
@@ -770,7 +797,7 @@ cudaError_t mac_launch_common(MacJobX* jobs, int n, Slots slots_of, JobList<MacJ
         if (jobs[i].L > (uint32_t)kLogMaxProverRing) return cudaErrorInvalidValue;
         const uint32_t slots = slots_of(jobs[i]);
         if (slots == 0) return cudaErrorInvalidValue;
-        const uint32_t kc = split && jobs[i].kc ? jobs[i].kc : 1u;
+        const uint32_t kc = coords && jobs[i].kc ? jobs[i].kc : 1u;
         if (kc != 1 && kc != 2 && kc != 4 && kc != 8) return cudaErrorInvalidValue;
         jobs[i].cta0 = (uint32_t)*total;
         JL.j[i] = jobs[i];
@@ -782,18 +809,37 @@ cudaError_t mac_launch_common(MacJobX* jobs, int n, Slots slots_of, JobList<MacJ
 }
 }  // namespace
 
-cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, cudaStream_t st) {
+cudaError_t launch_mac_triple_jobs(const DeviceTables& T, MacJobX* jobs, int n, cudaStream_t st, int* kernels) {
+    if (kernels) *kernels = 0;
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs) return cudaErrorInvalidValue;
     JobList<MacJobX> JL;
     uint64_t total;
     unsigned bx;
-    cudaError_t e = mac_launch_common(jobs, n, [](const MacJobX& j) { return j.L ? 1u << (j.L - 1) : 0u; }, JL,
-                                      &total, &bx);  // slot pairs
-    if (e != cudaSuccess) return e;
-    if (!total) return cudaSuccess;
-    mac_triple_jobs_kernel<<<(unsigned)total, bx, 0, st>>>(JL, T.pc);
-    return cudaGetLastError();
+    // one launch per coordinates-per-thread value present
+    for (uint32_t kc : {1u, 2u, 4u}) {
+        MacJobX group[kMaxJobs];
+        int m = 0;
+        for (int i = 0; i < n; ++i) {
+            const uint32_t jkc = jobs[i].kc ? jobs[i].kc : 1u;
+            if (jkc != 1 && jkc != 2 && jkc != 4) return cudaErrorInvalidValue;
+            if (jkc == kc) group[m++] = jobs[i];
+        }
+        if (!m) continue;
+        cudaError_t e = mac_launch_common(group, m, [](const MacJobX& j) { return j.L ? 1u << (j.L - 1) : 0u; },
+                                          JL, &total, &bx, true);  // slot pairs
+        if (e != cudaSuccess) return e;
+        if (!total) continue;
+        switch (kc) {
+            case 1: mac_triple_jobs_kernel<1><<<(unsigned)total, bx, 0, st>>>(JL, T.pc); break;
+            case 2: mac_triple_jobs_kernel<2><<<(unsigned)total, bx, 0, st>>>(JL, T.pc); break;
+            default: mac_triple_jobs_kernel<4><<<(unsigned)total, bx, 0, st>>>(JL, T.pc); break;
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        if (kernels) ++*kernels;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st, int* kernels) {

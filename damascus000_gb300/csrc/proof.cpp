@@ -174,7 +174,7 @@ int Plan::launch_all(Context* ctx, cudaStream_t st, std::string* err) {
                  for (size_t i = 0; i < v.size(); i += kMaxJobs) {
                      const int n = (int)std::min<size_t>(kMaxJobs, v.size() - i);
                      int k = 1;
-                     cudaError_t e = pass == 2 ? launch_mac_triple_jobs(T, v.data() + i, n, st)
+                     cudaError_t e = pass == 2 ? launch_mac_triple_jobs(T, v.data() + i, n, st, &k)
                                                : launch_mac_jobs(T, v.data() + i, n, pass == 1, st, &k);
                      if (e != cudaSuccess) return (int)e;
                      launches += k;
@@ -351,19 +351,21 @@ bool ProofState::plan_commit(Plan& P, uint32_t L, uint32_t cols, uint32_t c, con
         return false;
     }
     const uint32_t half = cols / 2;
+    const uint32_t kc = (uint32_t)ctx_->tuning(kTuneTripleCoords, L);
+    const int bps = ctx_->tuning(kTuneMacTriple, L);
     if (c <= half) {
         ntt(m_src, mh, c);
         ntt(g_src, gh, 8ull * c);
         ntt(g_src + half * gcol_in, gh + half * gcol_out, 8ull * c);
-        parts_ = ctx_->mac_parts(kTuneMacTriple, L, (uint32_t)(s / 2), c);
+        parts_ = ctx_->mac_parts_for(bps, (uint32_t)(s / 2), c, kRows / kc);
         const size_t ps = (size_t)parts_ * kRows * s;
-        P.triple.push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, c, parts_, 0, half, L});
+        P.triple.push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, c, parts_, 0, half, L, kc});
     } else {
         ntt(m_src, mh, cols);
         ntt(g_src, gh, 8ull * cols);
-        parts_ = ctx_->mac_parts(kTuneMacTriple, L, (uint32_t)(s / 2), half);
+        parts_ = ctx_->mac_parts_for(bps, (uint32_t)(s / 2), half, kRows / kc);
         const size_t ps = (size_t)parts_ * kRows * s;
-        P.triple.push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, half, parts_, 0, 0, L});
+        P.triple.push_back(MacJobX{gh, mh, part, part + ps, part + 2 * ps, 0, 0, half, parts_, 0, 0, L, kc});
     }
     return true;
 }
