@@ -783,9 +783,13 @@ int damascus_engine_cancel(damascus_engine* e, uint64_t ticket) {
     if (!e) return DAMASCUS_EINVAL;
     {
         std::lock_guard<std::mutex> g(e->mu);
-        if (e->status.count(ticket)) return DAMASCUS_ESTATE;  // finished, result not taken yet
+        if (e->status.count(ticket))  // finished, result not taken yet
+            return set_err(e->owner, DAMASCUS_ESTATE, "cancel: the request has already finished");
     }
-    return e->e->cancel(ticket);
+    const int rc = e->e->cancel(ticket);
+    if (rc == kEInval) return set_err(e->owner, DAMASCUS_EINVAL, "cancel: unknown ticket (or its proof was taken)");
+    if (rc == kEState) return set_err(e->owner, DAMASCUS_ESTATE, "cancel: the request has already finished");
+    return rc;
 }
 
 int damascus_engine_set_request_timeout(damascus_engine* e, double timeout_ms) {

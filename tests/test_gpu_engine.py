@@ -2,6 +2,7 @@
 one-at-a-time path (and to the oracle for small files), whether the request ran
 alone or mixed with others of different depths; admission respects the HBM
 budget; a failing request does not disturb the others."""
+import ctypes
 import random
 
 import pytest
@@ -207,10 +208,17 @@ def test_engine_cancel_queued_and_admitted_requests(ctx):
                 with pytest.raises(D.DamascusError) as e:
                     eng.wait(t)
                 assert e.value.code == D.ECANCELED
-            proof = eng.wait(ts)[0]
+            proof = eng.wait(ts)[0]  # finished and taken: the ticket is forgotten
             with pytest.raises(D.DamascusError) as e:
-                eng.cancel(ts)  # already finished
-            assert e.value.code == D.ESTATE
+                eng.cancel(ts)
+            assert e.value.code == D.EINVAL
+            # finished but not yet taken: too late to cancel
+            lib = D.load()
+            t2 = eng.submit(*small, EPOCH)
+            n, lat = ctypes.c_size_t(), ctypes.c_double()
+            assert lib.damascus_engine_wait(eng._h, t2, ctypes.byref(n), ctypes.byref(lat)) == 1
+            assert lib.damascus_engine_cancel(eng._h, t2) == D.ESTATE
+            assert eng.wait(t2)[0] == proof
             assert eng.health()["unfinished"] == 0
         assert c.reserved == 0
     finally:
