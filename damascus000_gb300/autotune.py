@@ -7,6 +7,10 @@ writes a table that `apply()` loads into a context:
 
 * `NTT_GROUP`  — threads per block of the forward transform for rings below 2^10
   (32 or 64: how many small polynomials share a block);
+* `NTT_RADIX` — residues per thread of the forward transform for rings of 2^5 and
+  up (16 or 32: radix-16 or radix-32 register passes; radix 32 needs one
+  shared-memory exchange fewer at 2^9 and 2^10 but holds twice the registers).
+  It is tuned jointly with `NTT_GROUP`;
 * `MAC_TRIPLE`, `MAC_SPLIT`, `MAC_PLAIN` — the resident blocks per SM that a
   multiply-accumulate's column split fills (its part count; more parts mean more
   blocks in flight but more partial sums for the finish to add);
@@ -31,9 +35,9 @@ import time
 from pathlib import Path
 from typing import Dict, List, Optional
 
-NTT_GROUP, MAC_TRIPLE, MAC_SPLIT, MAC_PLAIN, SPLIT_COORDS, TRIPLE_COORDS = 0, 1, 2, 3, 4, 5
+NTT_GROUP, MAC_TRIPLE, MAC_SPLIT, MAC_PLAIN, SPLIT_COORDS, TRIPLE_COORDS, NTT_RADIX = 0, 1, 2, 3, 4, 5, 6
 KNOB_NAMES = {NTT_GROUP: "ntt_group", MAC_TRIPLE: "mac_triple", MAC_SPLIT: "mac_split", MAC_PLAIN: "mac_plain",
-              SPLIT_COORDS: "split_coords", TRIPLE_COORDS: "triple_coords"}
+              SPLIT_COORDS: "split_coords", TRIPLE_COORDS: "triple_coords", NTT_RADIX: "ntt_radix"}
 CANDIDATES = {
     NTT_GROUP: [32, 64],
     MAC_TRIPLE: [2, 4, 8, 12, 16, 24],
@@ -41,6 +45,7 @@ CANDIDATES = {
     MAC_PLAIN: [2, 4, 8, 16],
     SPLIT_COORDS: [1, 2, 4, 8],
     TRIPLE_COORDS: [1, 2, 4],
+    NTT_RADIX: [16, 32],
 }
 DEFAULT_TABLE = Path(__file__).resolve().parent / "tuning_gb300.json"
 
@@ -50,7 +55,7 @@ def work_size(knob: int, L: int) -> int:
     witness + generator polynomials for the transform, column pairs for the triple
     MAC, columns for the split and single-sum MACs."""
     n = 1 << L
-    if knob == NTT_GROUP:
+    if knob in (NTT_GROUP, NTT_RADIX):
         return 9 * n
     if knob == MAC_TRIPLE:
         return max(1, n // 2)
@@ -60,12 +65,15 @@ def work_size(knob: int, L: int) -> int:
 def ring_sizes(knob: int) -> List[int]:
     if knob == NTT_GROUP:
         return list(range(4, 10))  # larger rings fill their blocks either way
+    if knob == NTT_RADIX:
+        return list(range(5, 14))
     return list(range(4, 13))
 
 
 # the library's built-in values (the split's coordinates per thread: 4 from rings of 2^9 on); the autotuner
 # reads them from a context made without a table
-DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1, TRIPLE_COORDS: 1}
+DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1, TRIPLE_COORDS: 1,
+            NTT_RADIX: 16}
 ENGINE_WAVES = "engine_waves"
 WAVE_CANDIDATES = [4, 8, 12, 16, 24, 32]
 DEFAULT_WAVES = 16
@@ -87,14 +95,17 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
     """Measures every candidate and sets the chosen value on `ctx`; returns the table."""
     entries = []
     for knob in knobs if knobs is not None else list(CANDIDATES):
-        if knob in (SPLIT_COORDS, TRIPLE_COORDS):
-            continue  # tuned with MAC_SPLIT / MAC_TRIPLE
+        if knob in (SPLIT_COORDS, TRIPLE_COORDS, NTT_GROUP):
+            continue  # tuned with MAC_SPLIT / MAC_TRIPLE / NTT_RADIX
         for L in ring_sizes(knob):
             if L > max_L:
                 continue
             count = work_size(knob, L)
             if knob in (MAC_SPLIT, MAC_TRIPLE):
                 entries += tune_coords(ctx, knob, L, count, reps, margin, log)
+                continue
+            if knob == NTT_RADIX:
+                entries += tune_transform(ctx, L, count, reps, margin, log)
                 continue
             default = ctx.tuning_get(knob, L)  # the library's built-in value
             times = {}
@@ -108,6 +119,27 @@ def tune(ctx, knobs: Optional[List[int]] = None, reps: int = 5, max_L: int = 12,
                 + " ".join(f"{k}:{t:.4f}" for k, t in times.items()))
     return {"device": "GB300", "generated": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()), "reps": reps,
             "margin": margin, "min_gain_ms": 0.001, "entries": entries}
+
+
+def tune_transform(ctx, L: int, count: int, reps: int, margin: float, log=print) -> List[Dict]:
+    """The forward transform's (residues per thread, threads per block) pair at
+    ring 2^L; the block size is a choice below 2^10 only."""
+    groups = CANDIDATES[NTT_GROUP] if L < 10 else [ctx.tuning_get(NTT_GROUP, L)]
+    default = (ctx.tuning_get(NTT_RADIX, L), ctx.tuning_get(NTT_GROUP, L))
+    times = {}
+    for g in groups:
+        ctx.tuning_set(NTT_GROUP, L, g)
+        for e in CANDIDATES[NTT_RADIX]:
+            times[(e, g)] = ctx.tuning_measure(NTT_RADIX, L, e, count, reps)
+    e, g = choose(times, default, margin)
+    ctx.tuning_set(NTT_RADIX, L, e)
+    ctx.tuning_set(NTT_GROUP, L, g)
+    ms = {f"{a}x{b}": round(t, 5) for (a, b), t in times.items()}
+    log(f"ntt        L={L:2d} count={count:6d} best={e}x{g} " + " ".join(f"{k}:{t:.4f}" for k, t in ms.items()))
+    out = [{"knob": KNOB_NAMES[NTT_RADIX], "log_ring": L, "value": e, "count": count, "ms": ms}]
+    if L < 10:
+        out.append({"knob": KNOB_NAMES[NTT_GROUP], "log_ring": L, "value": g, "count": count})
+    return out
 
 
 def tune_coords(ctx, knob: int, L: int, count: int, reps: int, margin: float, log=print) -> List[Dict]:

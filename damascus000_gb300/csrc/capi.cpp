@@ -276,7 +276,7 @@ static int commit_common(damascus_ctx* ctx, const uint8_t* witness, const uint8_
     } else if (e == cudaSuccess) {
         e = launch_gen_generators(g_seed, N, L, gg.m.as<uint4>(), s);  // already below q
     }
-    if (e == cudaSuccess) e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L));
+    if (e == cudaSuccess) e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L), C->tuning(kTuneNttRadix, L));
     if (e == cudaSuccess) e = launch_mac_jobs(T, &mj, 1, false, s);
     if (e == cudaSuccess) e = launch_finish_jobs(T, &fj, 1, L, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(com_out, out.m.as<uint8_t>(), kRank * n * 16, cudaMemcpyDeviceToHost, s);
@@ -370,7 +370,7 @@ int damascus_ring_mul_batch_device(damascus_ctx* ctx, const void* d_a, const voi
     }
     NttJob nj[2] = {{static_cast<const uint4*>(d_a), ra.m.as<uint32_t>(), (uint32_t)count, 0},
                     {static_cast<const uint4*>(d_b), rb.m.as<uint32_t>(), (uint32_t)count, 0}};
-    cudaError_t e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L));
+    cudaError_t e = launch_ntt_jobs(T, nj, 2, L, s, C->tuning(kTuneNttGroup, L), C->tuning(kTuneNttRadix, L));
     if (e0) {
         e1 = C->take_event();
         cudaEventRecord(e1, s);
@@ -582,6 +582,7 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
     const uint32_t L = log_ring;
     const uint64_t s = 1ull << L;
     const bool bad = knob == kTuneNttGroup       ? (L < 4 || (value != 32 && value != 64))
+                     : knob == kTuneNttRadix     ? (L < 5 || (value != 16 && value != 32))
                      : knob == kTuneSplitCoords  ? (L < 1 || (value != 1 && value != 2 && value != 4 && value != 8))
                      : knob == kTuneTripleCoords ? (L < 1 || (value != 1 && value != 2 && value != 4))
                                                  : (knob <= 0 || knob >= kTuneKnobs || L < 1 || value < 1 || value > 32);
@@ -596,13 +597,15 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
     std::function<cudaError_t()> launch;
     NttJob nj{};
     MacJobX mj{};
-    if (knob == kTuneNttGroup) {
+    if (knob == kTuneNttGroup || knob == kTuneNttRadix) {
         // count polynomials of arbitrary 128-bit words -> nine residue rows each
         if (a.alloc(C, count * s * 16) || b.alloc(C, count * kPrimes * s * 4))
             return set_err(ctx, DAMASCUS_ENOMEM_BUDGET, "HBM budget exhausted");
         cudaMemsetAsync(a.m.as<uint8_t>(), 0x5A, count * s * 16, st);
         nj = NttJob{a.m.as<uint4>(), b.m.as<uint32_t>(), count, 0};
-        launch = [&] { return launch_ntt_jobs(T, &nj, 1, L, st, value); };
+        const int group = knob == kTuneNttGroup ? value : C->tuning(kTuneNttGroup, L);
+        const int elems = knob == kTuneNttRadix ? value : C->tuning(kTuneNttRadix, L);
+        launch = [&, group, elems] { return launch_ntt_jobs(T, &nj, 1, L, st, group, elems); };
     } else {
         // generator / witness residues (all 0x01010101 < p) over `count` columns (pairs for the triple MAC);
         // a coordinates knob measures its MAC with that MAC's blocks-per-SM knob as set

@@ -23,9 +23,10 @@ enum TuneKnob : int {
     kTuneMacPlain = 3,   // the same for the single-sum MAC
     kTuneSplitCoords = 4,   // commitment coordinates per thread of the split MAC: 1, 2, 4 or 8
     kTuneTripleCoords = 5,  // the same for the triple MAC: 1, 2 or 4
-    kTuneKnobs = 6,
+    kTuneNttRadix = 6,      // residues per thread of the forward transform (pass radix): 16 or 32
+    kTuneKnobs = 7,
 };
-constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8, 1, 1};
+constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8, 1, 1, 16};
 // Built-in value of a knob at ring 2^L: kTuneDefault, except four coordinates per
 // thread for the split MAC from rings of 2^9 on (measured 16-21 % faster there on
 // GB300, within noise below).
@@ -128,7 +129,10 @@ struct HashJob {
 };
 
 // group: threads per block for rings below 2^10 (32 or 64, kTuneNttGroup)
-cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group = 64);
+// elems: residues per thread, i.e. the pass radix (16, or 32 for rings of 2^5
+// and up: radix-32 passes, one exchange fewer at 2^9 and 2^10; kTuneNttRadix)
+cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group = 64,
+                            int elems = 16);
 // kernels (optional): how many kernels it launched (the split MAC launches one
 // per coordinates-per-thread value among the jobs)
 cudaError_t launch_mac_jobs(const DeviceTables& T, MacJobX* jobs, int n, bool split, cudaStream_t st,

@@ -20,22 +20,37 @@ namespace dm {
 constexpr int kNttE = 16;  // elements per thread
 constexpr int kNttLogE = 4;
 
-DM_HD int ntt_pass_count(int L) { return L <= kNttLogE ? 1 : (L + kNttLogE - 1) / kNttLogE; }
-DM_HD int ntt_pass_lo(int L, int pass) {
-    const int lo = L - kNttLogE - kNttLogE * pass;
+// The pass shape is a parameter LE (2^LE residues per thread, LE stages per
+// pass): 4 everywhere, and 5 as the forward transform's alternative radix-32
+// passes (one exchange fewer at 2^9 and 2^10).  The un-suffixed names are LE = 4.
+template <int LE>
+DM_HD int ntt_pass_count_e(int L) { return L <= LE ? 1 : (L + LE - 1) / LE; }
+template <int LE>
+DM_HD int ntt_pass_lo_e(int L, int pass) {
+    const int lo = L - LE - LE * pass;
     return lo > 0 ? lo : 0;
 }
-// Element index of register r of thread t in pass `pass` (L >= 4).  Pass 0 holds
-// element r * 2^(L-4) + t (coalesced loads); the last pass 16 contiguous slots.
-DM_HD uint32_t ntt_place(int L, int pass, uint32_t t, uint32_t r) {
-    const int lo = ntt_pass_lo(L, pass);
-    return ((t >> lo) << (lo + kNttLogE)) | (r << lo) | (t & ((1u << lo) - 1u));
+// Element index of register r of thread t in pass `pass` (L >= LE).  Pass 0
+// holds element r * 2^(L-LE) + t (coalesced loads); the last pass 2^LE
+// contiguous slots.
+template <int LE>
+DM_HD uint32_t ntt_place_e(int L, int pass, uint32_t t, uint32_t r) {
+    const int lo = ntt_pass_lo_e<LE>(L, pass);
+    return ((t >> lo) << (lo + LE)) | (r << lo) | (t & ((1u << lo) - 1u));
 }
+DM_HD int ntt_pass_count(int L) { return ntt_pass_count_e<kNttLogE>(L); }
+DM_HD int ntt_pass_lo(int L, int pass) { return ntt_pass_lo_e<kNttLogE>(L, pass); }
+DM_HD uint32_t ntt_place(int L, int pass, uint32_t t, uint32_t r) { return ntt_place_e<kNttLogE>(L, pass, t, r); }
 // Shared-memory word of block-wide element index i: bits 0..4 XOR bits 4..8.  A
 // bijection that makes every pass's scalar stores and loads bank-conflict free
 // for the block shapes of the transform kernels (rows of 2^L words, 2^(L-4)
 // threads per row).
 DM_HD uint32_t ntt_swz(uint32_t i) { return i ^ ((i >> 4) & 31u); }
+// The same for radix-2^LE passes: bits 0..4 XOR bits LE..LE+4 (for LE = 4 the
+// function above; LE = 5 moves the folded field above the register field of
+// the last pass, where bits 0..4 are the register index).
+template <int LE>
+DM_HD uint32_t ntt_swz_e(uint32_t i) { return i ^ ((i >> LE) & 31u); }
 
 // ---- lazy Harvey butterflies (p < 2^28) ----
 //
@@ -53,10 +68,12 @@ DM_HD uint32_t ntt_swz(uint32_t i) { return i ^ ((i >> 4) & 31u); }
 // k = 2^st + ((t >> lo) << (3 - rb)) + (r >> (rb + 1)): a stage needs only
 // 8 >> rb distinct twiddles per thread (15 per four-stage pass, not 32).
 
-// The 8 >> rb twiddles tw[kb ..] of a stage.  kb is a multiple of their count
-// (2^st >= 8 >> rb), so pairs are 16-byte aligned and load as one 16-byte word.
-DM_HD void ntt_load_twiddles(Tw w[8], const Tw* tw, uint32_t kb, int rb) {
-    const int ng = 8 >> rb;
+// The (2^(LE-1) >> rb) twiddles tw[kb ..] of a stage.  kb is a multiple of their
+// count (2^st >= their count whenever L >= LE), so pairs are 16-byte aligned and
+// load as one 16-byte word.
+template <int LE>
+DM_HD void ntt_load_twiddles_e(Tw w[1 << (LE - 1)], const Tw* tw, uint32_t kb, int rb) {
+    const int ng = (1 << (LE - 1)) >> rb;
     if (ng == 1) {
         w[0] = tw[kb];
         return;
@@ -73,6 +90,7 @@ DM_HD void ntt_load_twiddles(Tw w[8], const Tw* tw, uint32_t kb, int rb) {
     for (int g = 0; g < ng; ++g) w[g] = tw[kb + g];
 #endif
 }
+DM_HD void ntt_load_twiddles(Tw w[8], const Tw* tw, uint32_t kb, int rb) { ntt_load_twiddles_e<kNttLogE>(w, tw, kb, rb); }
 
 // The last pass (lo = 0) gives every thread its own 8 >> rb twiddles per stage,
 // so in the natural order a warp's 16-byte loads stride 16 * (ng / 2) bytes and
@@ -107,6 +125,44 @@ DM_HD void ntt_load_twiddles_last(Tw w[8], const Tw* twl, int L, int st, uint32_
 
 // x mod p in [0, 2p) for any x < 2^32: Shoup product by 1 (one_s = floor(2^32 / p)).
 DM_HD uint32_t shoup_one(uint32_t x, uint32_t one_s, uint32_t p) { return x - mulhi32(x, one_s) * p; }
+
+// Forward stages [LE*pass, min(LE*pass+LE, L)) on the 2^LE registers of thread t
+// (radix-2^LE pass shape; see ntt_fwd_pass for LE = 4).  Values start every pass
+// below 8p and grow by 2p per stage; a pass of five stages brings them below 8p
+// again before its fifth (16p + 2p would not fit 32 bits for p near 2^28), so
+// outputs stay below 16p.  twl, the last-pass twiddle order, exists for LE = 4
+// only: other shapes read the natural table in every pass (twl unused).
+template <int LE>
+DM_HD void ntt_fwd_pass_e(uint32_t a[1 << LE], int L, int pass, uint32_t t, const Tw* tw, uint32_t p) {
+    constexpr int E = 1 << LE;
+    const int lo = ntt_pass_lo_e<LE>(L, pass);
+    const int st0 = LE * pass;
+    const int st_end = (st0 + LE < L) ? st0 + LE : L;
+    const uint32_t p2 = 2 * p, p8 = 8 * p;
+    const uint32_t th = t >> lo;
+    if (pass > 0) {
+        DM_UNROLL
+        for (int r = 0; r < E; ++r) a[r] = red_below(a[r], p8);  // [0, 8p)
+    }
+    DM_UNROLL
+    for (int st = st0; st < st_end; ++st) {
+        if (st - st0 == 4) {
+            DM_UNROLL
+            for (int r = 0; r < E; ++r) a[r] = red_below(a[r], p8);  // from [0, 16p) to [0, 8p)
+        }
+        const int rb = L - 1 - st - lo;  // bit of the butterfly distance within r
+        Tw w[E / 2];
+        ntt_load_twiddles_e<LE>(w, tw, (1u << st) + (th << (LE - 1 - rb)), rb);
+        DM_UNROLL
+        for (int r = 0; r < E; ++r) {
+            if (r & (1 << rb)) continue;
+            const uint32_t u = a[r];
+            const uint32_t v = shoup_mul(a[r | (1 << rb)], w[r >> (rb + 1)], p);  // [0, 2p)
+            a[r] = u + v;
+            a[r | (1 << rb)] = u - v + p2;
+        }
+    }
+}
 
 // Forward (Cooley-Tukey) stages [4*pass, min(4*pass+4, L)) on the 16 registers
 // of thread t; inputs below 8p (first pass) or below 16p (later passes, which
@@ -175,10 +231,18 @@ DM_HD void ntt_inv_pass(uint32_t a[kNttE], int L, int pass, uint32_t t, const Tw
 // a row-base | place(t, 0) word has no bits in the register field, so the word
 // of register r is swz(base | place(t, 0)) ^ swz(r << lo): one XOR with a
 // compile-time constant per access.
-DM_HD uint32_t ntt_swz_base(uint32_t base, int L, int pass, uint32_t t) {
-    return ntt_swz(base | ntt_place(L, pass, t, 0));
+template <int LE>
+DM_HD uint32_t ntt_swz_base_e(uint32_t base, int L, int pass, uint32_t t) {
+    return ntt_swz_e<LE>(base | ntt_place_e<LE>(L, pass, t, 0));
 }
-DM_HD uint32_t ntt_swz_reg(int L, int pass, int r) { return ntt_swz((uint32_t)r << ntt_pass_lo(L, pass)); }
+template <int LE>
+DM_HD uint32_t ntt_swz_reg_e(int L, int pass, int r) {
+    return ntt_swz_e<LE>((uint32_t)r << ntt_pass_lo_e<LE>(L, pass));
+}
+DM_HD uint32_t ntt_swz_base(uint32_t base, int L, int pass, uint32_t t) {
+    return ntt_swz_base_e<kNttLogE>(base, L, pass, t);
+}
+DM_HD uint32_t ntt_swz_reg(int L, int pass, int r) { return ntt_swz_reg_e<kNttLogE>(L, pass, r); }
 
 // Whole transforms of one ring of size s = 2^L < 16 held in registers (one
 // thread per ring and prime): forward from [0, 8p) (outputs below 14p), inverse

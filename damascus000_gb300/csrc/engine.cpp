@@ -66,6 +66,7 @@ int Context::set_tuning(int knob, uint32_t L, int value) {
     if (knob == kTuneNttGroup ? (value != 32 && value != 64)
         : knob == kTuneSplitCoords  ? (value != 1 && value != 2 && value != 4 && value != 8)
         : knob == kTuneTripleCoords ? (value != 1 && value != 2 && value != 4)
+        : knob == kTuneNttRadix     ? (value != 16 && value != 32)
                                    : (value < 1 || value > 32))
         return kEInval;
     tune_[knob][L].store(value, std::memory_order_relaxed);

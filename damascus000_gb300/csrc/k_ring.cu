@@ -60,42 +60,48 @@ struct RowShape {
 // threads with kPrimesPerThread residue rows per thread; shared memory holds
 // kPrimesPerThread x P rows, prime-major, so each prime's rows sit together as
 // in a one-prime block.
-template <int L, int G = DM_ROW_GROUP_THREADS>
+// LE: the pass radix, 2^LE residues per thread (4, or 5 for the radix-32
+// alternative the kTuneNttRadix knob selects).
+template <int L, int G = DM_ROW_GROUP_THREADS, int LE = kNttLogE>
 struct FwdShape {
     static_assert(G == 32 || G == 64, "row groups of 32 or 64 threads");
-    static constexpr int T = 1 << (L - 4);
+    static_assert(LE == 4 || LE == 5, "radix-16 or radix-32 passes");
+    static constexpr int T = 1 << (L - LE);
     static constexpr int P = T >= G ? 1 : G / T;
     static constexpr int THREADS = P * T;
-    static constexpr int PASSES = (L + 3) / 4;
+    static constexpr int PASSES = (L + LE - 1) / LE;
     static constexpr size_t SMEM = PASSES > 1 ? (size_t)kPrimesPerThread * P * (1u << L) * sizeof(uint32_t) : 0;
     // resident blocks per SM the register budget is sized for (32 warps per SM
     // with one prime per thread: measured faster than 48 or 64; the registers
-    // hold loads in flight)
-    static constexpr int MIN_BLOCKS =
-        (DM_FWD_RESIDENT_WARPS * 32) / THREADS > 0 ? (DM_FWD_RESIDENT_WARPS * 32) / THREADS : 1;
+    // hold loads in flight).  Radix-32 passes hold twice the residues and
+    // twiddles per thread: 16 warps.
+    static constexpr int WARPS = LE == kNttLogE ? DM_FWD_RESIDENT_WARPS : 16;
+    static constexpr int MIN_BLOCKS = (WARPS * 32) / THREADS > 0 ? (WARPS * 32) / THREADS : 1;
 };
 
 // Exchange barrier of one row group: a group of 2^(L-4) consecutive threads that
 // fits one warp needs only a warp barrier; larger groups are the whole block.
 // Every thread of a group, active or not, runs the same passes and so the same
 // barriers.
-template <int L>
+template <int L, int LE = kNttLogE>
 DM_D void row_sync() {
-    if constexpr ((1 << (L - 4)) <= 32) {
+    if constexpr ((1 << (L - LE)) <= 32) {
         __syncwarp();
     } else {
-        static_assert(RowShape<L>::P == 1 && FwdShape<L, 64>::P == 1, "groups above a warp fill their block");
+        static_assert(FwdShape<L, 64, LE>::P == 1 && (LE != kNttLogE || RowShape<L>::P == 1),
+                      "groups above a warp fill their block");
         __syncthreads();
     }
 }
 
 // ================================================================ forward NTT
 
-template <int L, int G>
-__global__ void __launch_bounds__(FwdShape<L, G>::THREADS, FwdShape<L, G>::MIN_BLOCKS)
+template <int L, int G, int LE = kNttLogE>
+__global__ void __launch_bounds__(FwdShape<L, G, LE>::THREADS, FwdShape<L, G, LE>::MIN_BLOCKS)
     ntt_fwd_kernel(JobList<NttJob> J, PrimeConsts pc, const Tw* __restrict__ fwd, const Tw* __restrict__ fwd_last) {
-    using S = FwdShape<L, G>;
+    using S = FwdShape<L, G, LE>;
     constexpr int K = kPrimesPerThread;
+    constexpr int E = 1 << LE;
     extern __shared__ __align__(16) uint32_t sm[];
     const NttJob jb = J.j[find_job(J)];
     const uint32_t lcta = blockIdx.x - jb.cta0;
@@ -104,12 +110,12 @@ __global__ void __launch_bounds__(FwdShape<L, G>::THREADS, FwdShape<L, G>::MIN_B
     const uint32_t t = threadIdx.x % S::T;
     const uint64_t poly = (uint64_t)grp * S::P + prow;
     const bool active = poly < jb.npolys;
-    uint32_t a[K][kNttE];
+    uint32_t a[K][E];
     if (active) {
         const uint4* src = jb.src + (poly << L);
 #pragma unroll
-        for (int r = 0; r < kNttE; ++r) {
-            const fq x = ldq(src, ntt_place(L, 0, t, r));
+        for (int r = 0; r < E; ++r) {
+            const fq x = ldq(src, ntt_place_e<LE>(L, 0, t, r));
 #pragma unroll
             for (int k = 0; k < K; ++k) a[k][r] = residue_fwd(x, pc, pi0 + k);
         }
@@ -117,29 +123,33 @@ __global__ void __launch_bounds__(FwdShape<L, G>::THREADS, FwdShape<L, G>::MIN_B
 #pragma unroll
         for (int k = 0; k < K; ++k)
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) a[k][r] = 0;
+            for (int r = 0; r < E; ++r) a[k][r] = 0;
     }
 #pragma unroll
     for (int pass = 0; pass < S::PASSES; ++pass) {
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-            ntt_fwd_pass(a[k], L, pass, t, fwd + (pi0 + k) * kMaxRing,
-                         fwd_last + (pi0 + k) * kLastSpan + (1u << L) - 16u, pc.p[pi0 + k]);
+        for (int k = 0; k < K; ++k) {
+            if constexpr (LE == kNttLogE)
+                ntt_fwd_pass(a[k], L, pass, t, fwd + (pi0 + k) * kMaxRing,
+                             fwd_last + (pi0 + k) * kLastSpan + (1u << L) - 16u, pc.p[pi0 + k]);
+            else
+                ntt_fwd_pass_e<LE>(a[k], L, pass, t, fwd + (pi0 + k) * kMaxRing, pc.p[pi0 + k]);
+        }
         if (pass + 1 < S::PASSES) {
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                const uint32_t ws = ntt_swz_base((uint32_t)(k * S::P + prow) << L, L, pass, t);
+                const uint32_t ws = ntt_swz_base_e<LE>((uint32_t)(k * S::P + prow) << L, L, pass, t);
 #pragma unroll
-                for (int r = 0; r < kNttE; ++r) sm[ws ^ ntt_swz_reg(L, pass, r)] = a[k][r];
+                for (int r = 0; r < E; ++r) sm[ws ^ ntt_swz_reg_e<LE>(L, pass, r)] = a[k][r];
             }
-            row_sync<L>();
+            row_sync<L, LE>();
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                const uint32_t rs = ntt_swz_base((uint32_t)(k * S::P + prow) << L, L, pass + 1, t);
+                const uint32_t rs = ntt_swz_base_e<LE>((uint32_t)(k * S::P + prow) << L, L, pass + 1, t);
 #pragma unroll
-                for (int r = 0; r < kNttE; ++r) a[k][r] = sm[rs ^ ntt_swz_reg(L, pass + 1, r)];
+                for (int r = 0; r < E; ++r) a[k][r] = sm[rs ^ ntt_swz_reg_e<LE>(L, pass + 1, r)];
             }
-            row_sync<L>();
+            row_sync<L, LE>();
         }
     }
     if (active) {
@@ -147,13 +157,12 @@ __global__ void __launch_bounds__(FwdShape<L, G>::THREADS, FwdShape<L, G>::MIN_B
         for (int k = 0; k < K; ++k) {
             const uint32_t pi = pi0 + k, p = pc.p[pi], one_s = pc.one_s[pi];
 #pragma unroll
-            for (int r = 0; r < kNttE; ++r) a[k][r] = ntt_fwd_final(a[k][r], one_s, p);
-            // the last pass holds slots 16 t .. 16 t + 15
-            uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * kNttE);
-            dst[0] = make_uint4(a[k][0], a[k][1], a[k][2], a[k][3]);
-            dst[1] = make_uint4(a[k][4], a[k][5], a[k][6], a[k][7]);
-            dst[2] = make_uint4(a[k][8], a[k][9], a[k][10], a[k][11]);
-            dst[3] = make_uint4(a[k][12], a[k][13], a[k][14], a[k][15]);
+            for (int r = 0; r < E; ++r) a[k][r] = ntt_fwd_final(a[k][r], one_s, p);
+            // the last pass holds slots E t .. E t + E - 1
+            uint4* dst = reinterpret_cast<uint4*>(jb.dst + ((poly * kPrimes + pi) << L) + t * E);
+#pragma unroll
+            for (int q = 0; q < E / 4; ++q)
+                dst[q] = make_uint4(a[k][4 * q], a[k][4 * q + 1], a[k][4 * q + 2], a[k][4 * q + 3]);
         }
     }
 }
@@ -656,29 +665,40 @@ __global__ void __launch_bounds__(kCrtThreads) crt_jobs_kernel(JobList<FinishJob
 }
 
 // ---------------------------------------------------------------- launch helpers
-template <int L, int G>
+template <int L, int G, int LE = kNttLogE>
 cudaError_t ntt_launch_LG(const DeviceTables& T, JobList<NttJob>& JL, NttJob* jobs, int n, cudaStream_t st) {
-    using S = FwdShape<L, G>;
+    using S = FwdShape<L, G, LE>;
     const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
         return ((uint64_t)(j.npolys + S::P - 1) / S::P) * kGroups;
     });
     if (!ctas) return cudaSuccess;
-    ntt_fwd_kernel<L, G><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.fwd, T.fwd_last);
+    ntt_fwd_kernel<L, G, LE><<<ctas, S::THREADS, S::SMEM, st>>>(JL, T.pc, T.fwd, T.fwd_last);
     return cudaGetLastError();
 }
 
 template <int L>
-cudaError_t ntt_launch_L(const DeviceTables& T, JobList<NttJob>& JL, NttJob* jobs, int n, cudaStream_t st, int group) {
+cudaError_t ntt_launch_L(const DeviceTables& T, JobList<NttJob>& JL, NttJob* jobs, int n, cudaStream_t st, int group,
+                         int elems) {
     if constexpr (L < 4) {
         const uint32_t ctas = assign_ctas<NttJob>(jobs, n, JL, [](const NttJob& j) -> uint64_t {
             return ((uint64_t)j.npolys * kPrimes + 127) / 128;
         });
         if (!ctas) return cudaSuccess;
         ntt_fwd_small_kernel<L><<<ctas, 128, 0, st>>>(JL, T.pc, T.fwd);
-    } else if constexpr (L < 10) {
-        return group == 32 ? ntt_launch_LG<L, 32>(T, JL, jobs, n, st) : ntt_launch_LG<L, 64>(T, JL, jobs, n, st);
     } else {
-        return ntt_launch_LG<L, 64>(T, JL, jobs, n, st);
+        if constexpr (L >= 5) {
+            if (elems == 32) {
+                if constexpr (L < 10)
+                    return group == 32 ? ntt_launch_LG<L, 32, 5>(T, JL, jobs, n, st)
+                                       : ntt_launch_LG<L, 64, 5>(T, JL, jobs, n, st);
+                else
+                    return ntt_launch_LG<L, 64, 5>(T, JL, jobs, n, st);
+            }
+        }
+        if constexpr (L < 10)
+            return group == 32 ? ntt_launch_LG<L, 32>(T, JL, jobs, n, st) : ntt_launch_LG<L, 64>(T, JL, jobs, n, st);
+        else
+            return ntt_launch_LG<L, 64>(T, JL, jobs, n, st);
     }
     return cudaGetLastError();
 }
@@ -774,11 +794,13 @@ void free_tables(DeviceTables* t) {
     t->fwd = t->inv = t->fwd_last = t->inv_last = nullptr;
 }
 
-cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group) {
+cudaError_t launch_ntt_jobs(const DeviceTables& T, NttJob* jobs, int n, uint32_t L, cudaStream_t st, int group,
+                            int elems) {
     if (n <= 0) return cudaSuccess;
-    if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing || (group != 32 && group != 64)) return cudaErrorInvalidValue;
+    if (n > kMaxJobs || L > (uint32_t)kLogMaxProverRing || (group != 32 && group != 64) || (elems != 16 && elems != 32))
+        return cudaErrorInvalidValue;
     JobList<NttJob> JL;
-#define DM_NTT_CALL(l) ntt_launch_L<l>(T, JL, jobs, n, st, group)
+#define DM_NTT_CALL(l) ntt_launch_L<l>(T, JL, jobs, n, st, group, elems)
     DM_DISPATCH_L(L, DM_NTT_CALL)
 #undef DM_NTT_CALL
     return cudaErrorInvalidValue;

@@ -148,7 +148,8 @@ int Plan::launch_all(Context* ctx, cudaStream_t st, std::string* err) {
                  for (size_t i = 0; i < ntt[L].size(); i += kMaxJobs) {
                      const int n = (int)std::min<size_t>(kMaxJobs, ntt[L].size() - i);
                      cudaError_t e = launch_ntt_jobs(T, ntt[L].data() + i, n, (uint32_t)L, st,
-                                                     ctx->tuning(kTuneNttGroup, (uint32_t)L));
+                                                     ctx->tuning(kTuneNttGroup, (uint32_t)L),
+                                                     ctx->tuning(kTuneNttRadix, (uint32_t)L));
                      if (e != cudaSuccess) return (int)e;
                      ++launches;
                  }

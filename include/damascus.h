@@ -342,7 +342,9 @@ enum {
     DAMASCUS_TUNE_MAC_SPLIT = 2,  /* the same for the split (vector-stage) MAC */
     DAMASCUS_TUNE_MAC_PLAIN = 3,  /* the same for the single-sum MAC */
     DAMASCUS_TUNE_SPLIT_COORDS = 4, /* commitment coordinates per thread of the split MAC: 1, 2, 4 or 8 */
-    DAMASCUS_TUNE_TRIPLE_COORDS = 5 /* the same for the triple MAC: 1, 2 or 4 */
+    DAMASCUS_TUNE_TRIPLE_COORDS = 5, /* the same for the triple MAC: 1, 2 or 4 */
+    DAMASCUS_TUNE_NTT_RADIX = 6      /* residues per thread of the forward transform, rings of 2^5 and up: 16 or 32
+                                        (radix-16 or radix-32 register passes) */
 };
 int damascus_tuning_set(damascus_ctx* ctx, int knob, uint32_t log_ring, int value);
 int damascus_tuning_get(damascus_ctx* ctx, int knob, uint32_t log_ring, int* value);

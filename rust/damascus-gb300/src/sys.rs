@@ -27,6 +27,7 @@ pub const DAMASCUS_TUNE_MAC_SPLIT: c_int = 2;
 pub const DAMASCUS_TUNE_MAC_PLAIN: c_int = 3;
 pub const DAMASCUS_TUNE_SPLIT_COORDS: c_int = 4;
 pub const DAMASCUS_TUNE_TRIPLE_COORDS: c_int = 5;
+pub const DAMASCUS_TUNE_NTT_RADIX: c_int = 6;
 
 /// Opaque handles (never constructed on the Rust side).
 #[repr(C)]

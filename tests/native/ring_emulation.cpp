@@ -1,6 +1,7 @@
 // Host emulation of the nine-prime ring pipeline exactly as the transform
 // kernels run it: the same device functions (dm_ntt.cuh, dm_field.cuh compiled
-// for the CPU), the register passes of 16 residues per thread, the swizzled
+// for the CPU), the register passes of 16 residues per thread (and of 32, the
+// forward transform's radix-32 alternative, checked against them), the swizzled
 // shared-memory exchanges, the last-pass twiddle order, the lazy value bounds,
 // the MAC, the even/odd cross terms, the inverse and the Garner CRT.  Results
 // are compared with schoolbook negacyclic products in Z_q for every ring size
@@ -104,6 +105,47 @@ std::vector<uint32_t> forward_row(const std::vector<fq>& x, int L, int pi) {
     return out;
 }
 
+// The same transform in the radix-2^LE pass shape of the forward kernel's
+// alternative (LE = 5: 32 residues per thread, 2^(L-5) threads per row, the
+// natural twiddle table in every pass), for L >= LE.
+template <int LE>
+std::vector<uint32_t> forward_row_e(const std::vector<fq>& x, int L, int pi) {
+    constexpr int E = 1 << LE;
+    const HostTables& T = host_tables();
+    const uint32_t p = T.pc.p[pi];
+    const Tw* tw = T.fwd.data() + (size_t)pi * kMaxRing;
+    const uint32_t s = 1u << L;
+    const uint32_t nt = s / E;
+    const int np = ntt_pass_count_e<LE>(L);
+    std::vector<std::vector<uint32_t>> R(nt, std::vector<uint32_t>(E));
+    std::vector<uint32_t> sm(2u * s, 0xFFFFFFFFu);
+    const uint32_t base = 1u << L;
+    for (uint32_t t = 0; t < nt; ++t)
+        for (int r = 0; r < E; ++r) R[t][r] = residue_fwd(x[ntt_place_e<LE>(L, 0, t, r)], T.pc, pi);
+    for (int pass = 0; pass < np; ++pass) {
+        for (uint32_t t = 0; t < nt; ++t) ntt_fwd_pass_e<LE>(R[t].data(), L, pass, t, tw, p);
+        for (uint32_t t = 0; t < nt; ++t)
+            for (int r = 0; r < E; ++r)
+                if ((uint64_t)R[t][r] >= 16ull * p) fail("radix-32 pass output bound 16p", L);
+        if (pass + 1 < np) {
+            for (uint32_t t = 0; t < nt; ++t)
+                for (int r = 0; r < E; ++r) {
+                    const uint32_t w = ntt_swz_base_e<LE>(base, L, pass, t) ^ ntt_swz_reg_e<LE>(L, pass, r);
+                    if (w != ntt_swz_e<LE>(base + ntt_place_e<LE>(L, pass, t, r)) || (w >> L) != 1)
+                        fail("radix-32 exchange word", L);
+                    sm[w] = R[t][r];
+                }
+            for (uint32_t t = 0; t < nt; ++t)
+                for (int r = 0; r < E; ++r)
+                    R[t][r] = sm[ntt_swz_base_e<LE>(base, L, pass + 1, t) ^ ntt_swz_reg_e<LE>(L, pass + 1, r)];
+        }
+    }
+    std::vector<uint32_t> out(s);
+    for (uint32_t t = 0; t < nt; ++t)
+        for (int r = 0; r < E; ++r) out[t * E + r] = ntt_fwd_final(R[t][r], T.pc.one_s[pi], p);
+    return out;
+}
+
 // Inverse of one row of reduced slots; mode 0 plain, 1 / 2 the even/odd cross
 // terms (twist by w_i or w_i^-1 and the extra 1/4), as the finish kernels do.
 std::vector<uint32_t> inverse_row(std::vector<uint32_t> in, int L, int pi, int mode) {
@@ -159,20 +201,21 @@ std::vector<fq> crt(const std::vector<std::vector<uint32_t>>& rows, uint32_t s) 
     return o;
 }
 
-// Bank check of every exchange for a block of `rows` rows of 2^(L-4) threads:
+// Bank check of every exchange for a block of `rows` rows of 2^(L-LE) threads:
 // for each warp and register, the 32 words stored (and loaded) sit in 32
 // different banks.
+template <int LE = kNttLogE>
 void check_banks(int L, int rows) {
-    const uint32_t T = 1u << (L - 4), threads = T * rows;
-    for (int pass = 0; pass + 1 < ntt_pass_count(L); ++pass)
+    const uint32_t T = 1u << (L - LE), threads = T * rows;
+    for (int pass = 0; pass + 1 < ntt_pass_count_e<LE>(L); ++pass)
         for (int dir = 0; dir < 2; ++dir)
             for (uint32_t w0 = 0; w0 < threads; w0 += 32)
-                for (int r = 0; r < kNttE; ++r) {
+                for (int r = 0; r < (1 << LE); ++r) {
                     uint32_t used = 0;
                     for (uint32_t lane = 0; lane < 32 && w0 + lane < threads; ++lane) {
                         const uint32_t th = w0 + lane, row = th / T, t = th % T;
                         const int ps = pass + dir;
-                        const uint32_t word = ntt_swz_base(row << L, L, ps, t) ^ ntt_swz_reg(L, ps, r);
+                        const uint32_t word = ntt_swz_base_e<LE>(row << L, L, ps, t) ^ ntt_swz_reg_e<LE>(L, ps, r);
                         used |= 1u << (word % 32);
                     }
                     const uint32_t lanes = threads - w0 < 32 ? threads - w0 : 32;
@@ -208,6 +251,8 @@ int main(int argc, char** argv) {
         for (int group : {64, 32}) {
             const int rows = (1 << (L - 4)) >= group ? 1 : group >> (L - 4);
             check_banks(L, rows);
+            const int rows5 = (1 << (L - 5)) >= group ? 1 : group >> (L - 5);
+            check_banks<5>(L, rows5);
         }
     for (int L = 0; L <= max_L; ++L) {
         const uint32_t s = 1u << L;
@@ -225,6 +270,8 @@ int main(int argc, char** argv) {
             for (uint32_t i = 0; i < s; ++i) want[i] = fq_add(want[i], c[i]);
             for (int pi = 0; pi < kPrimes; ++pi) {
                 const std::vector<uint32_t> A = forward_row(a, L, pi), B = forward_row(b, L, pi);
+                if (L >= 5 && (forward_row_e<5>(a, L, pi) != A || forward_row_e<5>(b, L, pi) != B))
+                    fail("radix-32 passes differ from radix-16", L);
                 for (uint32_t i = 0; i < s; ++i)
                     acc[pi][i] = red64((uint64_t)acc[pi][i] + (uint64_t)A[i] * B[i], T.pc, pi);
             }

@@ -396,3 +396,19 @@ def test_cuda_ntt_batch_dropin_cyclic_convolution(n):
         for k in idx:
             exp = sum(a[pi][i] * b[pi][(k - i) % n] for i in range(n)) % p
             assert out[pi][k] == exp, (pi, k)
+
+
+@pytest.mark.parametrize("n", [32, 64, 256, 512, 1024, 2048, 4096])
+def test_ring_mul_radix32_passes_match_oracle(oracle_lib, n):
+    """The forward transform's radix-32 register passes (DAMASCUS_TUNE_NTT_RADIX = 32)
+    give the same products as the oracle, including the all-(q-1) worst case."""
+    L = n.bit_length() - 1
+    rng = random.Random(1000 + n)
+    a = [rng.randrange(Q) for _ in range(2 * n)] + [Q - 1] * n
+    b = [rng.randrange(Q) for _ in range(2 * n)] + [Q - 1] * n
+    with D.Context(0, tuning=None) as c:
+        c.tuning_set(6, L, 32)
+        out = D.unfe_vec(c.ring_mul_batch(D.fe_vec(a), D.fe_vec(b), n, 3))
+    for i in range(3):
+        exp = oracle_lib.negacyclic_multiply(a[i * n:(i + 1) * n], b[i * n:(i + 1) * n])
+        assert out[i * n:(i + 1) * n] == exp, (n, i)

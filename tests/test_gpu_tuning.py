@@ -23,14 +23,16 @@ def test_tuning_set_get_and_validation():
         assert c.tuning_get(A.SPLIT_COORDS, 9) == 2
         for knob, L, v in [(A.NTT_GROUP, 6, 48), (A.MAC_TRIPLE, 6, 0), (A.MAC_PLAIN, 6, 33), (7, 6, 8),
                            (A.MAC_SPLIT, 14, 8), (A.SPLIT_COORDS, 9, 3), (A.SPLIT_COORDS, 9, 16),
-                           (A.TRIPLE_COORDS, 9, 8), (A.TRIPLE_COORDS, 9, 3)]:
+                           (A.TRIPLE_COORDS, 9, 8), (A.TRIPLE_COORDS, 9, 3), (A.NTT_RADIX, 9, 64),
+                           (A.NTT_RADIX, 9, 8)]:
             with pytest.raises(D.DamascusError):
                 c.tuning_set(knob, L, v)
 
 
 def test_tuning_measure_runs_every_knob():
     with D.Context(0, tuning=None) as c:
-        for knob in (A.NTT_GROUP, A.MAC_TRIPLE, A.MAC_SPLIT, A.MAC_PLAIN, A.SPLIT_COORDS, A.TRIPLE_COORDS):
+        for knob in (A.NTT_GROUP, A.MAC_TRIPLE, A.MAC_SPLIT, A.MAC_PLAIN, A.SPLIT_COORDS, A.TRIPLE_COORDS,
+                     A.NTT_RADIX):
             for v in A.CANDIDATES[knob][:2] + A.CANDIDATES[knob][-1:]:
                 ms = c.tuning_measure(knob, 6, v, A.work_size(knob, 6), reps=2)
                 assert 0.0 < ms < 1000.0
@@ -53,6 +55,7 @@ def test_proofs_identical_under_extreme_shapes(shape, coords, oracle_lib):
                 c.tuning_set(knob, L, {"small": 1, "large": 32, "mixed": 4}[shape])
             c.tuning_set(A.SPLIT_COORDS, L, coords or (1, 2, 4, 8)[L % 4])
             c.tuning_set(A.TRIPLE_COORDS, L, min(coords, 4) if coords else (1, 2, 4)[L % 3])
+            c.tuning_set(A.NTT_RADIX, L, 32 if shape != "mixed" else (16, 32)[L % 2])
         got = [c.prove(f, s, EPOCH) for f, s in files]
         with D.Engine(c, host_threads=4) as eng:
             via_engine = eng.prove_batch([(f, s, EPOCH) for f, s in files])

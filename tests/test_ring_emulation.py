@@ -7,7 +7,10 @@ bounds), the MAC, the even/odd cross terms and the Garner CRT, and compares
 with schoolbook negacyclic products in Z_q for ring sizes 1 .. 4096 (the
 reference's `negacyclic_multiply` contract, src/algebra/ntt.rs:112-195 and its
 test `negacyclic_multiply_across_runtime_sizes`, :509-521).  It also checks
-that each exchange is bank-conflict free for the kernels' block shapes.
+that each exchange is bank-conflict free for the kernels' block shapes, and
+that the forward transform's radix-32 pass shape (32 residues per thread, the
+alternative the autotuner may pick from 2^5 on) gives the same slots as the
+radix-16 one within the same lazy bounds.
 """
 import shutil
 import subprocess
