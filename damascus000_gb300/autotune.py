@@ -70,7 +70,7 @@ def ring_sizes(knob: int) -> List[int]:
     return list(range(4, 13))
 
 
-# the library's built-in values (the split's coordinates per thread: 4 from rings of 2^9 on); the autotuner
+# the library's built-in values (the split's coordinates per thread: 8 from rings of 2^9 on); the autotuner
 # reads them from a context made without a table
 DEFAULTS = {NTT_GROUP: 64, MAC_TRIPLE: 8, MAC_SPLIT: 8, MAC_PLAIN: 8, SPLIT_COORDS: 1, TRIPLE_COORDS: 1,
             NTT_RADIX: 16}

@@ -27,10 +27,10 @@ enum TuneKnob : int {
     kTuneKnobs = 7,
 };
 constexpr int kTuneDefault[kTuneKnobs] = {64, 8, 8, 8, 1, 1, 16};
-// Built-in value of a knob at ring 2^L: kTuneDefault, except four coordinates per
-// thread for the split MAC from rings of 2^9 on (measured 16-21 % faster there on
-// GB300, within noise below).
-constexpr int tune_default(int knob, int L) { return knob == kTuneSplitCoords && L >= 9 ? 4 : kTuneDefault[knob]; }
+// Built-in value of a knob at ring 2^L: kTuneDefault, except eight coordinates
+// per thread for the split MAC from rings of 2^9 on (measured 20-26 % faster than
+// one there on GB300, and 2-9 % faster than four; within noise below 2^9).
+constexpr int tune_default(int knob, int L) { return knob == kTuneSplitCoords && L >= 9 ? 8 : kTuneDefault[knob]; }
 static_assert((uint64_t)kMaxMacParts * ((1u << 28) - 1) < (1ull << 32), "part sums fit 32 bits");
 
 // ---- forward NTT: coefficients [npolys][2^L] -> residues [npolys][9][2^L] ----

@@ -18,7 +18,7 @@ def test_tuning_set_get_and_validation():
         c.tuning_set(A.NTT_GROUP, 6, 32)
         c.tuning_set(A.MAC_SPLIT, 9, 24)
         assert c.tuning_get(A.NTT_GROUP, 6) == 32 and c.tuning_get(A.MAC_SPLIT, 9) == 24
-        assert c.tuning_get(A.SPLIT_COORDS, 8) == 1 and c.tuning_get(A.SPLIT_COORDS, 9) == 4
+        assert c.tuning_get(A.SPLIT_COORDS, 8) == 1 and c.tuning_get(A.SPLIT_COORDS, 9) == 8
         c.tuning_set(A.SPLIT_COORDS, 9, 2)
         assert c.tuning_get(A.SPLIT_COORDS, 9) == 2
         for knob, L, v in [(A.NTT_GROUP, 6, 48), (A.MAC_TRIPLE, 6, 0), (A.MAC_PLAIN, 6, 33), (7, 6, 8),
