@@ -265,9 +265,17 @@ DM_D void triple_rows(const MacJobX& jb, uint32_t kg, uint32_t pi, uint32_t part
     for (int j = 0; j < KC; ++j)
 #pragma unroll
         for (int q = 0; q < NS; ++q) lo[j][q] = 0, hi[j][q] = 0;
-    // products below 2^56: a block sum of 16 (pair) or 8 (full: two products per sum) fits 64 bits
-    constexpr uint32_t kBlock = PAIR ? 16 : 8;
-    constexpr int kUnroll = KC >= 4 ? 2 : (KC == 2 ? 2 : 4);
+    // products below 2^56: a block sum of up to 256 of them fits 64 bits; a block of
+    // 16 columns sums 16 (pair) or 32 (full: two products per sum)
+#ifndef DM_TRIPLE_FULL_BLOCK
+#define DM_TRIPLE_FULL_BLOCK 8
+#endif
+#ifndef DM_TRIPLE_UNROLL1
+#define DM_TRIPLE_UNROLL1 4
+#endif
+    constexpr uint32_t kBlock = PAIR ? 16 : DM_TRIPLE_FULL_BLOCK;
+    static_assert(DM_TRIPLE_FULL_BLOCK <= 64, "block sums of 2 x 64 products below 2^56 fit 64 bits");
+    constexpr int kUnroll = KC >= 4 ? 2 : (KC == 2 ? 2 : DM_TRIPLE_UNROLL1);
     uint32_t i = i0;
     while (i < i1) {
         const uint32_t e = i + kBlock < i1 ? i + kBlock : i1;
