@@ -596,7 +596,7 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
     Scratch a, b, part;
     std::function<cudaError_t()> launch;
     NttJob nj{};
-    MacJobX mj{};
+    MacJobX mj{}, mj_pair{};
     if (knob == kTuneNttGroup || knob == kTuneNttRadix) {
         // count polynomials of arbitrary 128-bit words -> nine residue rows each
         if (a.alloc(C, count * s * 16) || b.alloc(C, count * kPrimes * s * 4))
@@ -628,8 +628,13 @@ int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int 
         const uint64_t ps = (uint64_t)parts * rows * s;
         mj = MacJobX{a.m.as<uint32_t>(), b.m.as<uint32_t>(), P, P + ps, P + 2 * ps, 0, 0, count, parts, 0, 0, L,
                      (split || triple) ? kc : 0u};
-        if (triple)
-            launch = [&] { return launch_mac_triple_jobs(T, &mj, 1, st); };
+        mj_pair = mj;
+        mj_pair.pair = count;  // the witness's columns from `count` on are zero: read at i only
+        if (triple)  // both forms a proof runs: full pairs, then the known-zero-half form
+            launch = [&] {
+                cudaError_t r = launch_mac_triple_jobs(T, &mj, 1, st);
+                return r == cudaSuccess ? launch_mac_triple_jobs(T, &mj_pair, 1, st) : r;
+            };
         else
             launch = [&, split] { return launch_mac_jobs(T, &mj, 1, split, st); };
     }

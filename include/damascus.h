@@ -351,7 +351,8 @@ int damascus_tuning_get(damascus_ctx* ctx, int knob, uint32_t log_ring, int* val
 /* Mean device time of one launch over `reps` launches (CUDA events, context
  * stream, after one warm-up launch) of the knob's kernel with `value`, on
  * synthetic device data: `count` polynomials (transform), column pairs (triple
- * MAC) or columns (split, single-sum MAC). */
+ * MAC: one launch over full pairs plus one in the form whose second witness
+ * half is known zero, both timed) or columns (split, single-sum MAC). */
 int damascus_tuning_measure(damascus_ctx* ctx, int knob, uint32_t log_ring, int value, uint32_t count, int reps,
                             double* ms_per_launch);
 
