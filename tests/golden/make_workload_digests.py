@@ -14,6 +14,8 @@ Sets (files from damascus000_gb300.synth, master seed 0xDA3A5C05 as bench.py):
   d12      the statement (com_0) and round-0 record of a 58.7 MB file (d = 12,
            4096 x 4096 witness, rings of 2^12): the nine-prime CRT range of the
            GPU path against the reference's per-product CRT
+  d13      the same for a 218 MB file (d = 13, 8192 x 8192 witness, rings of
+           2^13, the deepest the library proves; the oracle needs about an hour)
 
 Resumable: entries already in the JSON with the same file length are kept.
 Every entry records the SHA-256 of the whole proof
@@ -39,6 +41,7 @@ MASTER_SEED = 0xDA3A5C05
 EPOCH = bytes([11]) * 32
 SYSTEM_SEED = bytes([7]) * 32
 D12_FILE = dict(master_seed=12, length=2048 * 2048 * 13 + 4096 * 1024, index=0)
+D13_FILE = dict(master_seed=13, length=4096 * 4096 * 13 + 1, index=0)
 
 
 def statement_len(vector_len: int, ring_len: int) -> int:
@@ -74,15 +77,16 @@ def file_set(name: str):
     return [((d, s), {"index": i}) for i, (d, s, _) in enumerate(files)]
 
 
-def d12_entry(threads: int):
-    data, seed = synth.random_file(D12_FILE["master_seed"], D12_FILE["length"], D12_FILE["index"])
+def deep_entry(spec, depth: int, threads: int):
+    """Statement, round-0 record and the commitment after round 0 of one deep file."""
+    data, seed = synth.random_file(spec["master_seed"], spec["length"], spec["index"])
     t0 = time.time()
-    p = O.Prover(data, seed, EPOCH, use_ntt=True, threads=threads)
+    p = O.Prover(data, seed, EPOCH, max_preprocess=1 << 40, use_ntt=True, threads=threads)
     stmt = p.statement()
     rec0 = p.fold_round(0)
     com1 = p.current_commitment()
     N, n = p.dims()
-    return dict(D12_FILE, depth=12, seed_generators=seed.hex(),
+    return dict(spec, depth=depth, seed_generators=seed.hex(),
                 statement_sha256=hashlib.sha256(stmt).hexdigest(), statement_len=len(stmt),
                 round0_record_sha256=hashlib.sha256(rec0).hexdigest(), round0_record_len=len(rec0),
                 commitment_after_round0_sha256=hashlib.sha256(com1).hexdigest(), dims_after_round0=[N, n],
@@ -106,11 +110,11 @@ def main():
     out.update({"master_seed": MASTER_SEED, "epoch_seed": EPOCH.hex(), "system_seed": SYSTEM_SEED.hex(),
                 "generator": "tests/golden/make_workload_digests.py (CPU oracle, oracle/damascus_oracle.c)"})
     for name in args.sets.split(","):
-        if name == "d12":
-            if "d12" not in out:
-                out["d12"] = d12_entry(threads)
+        if name in ("d12", "d13"):
+            if name not in out:
+                out[name] = deep_entry(D12_FILE if name == "d12" else D13_FILE, int(name[1:]), threads)
                 save(out)
-                print("d12", out["d12"]["oracle_s"], "s", flush=True)
+                print(name, out[name]["oracle_s"], "s", flush=True)
             continue
         have = out.setdefault(name, [])
         for k, ((data, seed), extra) in enumerate(file_set(name)):
