@@ -58,6 +58,7 @@ WORKLOADS = {
                     desc="batched: 64 files log-uniform 50KB-4MiB (d 6-10), one engine batch"),
     "d6": dict(kind="plain", file_bytes=53_248, desc="plain full flow d=6: 53,248 random bytes, 64x64 witness"),
     "d9": dict(kind="plain", file_bytes=1 << 20, desc="plain full flow d=9: 1 MiB random file, 512x512 witness"),
+    "d10": dict(kind="plain", file_bytes=4 << 20, desc="plain full flow d=10: 4 MiB random file, 1024x1024 witness"),
     "d11": dict(kind="plain", file_bytes=16 << 20, desc="plain full flow d=11: 16 MiB random file, 2048x2048 witness"),
     "ringmul": dict(kind="ringmul", pairs=4096, n=512,
                     desc="ring-mult microbench: 4,096 random degree-512 R_q pairs per step"),
