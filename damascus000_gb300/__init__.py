@@ -51,6 +51,7 @@ EXPORTED_SYMBOLS = (
     "damascus_prover_new", "damascus_prover_free", "damascus_prover_rounds_total",
     "damascus_prover_current_round", "damascus_prover_dimensions", "damascus_prover_statement",
     "damascus_prover_current_commitment", "damascus_prover_fold_round", "damascus_prover_final_opening",
+    "damascus_prover_fold_round_timed",
     "damascus_prove", "damascus_prove_device", "damascus_prove_device_timed", "damascus_ctx_flush_l2",
     "damascus_verifier_new", "damascus_verifier_free", "damascus_verifier_update_commitment",
     "damascus_verifier_verify_final_opening", "damascus_verifier_round", "damascus_verifier_dimensions",
@@ -142,6 +143,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_prover_statement", i32, vp, vp, sz, P(sz))
     sig("damascus_prover_current_commitment", i32, vp, vp, sz, P(sz))
     sig("damascus_prover_fold_round", i32, vp, u64, vp, sz, P(sz))
+    sig("damascus_prover_fold_round_timed", i32, vp, u64, vp, sz, P(sz), P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double))
     sig("damascus_prover_final_opening", i32, vp, vp)
     sig("damascus_prove", i32, vp, cp, sz, cp, cp, vp, sz, P(sz))
     sig("damascus_prove_device", i32, vp, vp, sz, cp, cp, vp, sz, P(sz))
@@ -560,6 +562,20 @@ class DamascusProver:
         self._ctx.check(self._lib.damascus_prover_fold_round(self._h, rnd, buf, cap, ctypes.byref(ln)),
                         f"fold_round({rnd})")
         return buf.raw[:ln.value]
+
+    def fold_round_timed(self, rnd: int):
+        """fold_round plus the reference's RoundOutput timings
+        (src/protocol/prover.rs:26-31): (record, {"vector_fold_ms",
+        "poly_fold_ms", "total_round_ms"})."""
+        N, n = self.current_dimensions()
+        cap = record_size(N, max(n // 2, 1))
+        buf = ctypes.create_string_buffer(cap)
+        ln = ctypes.c_size_t()
+        t = [ctypes.c_double() for _ in range(3)]
+        self._ctx.check(self._lib.damascus_prover_fold_round_timed(
+            self._h, rnd, buf, cap, ctypes.byref(ln), *(ctypes.byref(x) for x in t)), f"fold_round({rnd})")
+        return buf.raw[:ln.value], {"vector_fold_ms": t[0].value, "poly_fold_ms": t[1].value,
+                                    "total_round_ms": t[2].value}
 
     def final_opening(self) -> Optional[bytes]:
         out = ctypes.create_string_buffer(16)

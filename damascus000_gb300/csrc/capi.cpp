@@ -442,18 +442,33 @@ int damascus_prover_current_commitment(const damascus_prover* p, uint8_t* buf, s
     return DAMASCUS_OK;
 }
 
-int damascus_prover_fold_round(damascus_prover* p, uint64_t round, uint8_t* record_out, size_t cap,
-                               size_t* record_len) {
+int damascus_prover_fold_round_timed(damascus_prover* p, uint64_t round, uint8_t* record_out, size_t cap,
+                                     size_t* record_len, double* vector_ms, double* poly_ms, double* total_ms) {
     if (!p) return DAMASCUS_EINVAL;
+    // the record's size is known before the round runs: a small buffer fails
+    // without advancing the prover, so the caller can retry
+    const uint32_t n = p->p->ring_len();
+    const size_t need = record_encoded_size(n, n > 1 ? n / 2 : 1);
+    if (record_len) *record_len = need;
+    if (!record_out || cap < need) return set_err(p->owner, DAMASCUS_ESIZE, "record buffer too small");
     RoundRecord rec;
-    int rc = p->p->fold_round(round, &rec);
+    double t[3] = {0, 0, 0};
+    int rc = p->p->fold_round(round, &rec, t);
     if (rc != kOk) return rc;
     std::vector<uint8_t> v;
     encode_record(v, rec);
     if (record_len) *record_len = v.size();
-    if (!record_out || cap < v.size()) return set_err(p->owner, DAMASCUS_ESIZE, "record buffer too small");
+    if (v.size() > cap) return set_err(p->owner, DAMASCUS_ESIZE, "record larger than its computed size");
     std::memcpy(record_out, v.data(), v.size());
+    if (vector_ms) *vector_ms = t[0];
+    if (poly_ms) *poly_ms = t[1];
+    if (total_ms) *total_ms = t[2];
     return DAMASCUS_OK;
+}
+
+int damascus_prover_fold_round(damascus_prover* p, uint64_t round, uint8_t* record_out, size_t cap,
+                               size_t* record_len) {
+    return damascus_prover_fold_round_timed(p, round, record_out, cap, record_len, nullptr, nullptr, nullptr);
 }
 
 int damascus_prover_final_opening(const damascus_prover* p, uint8_t out[16]) {

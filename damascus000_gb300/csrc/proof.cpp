@@ -1,5 +1,7 @@
 #include "proof.h"
 
+#include <chrono>
+
 #include <cstring>
 
 #include "host_blake3.h"
@@ -607,15 +609,24 @@ int GpuProver::run_stage() {
     return kOk;
 }
 
-int GpuProver::fold_round(uint64_t j, RoundRecord* out) {
+int GpuProver::fold_round(uint64_t j, RoundRecord* out, double times_ms[3]) {
     if (failed_) return fail(kEState, "prover is in a failed state");
     if (j != ps_.round()) return fail(kEState, "round index mismatch");
     if (ps_.stage() != Stage::Vec) return fail(kEState, "all rounds have finished");
+    using Clk = std::chrono::steady_clock;
+    const Clk::time_point t0 = Clk::now();
     int rc = run_stage();  // vector stage
     if (rc != kOk) return rc;
+    const Clk::time_point t1 = Clk::now();
     rc = run_stage();  // poly stage
     if (rc != kOk) return rc;
+    const Clk::time_point t2 = Clk::now();
     if (out) *out = ps_.records().back();
+    if (times_ms) {
+        times_ms[0] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        times_ms[1] = std::chrono::duration<double, std::milli>(t2 - t1).count();
+        times_ms[2] = std::chrono::duration<double, std::milli>(t2 - t0).count();
+    }
     return kOk;
 }
 

@@ -134,7 +134,10 @@ class GpuProver {
     // file is a host pointer, or a device pointer when on_device.
     int init(const uint8_t* file, uint64_t len, bool on_device, const uint8_t seed_generators[32],
              const uint8_t epoch_seed[32], uint64_t max_preprocess_bytes);
-    int fold_round(uint64_t round_idx, RoundRecord* out);
+    // times_ms (optional): wall time of the vector stage, the polynomial stage
+    // and the whole round, as RoundOutput's vector_fold_time / poly_fold_time /
+    // total_round_time (src/protocol/prover.rs:26-31)
+    int fold_round(uint64_t round_idx, RoundRecord* out, double times_ms[3] = nullptr);
     bool final_opening(fq* out) const { return ps_.opening(out); }
     const Statement& statement() const { return ps_.statement(); }
     uint32_t rounds_total() const { return ps_.depth(); }

@@ -144,9 +144,16 @@ void damascus_prover_dimensions(const damascus_prover* p, uint64_t* vector_len, 
 int damascus_prover_statement(const damascus_prover* p, uint8_t* buf, size_t cap, size_t* len);
 /* current_commitment() as 8 x n field elements (prover.rs:121-123) */
 int damascus_prover_current_commitment(const damascus_prover* p, uint8_t* buf, size_t cap, size_t* len);
-/* fold_round(round) (prover.rs:140-313): writes bincode(RoundRecord). */
+/* fold_round(round) (prover.rs:140-313): writes bincode(RoundRecord).  A buffer
+ * smaller than damascus_record_size(ring_len, ring_len / 2) fails with
+ * DAMASCUS_ESIZE (and *record_len = the size needed) before the round runs. */
 int damascus_prover_fold_round(damascus_prover* p, uint64_t round, uint8_t* record_out, size_t cap,
                                size_t* record_len);
+/* The same, also returning RoundOutput's timings (prover.rs:26-31): the wall
+ * time of the vector-fold stage, of the polynomial-fold stage and of the whole
+ * round, in milliseconds (any may be null). */
+int damascus_prover_fold_round_timed(damascus_prover* p, uint64_t round, uint8_t* record_out, size_t cap,
+                                     size_t* record_len, double* vector_ms, double* poly_ms, double* total_ms);
 /* final_opening (prover.rs:133-138); DAMASCUS_ESTATE before the last round. */
 int damascus_prover_final_opening(const damascus_prover* p, uint8_t out[16]);
 

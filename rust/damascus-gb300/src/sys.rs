@@ -89,6 +89,7 @@ extern "C" {
     pub fn damascus_prover_statement(p: *const Prover, buf: *mut u8, cap: usize, len: *mut usize) -> c_int;
     pub fn damascus_prover_current_commitment(p: *const Prover, buf: *mut u8, cap: usize, len: *mut usize) -> c_int;
     pub fn damascus_prover_fold_round(p: *mut Prover, round: u64, record_out: *mut u8, cap: usize, record_len: *mut usize) -> c_int;
+    pub fn damascus_prover_fold_round_timed(p: *mut Prover, round: u64, record_out: *mut u8, cap: usize, record_len: *mut usize, vector_ms: *mut f64, poly_ms: *mut f64, total_ms: *mut f64) -> c_int;
     pub fn damascus_prover_final_opening(p: *const Prover, out: *mut u8) -> c_int;
     pub fn damascus_prove(ctx: *mut Ctx, file: *const u8, len: usize, seed_generators: *const u8, epoch_seed: *const u8, proof_out: *mut u8, cap: usize, proof_len: *mut usize) -> c_int;
     pub fn damascus_prove_device(ctx: *mut Ctx, d_file: *const c_void, len: usize, seed_generators: *const u8, epoch_seed: *const u8, proof_out: *mut u8, cap: usize, proof_len: *mut usize) -> c_int;

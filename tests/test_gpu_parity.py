@@ -1,6 +1,7 @@
 """GPU parity: every kernel-level and protocol-level output of the sm_103a
 library against the CPU oracle, bit-exact (integer work has no tolerance).
 Calls go through the C ABI (ctypes)."""
+import ctypes
 import hashlib
 import json
 import random
@@ -256,6 +257,31 @@ def test_round_index_mismatch_and_early_opening(ctx):
     with pytest.raises(D.DamascusError) as e:
         p.fold_round(1)
     assert e.value.code == D.ESTATE
+
+
+def test_timed_round_and_small_record_buffer(ctx, oracle_lib):
+    """fold_round_timed returns the same records as the oracle plus RoundOutput's
+    three timings (src/protocol/prover.rs:26-31); a record buffer one byte short
+    fails with ESIZE before the round runs, so the same round can be retried."""
+    data, seed = synth.random_file(31, byte_len_for_depth(7), 0)
+    op = oracle_lib.Prover(data, seed, EPOCH)
+    gp = D.DamascusProver(ctx, data, seed, EPOCH)
+    try:
+        assert gp.statement() == op.statement()
+        lib = gp._lib
+        for r in range(op.rounds_total):
+            want = op.fold_round(r)
+            short = ctypes.create_string_buffer(len(want) - 1)
+            need = ctypes.c_size_t()
+            assert lib.damascus_prover_fold_round(gp._h, r, short, len(want) - 1, ctypes.byref(need)) == D.ESIZE
+            assert need.value == len(want)
+            rec, t = gp.fold_round_timed(r)
+            assert rec == want, r
+            assert t["vector_fold_ms"] > 0 and t["poly_fold_ms"] > 0
+            assert t["total_round_ms"] >= t["vector_fold_ms"] + t["poly_fold_ms"] - 1e-6
+        assert gp.final_opening() == op.final_opening()
+    finally:
+        gp.close()
 
 
 def test_default_memory_limit_rejects_depth13_on_every_file_path(ctx):
