@@ -236,6 +236,22 @@ impl<'c> Prover<'c> {
         Ok(out)
     }
 
+    /// `fold_round` with `RoundOutput`'s timings (src/protocol/prover.rs:26-31):
+    /// the record and the vector-fold, poly-fold and whole-round wall times.
+    pub fn fold_round_timed(&mut self, round: u64) -> Result<(Vec<u8>, [std::time::Duration; 3])> {
+        let (nv, np) = self.current_dimensions();
+        let cap = unsafe { sys::damascus_record_size(nv, (np / 2).max(1)) };
+        let mut out = vec![0u8; cap];
+        let mut len = 0usize;
+        let mut ms = [0f64; 3];
+        let [v, p, t] = &mut ms;
+        self.ctx.check(unsafe {
+            sys::damascus_prover_fold_round_timed(self.raw, round, out.as_mut_ptr(), cap, &mut len, v, p, t)
+        })?;
+        out.truncate(len);
+        Ok((out, ms.map(|x| std::time::Duration::from_secs_f64(x / 1000.0))))
+    }
+
     /// The terminal opening m* (16-byte LE) once every round has run.
     pub fn final_opening(&self) -> Result<[u8; 16]> {
         let mut out = [0u8; 16];
