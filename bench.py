@@ -938,6 +938,9 @@ def run_gpu(args, wl):
                                 "launches_per_step": (st1["launches"] - st0["launches"]) / args.steps,
                                 "gpu_idle_ms_per_step": (st1["gpu_idle_ms"] - st0["gpu_idle_ms"]) / args.steps,
                                 "host_stage_ms_per_step": (st1["host_stage_ms"] - st0["host_stage_ms"]) / args.steps,
+                                "scheduler_ms_per_step": {
+                                    "admit": (st1["admit_ms"] - st0["admit_ms"]) / args.steps,
+                                    "plan_and_launch": (st1["launch_ms"] - st0["launch_ms"]) / args.steps},
                                 "generator_cache": ctx.generator_cache_stats() if wl.get("generator_cache") else None},
                      "e2e": {"value": world * total / MIB / e2e_s, "unit": UNIT, "h2d_bytes_per_step": total,
                              "d2h_bytes_per_step": d2h},

@@ -48,6 +48,7 @@ EXPORTED_SYMBOLS = (
     "damascus_proof_size", "damascus_record_size", "damascus_statement_size", "damascus_prover_footprint",
     "damascus_file_id", "damascus_derive_generators", "damascus_commit_with_generators", "damascus_commit",
     "damascus_ring_mul_batch", "damascus_ring_mul_batch_device", "damascus_engine_profile",
+    "damascus_engine_scheduler_profile",
     "damascus_prover_new", "damascus_prover_free", "damascus_prover_rounds_total",
     "damascus_prover_current_round", "damascus_prover_dimensions", "damascus_prover_statement",
     "damascus_prover_current_commitment", "damascus_prover_fold_round", "damascus_prover_final_opening",
@@ -178,6 +179,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_drain", i32, vp)
     sig("damascus_engine_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64))
     sig("damascus_engine_profile", i32, vp, P(ctypes.c_double), P(ctypes.c_double))
+    sig("damascus_engine_scheduler_profile", i32, vp, P(ctypes.c_double), P(ctypes.c_double))
     sig("damascus_tuning_set", i32, vp, i32, u32, i32)
     sig("damascus_tuning_get", i32, vp, i32, u32, P(i32))
     sig("damascus_tuning_measure", i32, vp, i32, u32, i32, u32, i32, P(ctypes.c_double))
@@ -729,6 +731,9 @@ class Engine:
         h, i = ctypes.c_double(), ctypes.c_double()
         self._ctx.check(self._lib.damascus_engine_profile(self._h, ctypes.byref(h), ctypes.byref(i)), "engine profile")
         out.update(host_stage_ms=h.value, gpu_idle_ms=i.value)
+        self._ctx.check(self._lib.damascus_engine_scheduler_profile(self._h, ctypes.byref(h), ctypes.byref(i)),
+                        "engine scheduler profile")
+        out.update(admit_ms=h.value, launch_ms=i.value)
         return out
 
     def prove_batch(self, items) -> list:

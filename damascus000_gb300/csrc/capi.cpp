@@ -865,6 +865,14 @@ int damascus_engine_profile(damascus_engine* e, double* host_stage_ms, double* g
     return DAMASCUS_OK;
 }
 
+int damascus_engine_scheduler_profile(damascus_engine* e, double* admit_ms, double* launch_ms) {
+    if (!e) return DAMASCUS_EINVAL;
+    const EngineStats s = e->e->stats();
+    if (admit_ms) *admit_ms = s.admit_ms;
+    if (launch_ms) *launch_ms = s.launch_ms;
+    return DAMASCUS_OK;
+}
+
 // ------------------------------------------------------------------ verifier service
 int damascus_verify_service_create(damascus_ctx* ctx, int workers, uint64_t cache_bytes,
                                    damascus_verify_service** out) {

@@ -202,9 +202,12 @@ void Engine::scheduler() {
             queued_.pop_front();
             lk.unlock();
             const bool dev = r->device_file != nullptr;
+            const Clock::time_point t_admit = Clock::now();
             const int rc = r->ps->setup(dev ? r->device_file : r->pinned_file, r->len, dev, r->seed, r->epoch,
                                         ctx_->max_preprocess(), stream_);
+            const double admit_ms = std::chrono::duration<double, std::milli>(Clock::now() - t_admit).count();
             lk.lock();
+            stats_.admit_ms += admit_ms;
             if (rc != kOk) {
                 r->err = r->ps->error();
                 r->err_code = rc;
@@ -272,6 +275,7 @@ void Engine::launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock
         if (now > from) stats_.gpu_idle_ms += std::chrono::duration<double, std::milli>(now - from).count();
     }
     lk.unlock();
+    const Clock::time_point t_launch = Clock::now();
     cudaStream_t ws = wave_streams_[si];
     // admissions (allocations, file copies) on stream_ precede the wave's kernels
     cudaEventRecord(admit_ev_, stream_);
@@ -282,7 +286,9 @@ void Engine::launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock
     const int n = plan.launch(ctx_, ws, &err);
     cudaError_t e = cudaSuccess;
     if (n >= 0) e = cudaLaunchHostFunc(ws, on_wave_done, w);
+    const double launch_ms = std::chrono::duration<double, std::milli>(Clock::now() - t_launch).count();
     lk.lock();
+    stats_.launch_ms += launch_ms;
     if (n < 0 || e != cudaSuccess) {
         if (--inflight_waves_ == 0) idle_since_ = Clock::now();
         wave_stream_busy_[si] = false;

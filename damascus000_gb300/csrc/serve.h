@@ -34,6 +34,8 @@ struct EngineStats {
     uint64_t peak_reserved = 0;
     double host_stage_ms = 0;  // summed time of the host part of stages (all workers)
     double gpu_idle_ms = 0;    // wall time with no wave in flight while requests were admitted
+    double admit_ms = 0;       // scheduler thread: admitting requests (setup, Init stage launches)
+    double launch_ms = 0;      // scheduler thread: planning and launching stage waves
     uint64_t cancelled = 0, timed_out = 0;
 };
 

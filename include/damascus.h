@@ -240,6 +240,9 @@ int damascus_engine_stats(damascus_engine* e, uint64_t* completed, uint64_t* fai
  * (all workers), and wall time with no stage wave on the GPU while admitted
  * requests were unfinished. */
 int damascus_engine_profile(damascus_engine* e, double* host_stage_ms, double* gpu_idle_ms);
+/* The scheduler thread's busy time: admitting requests (setup and their Init
+ * stage launches) and planning and launching stage waves, in milliseconds. */
+int damascus_engine_scheduler_profile(damascus_engine* e, double* admit_ms, double* launch_ms);
 
 /* Streaming verifier service (no counterpart in the reference, which verifies
  * one proof at a time through DamascusVerifier, src/protocol/verifier.rs:22-134).

@@ -114,6 +114,7 @@ def test_engine_many_small_requests_and_profile(ctx):
         st = eng.stats()
     assert st["completed"] == 120 and st["failed"] == 0
     assert st["host_stage_ms"] > 0 and st["gpu_idle_ms"] >= 0
+    assert st["admit_ms"] > 0 and st["launch_ms"] > 0  # the scheduler thread admitted and launched
     assert st["launches"] > st["waves"] > 0
     for p in proofs:
         assert ctx.verify(p, EPOCH)
