@@ -15,7 +15,7 @@ Sets (files from damascus000_gb300.synth, master seed 0xDA3A5C05 as bench.py):
            4096 x 4096 witness, rings of 2^12): the nine-prime CRT range of the
            GPU path against the reference's per-product CRT
   d13      the same for a 218 MB file (d = 13, 8192 x 8192 witness, rings of
-           2^13, the deepest the library proves; the oracle needs about an hour)
+           2^13, the deepest the library proves; 30 min of the oracle on 8 cores)
 
 Resumable: entries already in the JSON with the same file length are kept.
 Every entry records the SHA-256 of the whole proof

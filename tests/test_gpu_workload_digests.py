@@ -11,11 +11,11 @@ path's proofs with those digests:
 * the 64-file batched set, d 6-10, through the engine in one batch;
 * the 96-request serving stream, d 6-11, through the engine, with per-file
   seeds and under one system seed with the provers' generator cache;
-* d = 12: the statement (com_0), the round-0 record and the commitment after
-  round 0 of a 58.7 MB file, rings of 2^12: the GPU path sums each commitment
-  coordinate in the NTT domain over nine 28-bit primes and reconstructs it once,
-  where the reference reconstructs every product separately
-  (src/algebra/ntt.rs:372-427).
+* d = 12 and d = 13: the statement (com_0), the round-0 record and the
+  commitment after round 0 of a 58.7 MB and a 218 MB file, rings of 2^12 and
+  2^13: the GPU path sums each commitment coordinate in the NTT domain over nine
+  28-bit primes and reconstructs it once, where the reference reconstructs
+  every product separately (src/algebra/ntt.rs:372-427).
 """
 import hashlib
 import json
@@ -97,11 +97,14 @@ def test_serving_stream_system_seed_with_generator_cache_matches_oracle():
     check(DIGESTS["serving_system_seed"], second, files)
 
 
-def test_d12_statement_and_round0_match_oracle(ctx):
-    e = DIGESTS["d12"]
+@pytest.mark.parametrize("depth", [12, 13])
+def test_deep_statement_and_round0_match_oracle(ctx, depth):
+    """d = 12 (58.7 MB, rings of 2^12) and d = 13 (218 MB, rings of 2^13, the
+    deepest supported: its 2 GiB expansion needs the limit raised)."""
+    e = DIGESTS[f"d{depth}"]
     data, seed = synth.random_file(e["master_seed"], e["length"], e["index"])
-    assert D.layout_for_byte_len(len(data))[0] == 12 and seed.hex() == e["seed_generators"]
-    p = D.DamascusProver(ctx, data, seed, EPOCH)  # 512 MiB estimate: inside the default limit
+    assert D.layout_for_byte_len(len(data))[0] == depth and seed.hex() == e["seed_generators"]
+    p = D.DamascusProver(ctx, data, seed, EPOCH, max_preprocess_bytes=4 << 30)
     try:
         stmt = p.statement()
         assert len(stmt) == e["statement_len"] and sha(stmt) == e["statement_sha256"]
