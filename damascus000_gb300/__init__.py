@@ -48,7 +48,7 @@ EXPORTED_SYMBOLS = (
     "damascus_proof_size", "damascus_record_size", "damascus_statement_size", "damascus_prover_footprint",
     "damascus_file_id", "damascus_derive_generators", "damascus_commit_with_generators", "damascus_commit",
     "damascus_ring_mul_batch", "damascus_ring_mul_batch_device", "damascus_engine_profile",
-    "damascus_engine_scheduler_profile",
+    "damascus_engine_scheduler_profile", "damascus_ctx_trace_start", "damascus_ctx_trace_read",
     "damascus_prover_new", "damascus_prover_free", "damascus_prover_rounds_total",
     "damascus_prover_current_round", "damascus_prover_dimensions", "damascus_prover_statement",
     "damascus_prover_current_commitment", "damascus_prover_fold_round", "damascus_prover_final_opening",
@@ -180,6 +180,8 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64))
     sig("damascus_engine_profile", i32, vp, P(ctypes.c_double), P(ctypes.c_double))
     sig("damascus_engine_scheduler_profile", i32, vp, P(ctypes.c_double), P(ctypes.c_double))
+    sig("damascus_ctx_trace_start", i32, vp)
+    sig("damascus_ctx_trace_read", i32, vp, vp, sz, P(sz), i32)
     sig("damascus_tuning_set", i32, vp, i32, u32, i32)
     sig("damascus_tuning_get", i32, vp, i32, u32, P(i32))
     sig("damascus_tuning_measure", i32, vp, i32, u32, i32, u32, i32, P(ctypes.c_double))
@@ -404,6 +406,26 @@ class Context:
 
     def reset_stats(self) -> None:
         self._lib.damascus_ctx_reset_stats(self._h)
+
+    def trace_start(self) -> None:
+        """Keeps every timed launch group from here on (turns profiling on)."""
+        self.check(self._lib.damascus_ctx_trace_start(self._h), "trace_start")
+
+    def trace_read(self, stop: bool = True):
+        """[(kind, stream, start_ms, end_ms, algorithmic_bytes, kernels)] since
+        trace_start() or the last read; stop ends the trace."""
+        ln = ctypes.c_size_t()
+        rc = self._lib.damascus_ctx_trace_read(self._h, None, 0, ctypes.byref(ln), int(stop))
+        if rc not in (0, ESIZE):
+            self.check(rc, "trace_read")
+        buf = ctypes.create_string_buffer(ln.value + 1)
+        self.check(self._lib.damascus_ctx_trace_read(self._h, buf, ln.value + 1, ctypes.byref(ln), int(stop)),
+                   "trace_read")
+        out = []
+        for line in buf.raw[:ln.value].decode().splitlines():
+            k, s, t0, t1, b, n = line.split(",")
+            out.append((k, int(s), float(t0), float(t1), float(b), int(n)))
+        return out
 
     def kernel_stat(self, name: str):
         """(launches, total_ms, algorithmic_bytes, algorithmic_ops) or None."""

@@ -26,6 +26,7 @@ using namespace dm;
 struct damascus_ctx {
     Context* ctx;
     std::string err_copy;
+    std::string trace;  // trace lines read from the context, not yet copied out
 };
 struct damascus_prover {
     damascus_ctx* owner;
@@ -1017,6 +1018,23 @@ int damascus_ctx_set_profiling(damascus_ctx* ctx, int on) {
 }
 void damascus_ctx_reset_stats(damascus_ctx* ctx) {
     if (ctx) ctx->ctx->reset_stats();
+}
+int damascus_ctx_trace_start(damascus_ctx* ctx) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    ctx->trace.clear();
+    return ctx->ctx->start_trace();
+}
+int damascus_ctx_trace_read(damascus_ctx* ctx, char* buf, size_t cap, size_t* len, int stop) {
+    if (!ctx) return DAMASCUS_EINVAL;
+    std::string more;
+    const int rc = ctx->ctx->read_trace(&more, stop != 0);
+    if (rc != DAMASCUS_OK) return rc;
+    ctx->trace += more;
+    if (len) *len = ctx->trace.size();
+    if (!buf || cap < ctx->trace.size()) return set_err(ctx, DAMASCUS_ESIZE, "trace buffer too small");
+    std::memcpy(buf, ctx->trace.data(), ctx->trace.size());
+    ctx->trace.clear();
+    return DAMASCUS_OK;
 }
 int damascus_ctx_kernel_stat(damascus_ctx* ctx, const char* name, uint64_t* launches, double* total_ms,
                              double* algo_bytes, double* algo_ops) {

@@ -1,5 +1,6 @@
 #include "engine.h"
 
+#include <cstdio>
 #include <cstring>
 #include <limits>
 
@@ -176,9 +177,47 @@ cudaEvent_t Context::take_event() {
     return e;
 }
 
-void Context::record(const char* name, cudaEvent_t a, cudaEvent_t b, double bytes, double ops, int kernels) {
+void Context::record(const char* name, cudaEvent_t a, cudaEvent_t b, double bytes, double ops, int kernels,
+                     cudaStream_t st) {
     std::lock_guard<std::mutex> g(prof_mu_);
-    pending_.push_back(Pending{name, a, b, bytes, ops, kernels});
+    pending_.push_back(Pending{name, a, b, bytes, ops, kernels, st});
+}
+
+int Context::start_trace() {
+    cudaSetDevice(device_);
+    flush_timings();
+    cudaEvent_t ref = take_event();
+    if (!ref) return kECuda;
+    // every stream's earlier work ends before the reference point
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaEventRecord(ref, stream_);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ref);
+    if (e != cudaSuccess) {
+        set_error(std::string("start_trace: ") + cudaGetErrorString(e));
+        return kECuda;
+    }
+    std::lock_guard<std::mutex> g(prof_mu_);
+    if (trace_ref_) event_pool_.push_back(trace_ref_);
+    trace_ref_ = ref;
+    trace_csv_.clear();
+    trace_streams_.clear();
+    tracing_ = true;
+    profiling_ = true;
+    return kOk;
+}
+
+int Context::read_trace(std::string* csv, bool stop) {
+    flush_timings();
+    std::lock_guard<std::mutex> g(prof_mu_);
+    if (csv) csv->swap(trace_csv_);
+    trace_csv_.clear();
+    if (stop) {
+        tracing_ = false;
+        if (trace_ref_) event_pool_.push_back(trace_ref_);
+        trace_ref_ = nullptr;
+        trace_streams_.clear();
+    }
+    return kOk;
 }
 
 void Context::flush_timings() {
@@ -192,6 +231,18 @@ void Context::flush_timings() {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, p.a, p.b);
         std::lock_guard<std::mutex> g(prof_mu_);
+        if (tracing_ && trace_ref_) {
+            float t0 = 0.f, t1 = 0.f;
+            cudaEventElapsedTime(&t0, trace_ref_, p.a);
+            cudaEventElapsedTime(&t1, trace_ref_, p.b);
+            size_t sid = 0;
+            while (sid < trace_streams_.size() && trace_streams_[sid] != p.st) ++sid;
+            if (sid == trace_streams_.size()) trace_streams_.push_back(p.st);
+            char line[160];
+            std::snprintf(line, sizeof line, "%s,%zu,%.4f,%.4f,%.0f,%d\n", p.name.c_str(), sid, t0, t1, p.bytes,
+                          p.kernels);
+            trace_csv_ += line;
+        }
         KernelStat& s = stats_[p.name];
         s.launches += (uint64_t)p.kernels;
         s.total_ms += ms;

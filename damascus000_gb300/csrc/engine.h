@@ -65,8 +65,16 @@ class Context {
     // Optional per-kernel event timing on the launching stream.
     void set_profiling(bool on) { profiling_ = on; }
     bool profiling() const { return profiling_; }
-    void record(const char* name, cudaEvent_t a, cudaEvent_t b, double bytes, double ops, int kernels = 1);
+    void record(const char* name, cudaEvent_t a, cudaEvent_t b, double bytes, double ops, int kernels = 1,
+                cudaStream_t st = nullptr);
     void flush_timings();  // resolves recorded event pairs (synchronises the stream)
+    // Launch trace: from start_trace() on, every timed launch group is also kept
+    // with its stream and its start and end relative to a reference event, and
+    // read_trace() returns them as CSV lines "kind,stream,start_ms,end_ms,bytes,
+    // kernels" (the start is when the stream reached the group, which includes
+    // any wait for the stream's previous work).  Turns profiling on.
+    int start_trace();
+    int read_trace(std::string* csv, bool stop);
     bool stat(const char* name, KernelStat* out);
     void reset_stats();
     cudaEvent_t take_event();
@@ -120,8 +128,13 @@ class Context {
         cudaEvent_t a, b;
         double bytes, ops;
         int kernels;
+        cudaStream_t st;
     };
     std::vector<Pending> pending_;
+    bool tracing_ = false;
+    cudaEvent_t trace_ref_ = nullptr;
+    std::string trace_csv_;
+    std::vector<cudaStream_t> trace_streams_;
     std::vector<cudaEvent_t> event_pool_;
     std::map<std::string, KernelStat> stats_;
     void* flush_buf_ = nullptr;

@@ -4,6 +4,7 @@
 
 #include <cstring>
 
+#include "dm_nvtx.h"
 #include "host_blake3.h"
 
 namespace dm {
@@ -96,6 +97,7 @@ int Plan::launch_all(Context* ctx, cudaStream_t st, std::string* err) {
             cudaEventRecord(a, st);
         }
         const int before = launches;
+        NvtxRange range(name);
         const int rc = body();
         if (rc != 0) {
             *err = std::string(name) + ": " + cudaGetErrorString((cudaError_t)rc);
@@ -104,7 +106,7 @@ int Plan::launch_all(Context* ctx, cudaStream_t st, std::string* err) {
         if (a) {
             cudaEvent_t b = ctx->take_event();
             cudaEventRecord(b, st);
-            ctx->record(name, a, b, bytes, ops, launches - before);
+            ctx->record(name, a, b, bytes, ops, launches - before, st);
         }
         return 0;
     };
@@ -595,6 +597,7 @@ int GpuProver::init(const uint8_t* file, uint64_t len, bool on_device, const uin
 }
 
 int GpuProver::run_stage() {
+    NvtxRange range(stage_name((int)ps_.stage()));
     Plan plan;
     ps_.plan_stage(plan);
     std::string err;
@@ -604,7 +607,11 @@ int GpuProver::run_stage() {
     if (last) cudaEventRecord(ev_end_, s_);
     cudaError_t e = cudaStreamSynchronize(s_);
     if (e != cudaSuccess) return fail(kECuda, std::string("stage: ") + cudaGetErrorString(e));
-    const int rc = ps_.complete_stage();
+    int rc;
+    {
+        NvtxRange fs("fiat-shamir");
+        rc = ps_.complete_stage();
+    }
     if (rc != kOk) return fail(rc, ps_.error());
     return kOk;
 }

@@ -1,5 +1,7 @@
 #include "serve.h"
 
+#include "dm_nvtx.h"
+
 #include <algorithm>
 #include <chrono>
 #include <cstdlib>
@@ -276,6 +278,7 @@ void Engine::launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock
     }
     lk.unlock();
     const Clock::time_point t_launch = Clock::now();
+    NvtxRange range(high ? "wave (deep)" : "wave");
     cudaStream_t ws = wave_streams_[si];
     // admissions (allocations, file copies) on stream_ precede the wave's kernels
     cudaEventRecord(admit_ev_, stream_);
@@ -327,7 +330,11 @@ void Engine::worker() {
             continue;
         }
         const Clock::time_point t0 = Clock::now();
-        const int rc = r->ps->complete_stage();
+        int rc;
+        {
+            NvtxRange fs("fiat-shamir");
+            rc = r->ps->complete_stage();
+        }
         if (rc == kOk && r->ps->stage() == Stage::Done) r->ps->encode_proof(&r->proof);
         const double host_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
         if (rc != kOk || r->ps->stage() == Stage::Done) {

@@ -327,6 +327,15 @@ int damascus_ctx_generator_cache_stats(damascus_ctx* ctx, uint64_t* hits, uint64
 /* Per-kernel CUDA-event timing on the launching stream (off by default). */
 int damascus_ctx_set_profiling(damascus_ctx* ctx, int on);
 void damascus_ctx_reset_stats(damascus_ctx* ctx);
+/* Launch trace (turns profiling on): from here every timed launch group (one
+ * kernel kind of one stage, on its stream) is kept with its stream number and
+ * its start and end in milliseconds after this call. */
+int damascus_ctx_trace_start(damascus_ctx* ctx);
+/* Waits for the traced work and writes CSV lines "kind,stream,start_ms,end_ms,
+ * algo_bytes,kernels" (a start is when the stream reached the group).  A small
+ * buffer gives DAMASCUS_ESIZE and *len = the bytes needed; the lines are kept
+ * for the next call.  stop != 0 ends the trace. */
+int damascus_ctx_trace_read(damascus_ctx* ctx, char* buf, size_t cap, size_t* len, int stop);
 /* 0 and fills the totals if the kernel ran since the last reset. */
 int damascus_ctx_kernel_stat(damascus_ctx* ctx, const char* name, uint64_t* launches, double* total_ms,
                              double* algo_bytes, double* algo_ops);

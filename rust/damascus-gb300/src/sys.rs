@@ -114,6 +114,8 @@ extern "C" {
     pub fn damascus_engine_take(e: *mut Engine, ticket: u64, proof_out: *mut u8, cap: usize) -> c_int;
     pub fn damascus_engine_drain(e: *mut Engine) -> c_int;
     pub fn damascus_engine_stats(e: *mut Engine, completed: *mut u64, failed: *mut u64, waves: *mut u64, launches: *mut u64, peak_reserved_bytes: *mut u64) -> c_int;
+    pub fn damascus_ctx_trace_start(ctx: *mut Ctx) -> c_int;
+    pub fn damascus_ctx_trace_read(ctx: *mut Ctx, buf: *mut c_char, cap: usize, len: *mut usize, stop: c_int) -> c_int;
     pub fn damascus_engine_profile(e: *mut Engine, host_stage_ms: *mut f64, gpu_idle_ms: *mut f64) -> c_int;
     pub fn damascus_engine_scheduler_profile(e: *mut Engine, admit_ms: *mut f64, launch_ms: *mut f64) -> c_int;
     pub fn damascus_verify_service_create(ctx: *mut Ctx, workers: c_int, cache_bytes: u64, out: *mut *mut VerifyService) -> c_int;

@@ -247,3 +247,21 @@ def test_engine_request_timeout_and_bounded_wait(ctx):
         st = eng.stats()
     assert proof == ctx.prove(*big, EPOCH)
     assert st["failed"] == 1
+
+
+def test_launch_trace_covers_every_kernel_kind(ctx):
+    """The launch trace: every timed group of an engine batch, with its stream,
+    a start no later than its end, and the kinds of a proof's stages."""
+    files = _files(95, [60_000, 300_000, 1_200_000])
+    with D.Engine(ctx, max_waves=4) as eng:
+        ctx.trace_start()
+        proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
+        rows = ctx.trace_read(stop=True)
+    ctx.set_profiling(False)
+    kinds = {r[0] for r in rows}
+    assert {"file_hash", "unpack_witness", "gen_generators", "ntt_fwd", "fold", "finish"} <= kinds
+    assert all(0 <= r[2] <= r[3] for r in rows) and all(r[5] >= 1 for r in rows)
+    assert max(r[1] for r in rows) < 5  # the admission stream and up to four wave streams
+    assert ctx.trace_read() == []  # stopped: nothing more is kept
+    for (d, s), p in zip(files, proofs):
+        assert p == ctx.prove(d, s, EPOCH)
