@@ -413,7 +413,10 @@ class Context:
 
     def trace_read(self, stop: bool = True):
         """[(kind, stream, start_ms, end_ms, algorithmic_bytes, kernels)] since
-        trace_start() or the last read; stop ends the trace."""
+        trace_start() or the last read; stop ends the trace.  Engines add host
+        rows on the same time base: ("sched_wave" | "sched_wave_deep", stream,
+        start, end, requests, launches), ("wave_done", stream, t, t, requests, 0)
+        and ("fiat_shamir", depth, start, end, 1, 0)."""
         ln = ctypes.c_size_t()
         rc = self._lib.damascus_ctx_trace_read(self._h, None, 0, ctypes.byref(ln), int(stop))
         if rc not in (0, ESIZE):

@@ -72,7 +72,7 @@ struct FinishJobX {
     uint32_t* partials;
     uint4* out;            // [npolys][2^L]
     const uint4* expect;   // compared with out when non-null
-    uint32_t* flag;        // set to 1 on mismatch
+    uint32_t* flag;        // set to 1 on mismatch (a plain store: device or mapped pinned host memory)
     uint32_t parts;
     uint32_t mode;         // FinishMode
     uint32_t rows;         // npolys * kPrimes
@@ -81,6 +81,10 @@ struct FinishJobX {
     // transformed rows `partials` and `rhs` (a negacyclic ring product per
     // polynomial) instead of a sum of partials.
     const uint32_t* rhs;
+    // When set: a second copy of out in mapped pinned host memory (same layout),
+    // written by the kernel itself, so the host reads the stage's commitments
+    // once the stream has passed the kernel, without a device-to-host copy.
+    uint4* host_out;
 };
 
 

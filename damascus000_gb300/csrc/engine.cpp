@@ -199,11 +199,23 @@ int Context::start_trace() {
     std::lock_guard<std::mutex> g(prof_mu_);
     if (trace_ref_) event_pool_.push_back(trace_ref_);
     trace_ref_ = ref;
+    trace_host_ref_ = std::chrono::steady_clock::now();
     trace_csv_.clear();
     trace_streams_.clear();
     tracing_ = true;
     profiling_ = true;
     return kOk;
+}
+
+void Context::trace_host(const char* kind, int lane, std::chrono::steady_clock::time_point t0,
+                         std::chrono::steady_clock::time_point t1, double count, int launches) {
+    std::lock_guard<std::mutex> g(prof_mu_);
+    if (!tracing_) return;
+    using ms = std::chrono::duration<double, std::milli>;
+    char line[160];
+    std::snprintf(line, sizeof line, "%s,%d,%.4f,%.4f,%.0f,%d\n", kind, lane, ms(t0 - trace_host_ref_).count(),
+                  ms(t1 - trace_host_ref_).count(), count, launches);
+    trace_csv_ += line;
 }
 
 int Context::read_trace(std::string* csv, bool stop) {

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -75,6 +76,14 @@ class Context {
     // any wait for the stream's previous work).  Turns profiling on.
     int start_trace();
     int read_trace(std::string* csv, bool stop);
+    // Host rows of the same trace (host clock from the same reference point,
+    // taken right after the reference event completed): `kind,lane,start_ms,
+    // end_ms,count,launches` with lane and count chosen by the caller (the engine
+    // logs each wave's planning and launching with its stream and request count,
+    // and each Fiat-Shamir step).
+    bool tracing() const { return tracing_.load(std::memory_order_relaxed); }
+    void trace_host(const char* kind, int lane, std::chrono::steady_clock::time_point t0,
+                    std::chrono::steady_clock::time_point t1, double count, int launches);
     bool stat(const char* name, KernelStat* out);
     void reset_stats();
     cudaEvent_t take_event();
@@ -131,7 +140,8 @@ class Context {
         cudaStream_t st;
     };
     std::vector<Pending> pending_;
-    bool tracing_ = false;
+    std::atomic<bool> tracing_{false};
+    std::chrono::steady_clock::time_point trace_host_ref_{};
     cudaEvent_t trace_ref_ = nullptr;
     std::string trace_csv_;
     std::vector<cudaStream_t> trace_streams_;

@@ -14,7 +14,11 @@ namespace {
 // Commitment slots in comm_ (each 8 * S elements).
 enum Slot { kC = 0, kL = 1, kR = 2, kCt = 3, kV = 4, kLp = 5, kRp = 6, kChk = 7, kSlots = 8 };
 constexpr uint32_t kMaxParts = kMaxMacParts;
-constexpr size_t kTail = 128;  // pinned tail: [0,32) file id, [32,40) flags, [48,64) m*
+// Pinned tail after the three commitment slots: [0,32) file id, [32,40) check
+// flags, [48,64) m*.  The file id and the flags are written there by the kernels
+// (mapped pinned memory), like the commitments the finishes mirror into the
+// slots, so a stage needs no device-to-host copy; m* alone is copied, once.
+constexpr size_t kTail = 128;
 
 constexpr uint32_t kRows = kRank * kPrimes;  // MAC rows per job: (coordinate, prime)
 
@@ -230,7 +234,7 @@ uint64_t ProofState::footprint(uint64_t len) {
     auto r = [](uint64_t b) { return (b + 255) & ~255ull; };
     return r(len + 16) + r(file_hash_scratch_words(len) * 4) + r(S2 * 16) + r(S2 / 2 * 16) + r(8 * S2 * 16) +
            r(4 * S2 * 16) + r(S2 * kPrimes * 4) + r(8 * S2 * kPrimes * 4) + r(3ull * kMaxParts * kRows * S * 4) +
-           r((uint64_t)kSlots * kRank * S * 16) + r(64);
+           r((uint64_t)kSlots * kRank * S * 16);
 }
 
 const uint4* ProofState::g_round0() const { return cached_.g ? cached_.g : g_a_.as<uint4>(); }
@@ -242,7 +246,7 @@ void ProofState::release() {
         ctx_->prover_cache()->release(cached_);
         cached_ = ProverGenCache::Ref{};
     }
-    DevMem* all[] = {&file_, &hash_scratch_, &m_a_, &m_b_, &g_a_, &g_b_, &mhat_, &ghat_, &partials_, &comm_, &misc_};
+    DevMem* all[] = {&file_, &hash_scratch_, &m_a_, &m_b_, &g_a_, &g_b_, &mhat_, &ghat_, &partials_, &comm_};
     for (DevMem* m : all) m->reset();
     if (pinned_) ctx_->put_pinned(pinned_, pinned_bytes_);
     pinned_ = nullptr;
@@ -307,7 +311,6 @@ int ProofState::setup(const uint8_t* file, uint64_t len, bool on_device, const u
         need(ghat_, 8 * S2 * kPrimes * 4);
         need(partials_, 3ull * kMaxParts * kRows * S * 4);
         need(comm_, (uint64_t)kSlots * kRank * S * 16);
-        need(misc_, 64);
         if (rc == kOk || !ctx_->prover_cache()) break;
         // the budget is held by cached generator families: drop unreferenced ones, once
         release();
@@ -317,13 +320,14 @@ int ProofState::setup(const uint8_t* file, uint64_t len, bool on_device, const u
     pinned_bytes_ = 3ull * kRank * S * 16 + kTail;
     pinned_ = static_cast<uint8_t*>(ctx_->get_pinned(pinned_bytes_));
     if (!pinned_) return fail(kECuda, "cudaMallocHost failed");
+    // the check flags start clear (kernels only ever set them); no kernel of this
+    // request has been launched yet, and the buffer's previous owner has finished
+    std::memset(pinned_ + 3ull * kRank * S * 16, 0, kTail);
     d_file_ = on_device ? file : file_.as<uint8_t>();
     if (!on_device && len) {
         cudaError_t e = cudaMemcpyAsync(file_.as<uint8_t>(), file, len, cudaMemcpyHostToDevice, stream);
         if (e != cudaSuccess) return fail(kECuda, std::string("H2D file: ") + cudaGetErrorString(e));
     }
-    cudaError_t e = cudaMemsetAsync(misc_.as<uint8_t>(), 0, 64, stream);
-    if (e != cudaSuccess) return fail(kECuda, std::string("memset: ") + cudaGetErrorString(e));
     blake3_keyed_hash(seed, "g0", 2, st_.g_0_seed);  // sis.rs:70, 208-210
     st_.original_len_bytes = len;
     st_.d = d;
@@ -381,12 +385,20 @@ void ProofState::plan_stage(Plan& P) {
     uint4* C = comm_.as<uint4>();
     auto cs = [&](int i) { return C + (size_t)i * slot; };
     uint32_t* part = partials_.as<uint32_t>();
-    uint32_t* flags = reinterpret_cast<uint32_t*>(misc_.as<uint8_t>() + 32);
     uint8_t* tail = pinned_ + 3 * slot * 16;
+    uint32_t* flags = reinterpret_cast<uint32_t*>(tail + 32);
+    // host mirrors of the three commitment slots the host reads after a stage
+    uint4* hm0 = reinterpret_cast<uint4*>(pinned_);
+    uint4* hm1 = reinterpret_cast<uint4*>(pinned_ + slot * 16);
+    uint4* hm2 = reinterpret_cast<uint4*>(pinned_ + 2 * slot * 16);
+    auto fin = [](uint32_t* partials, uint4* out, const uint4* expect, uint32_t* flag, uint32_t parts, uint32_t mode,
+                  uint4* host_out) {
+        return FinishJobX{partials, out, expect, flag, parts, mode, kRows, 0, nullptr, host_out};
+    };
     if (stage_ == Stage::Init) {
         const uint32_t L = d_;
         const uint64_t S2 = (uint64_t)S * S;
-        P.hash.push_back(HashJob{d_file_, len_, hash_scratch_.as<uint32_t>(), misc_.as<uint32_t>(), 0});
+        P.hash.push_back(HashJob{d_file_, len_, hash_scratch_.as<uint32_t>(), reinterpret_cast<uint32_t*>(tail), 0});
         P.unpack.push_back(UnpackJob{d_file_, len_, m_a_.as<uint4>(), S2, 0});
         GenJob g{};
         for (int i = 0; i < 8; ++i)
@@ -417,16 +429,10 @@ void ProofState::plan_stage(Plan& P) {
                                     cached_.ghat, cached_.ghat != nullptr);
         if (nj) {
             const size_t pstride = (size_t)parts_ * kRows * S;
-            P.finish[L].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
-            P.finish[L].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
+            P.finish[L].push_back(fin(part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, hm1));
+            P.finish[L].push_back(fin(part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, hm2));
         }
-        P.finish[L].push_back(FinishJobX{part, cs(kC), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
-        P.d2h.push_back(Copy{tail, misc_.as<uint8_t>(), 32});
-        P.d2h.push_back(Copy{pinned_, cs(kC), slot * 16});
-        if (nj) {
-            P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kL), slot * 16});
-            P.d2h.push_back(Copy{pinned_ + 2 * slot * 16, cs(kR), slot * 16});
-        }
+        P.finish[L].push_back(fin(part, cs(kC), nullptr, nullptr, parts_, kFinishPlain, hm0));
         return;
     }
     const uint32_t L = d_ - (uint32_t)round_, s = 1u << L, h = s / 2;
@@ -451,13 +457,12 @@ void ProofState::plan_stage(Plan& P) {
         uint32_t* prp = plp + (size_t)parts_ * kRows * h;
         P.split.push_back(
             MacJobX{ghat_.as<uint32_t>(), mhat_.as<uint32_t>(), pchk, plp, prp, 0, 0, c, parts_, 0, 0, L, kc});
-        P.finish[L].push_back(FinishJobX{pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain, kRows, 0});
-        P.finish[L - 1].push_back(FinishJobX{plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL, kRows, 0});
-        P.finish[L - 1].push_back(FinishJobX{prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR, kRows, 0});
-        P.d2h.push_back(Copy{pinned_, cs(kCt), (size_t)kRank * s * 16});
-        P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kLp), (size_t)kRank * h * 16});
-        P.d2h.push_back(Copy{pinned_ + 2 * slot * 16, cs(kRp), (size_t)kRank * h * 16});
-        P.d2h.push_back(Copy{tail + 32, flags, 8});
+        // The recomputed commitment V is checked against the folded one (Ct); the
+        // host reads V's mirror as Ct, which it equals unless the check flag is set
+        // (and then the stage fails before anything is absorbed).
+        P.finish[L].push_back(fin(pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain, hm0));
+        P.finish[L - 1].push_back(fin(plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL, hm1));
+        P.finish[L - 1].push_back(fin(prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR, hm2));
         return;
     }
     if (stage_ == Stage::Poly) {
@@ -470,16 +475,11 @@ void ProofState::plan_stage(Plan& P) {
         const bool nj = plan_commit(P, Ln, h, mcols_ < h ? mcols_ : h, m_a_.as<uint4>(), g_a_.as<uint4>(), part);
         if (nj) {
             const size_t pstride = (size_t)parts_ * kRows * h;
-            P.finish[Ln].push_back(FinishJobX{part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
-            P.finish[Ln].push_back(FinishJobX{part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, kRows, 0});
+            P.finish[Ln].push_back(fin(part + pstride, cs(kL), nullptr, nullptr, parts_, kFinishPlain, hm1));
+            P.finish[Ln].push_back(fin(part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, hm2));
         }
-        P.finish[Ln].push_back(FinishJobX{part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain, kRows, 0});
-        P.d2h.push_back(Copy{pinned_, cs(kC), (size_t)kRank * h * 16});
-        if (nj) {
-            P.d2h.push_back(Copy{pinned_ + slot * 16, cs(kL), (size_t)kRank * h * 16});
-            P.d2h.push_back(Copy{pinned_ + 2 * slot * 16, cs(kR), (size_t)kRank * h * 16});
-        }
-        P.d2h.push_back(Copy{tail + 32, flags, 8});
+        // as in the vector stage: the recomputed Chk's mirror is the folded C
+        P.finish[Ln].push_back(fin(part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain, hm0));
         if (round_ + 1 == d_) P.d2h.push_back(Copy{tail + 48, m_a_.as<uint4>(), 16});
     }
 }

@@ -149,6 +149,10 @@ int Engine::submit(const uint8_t* file, uint64_t len, const uint8_t seed[32], co
 void CUDART_CB Engine::on_wave_done(void* arg) {
     Wave* w = static_cast<Wave*>(arg);
     Engine* e = w->eng;
+    if (e->ctx_->tracing()) {
+        const Clock::time_point now = Clock::now();
+        e->ctx_->trace_host("wave_done", w->stream_idx, now, now, (double)w->reqs.size(), 0);
+    }
     {
         std::lock_guard<std::mutex> g(e->mu_);
         for (Request* r : w->reqs) e->host_q_.push_back(r);
@@ -288,8 +292,11 @@ void Engine::launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock
     std::string err;
     const int n = plan.launch(ctx_, ws, &err);
     cudaError_t e = cudaSuccess;
+    const size_t nreq = w->reqs.size();  // w belongs to the callback once it is enqueued
     if (n >= 0) e = cudaLaunchHostFunc(ws, on_wave_done, w);
-    const double launch_ms = std::chrono::duration<double, std::milli>(Clock::now() - t_launch).count();
+    const Clock::time_point t_end = Clock::now();
+    const double launch_ms = std::chrono::duration<double, std::milli>(t_end - t_launch).count();
+    if (ctx_->tracing()) ctx_->trace_host(high ? "sched_wave_deep" : "sched_wave", si, t_launch, t_end, (double)nreq, n);
     lk.lock();
     stats_.launch_ms += launch_ms;
     if (n < 0 || e != cudaSuccess) {
@@ -336,7 +343,9 @@ void Engine::worker() {
             rc = r->ps->complete_stage();
         }
         if (rc == kOk && r->ps->stage() == Stage::Done) r->ps->encode_proof(&r->proof);
-        const double host_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+        const Clock::time_point t1 = Clock::now();
+        const double host_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        if (ctx_->tracing()) ctx_->trace_host("fiat_shamir", (int)r->ps->depth(), t0, t1, 1.0, 0);
         if (rc != kOk || r->ps->stage() == Stage::Done) {
             if (rc != kOk) {
                 r->err = r->ps->error();

@@ -332,9 +332,13 @@ void damascus_ctx_reset_stats(damascus_ctx* ctx);
  * its start and end in milliseconds after this call. */
 int damascus_ctx_trace_start(damascus_ctx* ctx);
 /* Waits for the traced work and writes CSV lines "kind,stream,start_ms,end_ms,
- * algo_bytes,kernels" (a start is when the stream reached the group).  A small
- * buffer gives DAMASCUS_ESIZE and *len = the bytes needed; the lines are kept
- * for the next call.  stop != 0 ends the trace. */
+ * algo_bytes,kernels" (a start is when the stream reached the group).  Engines
+ * add host rows on the same time base: "sched_wave" / "sched_wave_deep" (a
+ * wave's planning and launching: its stream, request count and launches),
+ * "wave_done" (the wave's completion callback) and "fiat_shamir" (one request's
+ * host step; the second field is its depth).  A small buffer gives
+ * DAMASCUS_ESIZE and *len = the bytes needed; the lines are kept for the next
+ * call.  stop != 0 ends the trace. */
 int damascus_ctx_trace_read(damascus_ctx* ctx, char* buf, size_t cap, size_t* len, int stop);
 /* 0 and fills the totals if the kernel ran since the last reset. */
 int damascus_ctx_kernel_stat(damascus_ctx* ctx, const char* name, uint64_t* launches, double* total_ms,

@@ -258,10 +258,21 @@ def test_launch_trace_covers_every_kernel_kind(ctx):
         proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
         rows = ctx.trace_read(stop=True)
     ctx.set_profiling(False)
-    kinds = {r[0] for r in rows}
+    host_kinds = {"sched_wave", "sched_wave_deep", "wave_done", "fiat_shamir"}
+    gpu = [r for r in rows if r[0] not in host_kinds]
+    host = [r for r in rows if r[0] in host_kinds]
+    kinds = {r[0] for r in gpu}
     assert {"file_hash", "unpack_witness", "gen_generators", "ntt_fwd", "fold", "finish"} <= kinds
-    assert all(0 <= r[2] <= r[3] for r in rows) and all(r[5] >= 1 for r in rows)
-    assert max(r[1] for r in rows) < 5  # the admission stream and up to four wave streams
+    assert all(0 <= r[2] <= r[3] for r in gpu) and all(r[5] >= 1 for r in gpu)
+    assert max(r[1] for r in gpu) < 5  # the admission stream and up to four wave streams
+    # host rows: every wave's planning and launching (its stream, requests and
+    # launches), its completion callback, and one Fiat-Shamir step per stage
+    waves = [r for r in host if r[0].startswith("sched_wave")]
+    assert waves and all(0 <= r[1] < 4 and r[4] >= 1 and r[5] >= 1 and 0 <= r[2] <= r[3] for r in waves)
+    assert len([r for r in host if r[0] == "wave_done"]) == len(waves)
+    # every request's stages: Init plus two per round (60 KB, 300 KB and 1.2 MB
+    # files: d = 7, 8 and 9)
+    assert len([r for r in host if r[0] == "fiat_shamir"]) == sum(2 * d + 1 for d in (7, 8, 9))
     assert ctx.trace_read() == []  # stopped: nothing more is kept
     for (d, s), p in zip(files, proofs):
         assert p == ctx.prove(d, s, EPOCH)
