@@ -416,7 +416,10 @@ class Context:
         trace_start() or the last read; stop ends the trace.  Engines add host
         rows on the same time base: ("sched_wave" | "sched_wave_deep", stream,
         start, end, requests, launches), ("wave_done", stream, t, t, requests, 0)
-        and ("fiat_shamir", depth, start, end, 1, 0)."""
+        and ("fiat_shamir", depth, start, end, 1, 0); per request stage, with the
+        request's ticket in the fifth field, ("req_wait", depth, ready, launched,
+        ticket, 0), ("req_gpu", depth, launched, landed, ticket, 0) and
+        ("req_host", depth, landed, host step done, ticket, 0)."""
         ln = ctypes.c_size_t()
         rc = self._lib.damascus_ctx_trace_read(self._h, None, 0, ctypes.byref(ln), int(stop))
         if rc not in (0, ESIZE):

@@ -29,6 +29,8 @@ struct Engine::Request {
     bool cancel = false;          // the caller cancelled it
     bool has_deadline = false;    // the engine's request timeout applies
     Clock::time_point deadline{};
+    // current stage, for the launch trace: ready, its wave launched, landed
+    Clock::time_point t_ready{}, t_launch{}, t_landed{};
 };
 
 struct Engine::Wave {
@@ -152,6 +154,7 @@ void CUDART_CB Engine::on_wave_done(void* arg) {
     if (e->ctx_->tracing()) {
         const Clock::time_point now = Clock::now();
         e->ctx_->trace_host("wave_done", w->stream_idx, now, now, (double)w->reqs.size(), 0);
+        for (Request* r : w->reqs) r->t_landed = now;
     }
     {
         std::lock_guard<std::mutex> g(e->mu_);
@@ -224,6 +227,7 @@ void Engine::scheduler() {
             }
             r->state = Request::Active;
             if (active_++ == 0) active_since_ = Clock::now();
+            r->t_ready = Clock::now();
             ready_.push_back(r);
             if (ctx_->reserved() > stats_.peak_reserved) stats_.peak_reserved = ctx_->reserved();
         }
@@ -282,6 +286,7 @@ void Engine::launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock
     }
     lk.unlock();
     const Clock::time_point t_launch = Clock::now();
+    for (Request* r : w->reqs) r->t_launch = t_launch;
     NvtxRange range(high ? "wave (deep)" : "wave");
     cudaStream_t ws = wave_streams_[si];
     // admissions (allocations, file copies) on stream_ precede the wave's kernels
@@ -345,7 +350,16 @@ void Engine::worker() {
         if (rc == kOk && r->ps->stage() == Stage::Done) r->ps->encode_proof(&r->proof);
         const Clock::time_point t1 = Clock::now();
         const double host_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
-        if (ctx_->tracing()) ctx_->trace_host("fiat_shamir", (int)r->ps->depth(), t0, t1, 1.0, 0);
+        if (ctx_->tracing()) {
+            const int d = (int)r->ps->depth();
+            const double id = (double)r->ticket;
+            ctx_->trace_host("fiat_shamir", d, t0, t1, 1.0, 0);
+            // the stage's path: waiting for a wave, wave launch to completion
+            // callback, callback to the end of the host step (worker pickup included)
+            ctx_->trace_host("req_wait", d, r->t_ready, r->t_launch, id, 0);
+            ctx_->trace_host("req_gpu", d, r->t_launch, r->t_landed, id, 0);
+            ctx_->trace_host("req_host", d, r->t_landed, t1, id, 0);
+        }
         if (rc != kOk || r->ps->stage() == Stage::Done) {
             if (rc != kOk) {
                 r->err = r->ps->error();
@@ -361,6 +375,7 @@ void Engine::worker() {
         {
             std::lock_guard<std::mutex> g(mu_);
             stats_.host_stage_ms += host_ms;
+            r->t_ready = t1;
             ready_.push_back(r);
         }
         sched_cv_.notify_one();

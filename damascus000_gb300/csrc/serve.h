@@ -5,7 +5,8 @@
 // device until their last round.  A scheduler thread gathers the next GPU stage
 // of every ready request into one Plan ("wave"): same-degree rounds of different
 // requests land in the same kernel launches.  A host callback after each wave's
-// device->host copies hands its requests to a pool of host workers, which run
+// kernels (whose results the finishes write straight into mapped pinned host
+// memory) hands its requests to a pool of host workers, which run
 // the Fiat-Shamir part of the stage (transcript hashing, recompute verdicts,
 // records) and return the requests to the ready set.  Several waves are in
 // flight at once, so the GPU works on some requests while the host hashes for
@@ -110,7 +111,7 @@ class Engine {
     std::condition_variable sched_cv_, done_cv_, work_cv_;
     std::deque<Request*> queued_;  // submitted, not admitted
     std::vector<Request*> ready_;  // next stage can be launched
-    std::deque<Request*> host_q_;  // stage copies landed, host part pending
+    std::deque<Request*> host_q_;  // stage results landed, host part pending
     std::map<uint64_t, std::unique_ptr<Request>> all_;
     uint64_t next_ticket_ = 1;
     int inflight_waves_ = 0;

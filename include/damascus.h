@@ -336,7 +336,10 @@ int damascus_ctx_trace_start(damascus_ctx* ctx);
  * add host rows on the same time base: "sched_wave" / "sched_wave_deep" (a
  * wave's planning and launching: its stream, request count and launches),
  * "wave_done" (the wave's completion callback) and "fiat_shamir" (one request's
- * host step; the second field is its depth).  A small buffer gives
+ * host step; the second field is its depth), and per request stage, with the
+ * request's ticket in the fifth field, "req_wait" (ready until its wave
+ * launched), "req_gpu" (launched until the completion callback) and "req_host"
+ * (callback until its host step finished).  A small buffer gives
  * DAMASCUS_ESIZE and *len = the bytes needed; the lines are kept for the next
  * call.  stop != 0 ends the trace. */
 int damascus_ctx_trace_read(damascus_ctx* ctx, char* buf, size_t cap, size_t* len, int stop);

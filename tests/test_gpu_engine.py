@@ -258,7 +258,7 @@ def test_launch_trace_covers_every_kernel_kind(ctx):
         proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
         rows = ctx.trace_read(stop=True)
     ctx.set_profiling(False)
-    host_kinds = {"sched_wave", "sched_wave_deep", "wave_done", "fiat_shamir"}
+    host_kinds = {"sched_wave", "sched_wave_deep", "wave_done", "fiat_shamir", "req_wait", "req_gpu", "req_host"}
     gpu = [r for r in rows if r[0] not in host_kinds]
     host = [r for r in rows if r[0] in host_kinds]
     kinds = {r[0] for r in gpu}
@@ -272,7 +272,14 @@ def test_launch_trace_covers_every_kernel_kind(ctx):
     assert len([r for r in host if r[0] == "wave_done"]) == len(waves)
     # every request's stages: Init plus two per round (60 KB, 300 KB and 1.2 MB
     # files: d = 7, 8 and 9)
-    assert len([r for r in host if r[0] == "fiat_shamir"]) == sum(2 * d + 1 for d in (7, 8, 9))
+    steps = sum(2 * d + 1 for d in (7, 8, 9))
+    assert len([r for r in host if r[0] == "fiat_shamir"]) == steps
+    # and each step's path (ticket in the count field): ready -> launched ->
+    # landed -> host step done, in order
+    for kind in ("req_wait", "req_gpu", "req_host"):
+        path = [r for r in host if r[0] == kind]
+        assert len(path) == steps and all(0 <= r[2] <= r[3] for r in path)
+    assert len({r[4] for r in host if r[0] == "req_gpu"}) == len(files)
     assert ctx.trace_read() == []  # stopped: nothing more is kept
     for (d, s), p in zip(files, proofs):
         assert p == ctx.prove(d, s, EPOCH)
