@@ -201,7 +201,7 @@ int Plan::launch_all(Context* ctx, cudaStream_t st, std::string* err) {
                      const int n = (int)std::min<size_t>(kMaxJobs, finish[L].size() - i);
                      cudaError_t e = launch_finish_jobs(T, finish[L].data() + i, n, (uint32_t)L, st);
                      if (e != cudaSuccess) return (int)e;
-                     launches += 2;  // inverse transform + CRT
+                     launches += L <= 10 ? 1 : 2;  // the fused finish, or inverse transform + CRT
                  }
                  return 0;
              })))

@@ -4,9 +4,10 @@
 // budget and keep their witness, generators and fold state resident on the
 // device until their last round.  A scheduler thread gathers the next GPU stage
 // of every ready request into one Plan ("wave"): same-degree rounds of different
-// requests land in the same kernel launches.  A host callback after each wave's
-// kernels (whose results the finishes write straight into mapped pinned host
-// memory) hands its requests to a pool of host workers, which run
+// requests land in the same kernel launches.  When a wave's kernels have finished
+// (a poller thread queries each wave's event; the finishes write the results
+// straight into mapped pinned host memory) its requests go to a pool of host
+// workers, which run
 // the Fiat-Shamir part of the stage (transcript hashing, recompute verdicts,
 // records) and return the requests to the ready set.  Several waves are in
 // flight at once, so the GPU works on some requests while the host hashes for
@@ -88,6 +89,13 @@ class Engine {
     // it while planning and launching).
     void launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock<std::mutex>& lk);
     static void CUDART_CB on_wave_done(void* arg);
+    // A wave's stage has finished on the device (or failed with `status`): its
+    // requests go to the host workers.
+    void complete_wave(Wave* w, cudaError_t status);
+    void poller();
+    // One sweep over the waves in flight (mu_ held on entry and exit, dropped
+    // while querying); true when any completed.
+    bool poll_once(std::unique_lock<std::mutex>& lk);
     void scheduler();
     void worker();
     void finish_request(Request* r);
@@ -125,6 +133,15 @@ class Engine {
     EngineStats stats_;
     std::thread sched_thread_;
     std::vector<std::thread> workers_;
+    // Completion by polling (default): each wave records its stream's event, and
+    // a poller thread queries the events of the waves in flight, yielding between
+    // sweeps (it keeps one host core busy while waves run).  DM_ENGINE_POLL=0: a
+    // host callback per wave instead.
+    bool poll_ = true;
+    std::vector<cudaEvent_t> wave_events_;
+    std::vector<Wave*> polled_;
+    std::condition_variable poll_cv_;
+    std::thread poll_thread_;
 };
 
 }  // namespace dm
