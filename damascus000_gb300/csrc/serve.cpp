@@ -69,6 +69,7 @@ Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_w
     // measured 1-4 % slower.)  DM_ENGINE_POLL=0 restores the callbacks.
     poll_ = true;
     if (const char* v = std::getenv("DM_ENGINE_POLL")) poll_ = std::atoi(v) != 0;
+    if (const char* v = std::getenv("DM_ENGINE_SPIN_US")) spin_us_ = std::atoi(v);
     wave_events_.assign(max_waves_, nullptr);
     for (int i = 0; ok && poll_ && i < max_waves_; ++i)
         ok = check(cudaEventCreateWithFlags(&wave_events_[i], cudaEventDisableTiming), "cudaEventCreateWithFlags");
@@ -160,6 +161,7 @@ int Engine::submit(const uint8_t* file, uint64_t len, const uint8_t seed[32], co
         all_[r->ticket] = std::move(r);
         stats_.submitted++;
     }
+    sched_signal_.fetch_add(1, std::memory_order_release);
     sched_cv_.notify_one();
     return kOk;
 }
@@ -188,9 +190,16 @@ void Engine::complete_wave(Wave* w, cudaError_t status) {
         if (--e->inflight_waves_ == 0) e->idle_since_ = Clock::now();
         e->wave_stream_busy_[w->stream_idx] = false;
     }
-    e->work_cv_.notify_all();
+    e->work_signal_.fetch_add(1, std::memory_order_release);
+    e->sched_signal_.fetch_add(1, std::memory_order_release);
+    for (size_t i = 0; i < w->reqs.size(); ++i) e->work_cv_.notify_one();
     e->sched_cv_.notify_one();
     delete w;
+}
+
+void Engine::spin_for_signal(const std::atomic<uint64_t>& sig, uint64_t seen) const {
+    const Clock::time_point until = Clock::now() + std::chrono::microseconds(spin_us_);
+    while (sig.load(std::memory_order_acquire) == seen && Clock::now() < until) std::this_thread::yield();
 }
 
 bool Engine::poll_once(std::unique_lock<std::mutex>& lk) {
@@ -232,11 +241,18 @@ void Engine::poller() {
 void Engine::scheduler() {
     cudaSetDevice(ctx_->device());
     std::unique_lock<std::mutex> lk(mu_);
+    auto runnable = [&] {
+        return stop_ || (inflight_waves_ < max_waves_ && (!ready_.empty() || (!queued_.empty() && !admit_blocked_)));
+    };
     for (;;) {
-        sched_cv_.wait(lk, [&] {
-            return stop_ ||
-                   (inflight_waves_ < max_waves_ && (!ready_.empty() || (!queued_.empty() && !admit_blocked_)));
-        });
+        if (!runnable() && spin_us_ > 0 && inflight_waves_ > 0) {
+            // waves in flight: wait briefly awake for the next ready request
+            const uint64_t seen = sched_signal_.load(std::memory_order_acquire);
+            lk.unlock();
+            spin_for_signal(sched_signal_, seen);
+            lk.lock();
+        }
+        sched_cv_.wait(lk, runnable);
         if (stop_) return;
         // Admission in arrival order while the HBM budget holds the request's footprint.
         while (!queued_.empty()) {
@@ -400,6 +416,16 @@ void Engine::worker() {
         Request* r = nullptr;
         {
             std::unique_lock<std::mutex> lk(mu_);
+            if (!stop_ && host_q_.empty() && spin_us_ > 0 && spinning_workers_ < kSpinningWorkers) {
+                // a few workers wait briefly awake: a stage's requests reach the
+                // host without a thread wake-up
+                ++spinning_workers_;
+                const uint64_t seen = work_signal_.load(std::memory_order_acquire);
+                lk.unlock();
+                spin_for_signal(work_signal_, seen);
+                lk.lock();
+                --spinning_workers_;
+            }
             work_cv_.wait(lk, [&] { return stop_ || !host_q_.empty(); });
             if (host_q_.empty()) return;
             r = host_q_.front();
@@ -450,6 +476,7 @@ void Engine::worker() {
             r->t_ready = t1;
             ready_.push_back(r);
         }
+        sched_signal_.fetch_add(1, std::memory_order_release);
         sched_cv_.notify_one();
     }
 }
@@ -476,6 +503,7 @@ void Engine::finish_request(Request* r) {
         }
     }
     done_cv_.notify_all();
+    sched_signal_.fetch_add(1, std::memory_order_release);
     sched_cv_.notify_one();
 }
 
