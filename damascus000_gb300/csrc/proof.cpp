@@ -16,8 +16,9 @@ enum Slot { kC = 0, kL = 1, kR = 2, kCt = 3, kV = 4, kLp = 5, kRp = 6, kChk = 7,
 constexpr uint32_t kMaxParts = kMaxMacParts;
 // Pinned tail after the three commitment slots: [0,32) file id, [32,40) check
 // flags, [48,64) m*.  The file id and the flags are written there by the kernels
-// (mapped pinned memory), like the commitments the finishes mirror into the
-// slots, so a stage needs no device-to-host copy; m* alone is copied, once.
+// (mapped pinned memory), like the commitments of small rings that the finishes
+// mirror into the slots, so such a stage needs no device-to-host copy; m* is
+// copied once per proof.
 constexpr size_t kTail = 128;
 
 constexpr uint32_t kRows = kRank * kPrimes;  // MAC rows per job: (coordinate, prime)
@@ -387,10 +388,24 @@ void ProofState::plan_stage(Plan& P) {
     uint32_t* part = partials_.as<uint32_t>();
     uint8_t* tail = pinned_ + 3 * slot * 16;
     uint32_t* flags = reinterpret_cast<uint32_t*>(tail + 32);
-    // host mirrors of the three commitment slots the host reads after a stage
-    uint4* hm0 = reinterpret_cast<uint4*>(pinned_);
-    uint4* hm1 = reinterpret_cast<uint4*>(pinned_ + slot * 16);
-    uint4* hm2 = reinterpret_cast<uint4*>(pinned_ + 2 * slot * 16);
+    // The three commitment slots the host reads after a stage.  Up to rings of
+    // 2^(kCopyFromL - 1) the finishes mirror them into pinned host memory (no copy
+    // to issue, which is what the small, latency-bound stages pay for); from
+    // 2^kCopyFromL on (64 KiB slots and more; few, long stages) one copy per slot,
+    // which keeps the finishes' stores on the device.
+    constexpr uint32_t kCopyFromL = 9;
+    const uint32_t Lout = stage_ == Stage::Init ? d_ : (stage_ == Stage::Vec ? d_ - (uint32_t)round_
+                                                                                : d_ - (uint32_t)round_ - 1);
+    const bool mapped = Lout < kCopyFromL;
+    uint4* hm0 = mapped ? reinterpret_cast<uint4*>(pinned_) : nullptr;
+    uint4* hm1 = mapped ? reinterpret_cast<uint4*>(pinned_ + slot * 16) : nullptr;
+    uint4* hm2 = mapped ? reinterpret_cast<uint4*>(pinned_ + 2 * slot * 16) : nullptr;
+    auto copy3 = [&](const uint4* s0, const uint4* s1, const uint4* s2, size_t n0, size_t n12) {
+        if (mapped) return;
+        P.d2h.push_back(Copy{pinned_, s0, n0 * 16});
+        if (s1) P.d2h.push_back(Copy{pinned_ + slot * 16, s1, n12 * 16});
+        if (s2) P.d2h.push_back(Copy{pinned_ + 2 * slot * 16, s2, n12 * 16});
+    };
     auto fin = [](uint32_t* partials, uint4* out, const uint4* expect, uint32_t* flag, uint32_t parts, uint32_t mode,
                   uint4* host_out) {
         return FinishJobX{partials, out, expect, flag, parts, mode, kRows, 0, nullptr, host_out};
@@ -433,6 +448,7 @@ void ProofState::plan_stage(Plan& P) {
             P.finish[L].push_back(fin(part + 2 * pstride, cs(kR), nullptr, nullptr, parts_, kFinishPlain, hm2));
         }
         P.finish[L].push_back(fin(part, cs(kC), nullptr, nullptr, parts_, kFinishPlain, hm0));
+        copy3(cs(kC), nj ? cs(kL) : nullptr, nj ? cs(kR) : nullptr, slot, slot);
         return;
     }
     const uint32_t L = d_ - (uint32_t)round_, s = 1u << L, h = s / 2;
@@ -463,6 +479,7 @@ void ProofState::plan_stage(Plan& P) {
         P.finish[L].push_back(fin(pchk, cs(kV), cs(kCt), flags, parts_, kFinishPlain, hm0));
         P.finish[L - 1].push_back(fin(plp, cs(kLp), nullptr, nullptr, parts_, kFinishSplitL, hm1));
         P.finish[L - 1].push_back(fin(prp, cs(kRp), nullptr, nullptr, parts_, kFinishSplitR, hm2));
+        copy3(cs(kCt), cs(kLp), cs(kRp), (size_t)kRank * s, (size_t)kRank * h);
         return;
     }
     if (stage_ == Stage::Poly) {
@@ -480,6 +497,7 @@ void ProofState::plan_stage(Plan& P) {
         }
         // as in the vector stage: the recomputed Chk's mirror is the folded C
         P.finish[Ln].push_back(fin(part, cs(kChk), cs(kC), flags + 1, parts_, kFinishPlain, hm0));
+        copy3(cs(kC), nj ? cs(kL) : nullptr, nj ? cs(kR) : nullptr, (size_t)kRank * h, (size_t)kRank * h);
         if (round_ + 1 == d_) P.d2h.push_back(Copy{tail + 48, m_a_.as<uint4>(), 16});
     }
 }

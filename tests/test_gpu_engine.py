@@ -283,3 +283,20 @@ def test_launch_trace_covers_every_kernel_kind(ctx):
     assert ctx.trace_read() == []  # stopped: nothing more is kept
     for (d, s), p in zip(files, proofs):
         assert p == ctx.prove(d, s, EPOCH)
+
+
+@pytest.mark.parametrize("env", [{"DM_ENGINE_POLL": "0"}, {"DM_ENGINE_SPIN_US": "0"},
+                                 {"DM_ENGINE_POLL": "1", "DM_ENGINE_SPIN_US": "1000"}])
+def test_engine_completion_modes_give_identical_proofs(ctx, monkeypatch, env):
+    """Wave completion by host callback or by the polling thread, with or without
+    the short awake waits: the hand-overs change, the proofs do not (the engine
+    reads these settings when it is created)."""
+    files = _files(96, [40_000, 250_000, 700_000, 2_000_000])
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    with D.Engine(ctx, max_waves=6) as eng:
+        proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
+        st = eng.stats()
+    assert st["completed"] == len(files) and st["failed"] == 0
+    for (d, s), p in zip(files, proofs):
+        assert p == ctx.prove(d, s, EPOCH), len(d)
