@@ -115,22 +115,33 @@ int Context::flush_l2() {
 void* Context::get_pinned(size_t bytes) {
     {
         std::lock_guard<std::mutex> g(pin_mu_);
+        // best fit: the smallest idle buffer that holds `bytes`, so a small request
+        // does not take a large file's buffer
+        size_t best = pinned_free_.size();
         for (size_t i = 0; i < pinned_free_.size(); ++i)
-            if (pinned_free_[i].first >= bytes) {
-                void* p = pinned_free_[i].second;
-                pinned_free_.erase(pinned_free_.begin() + (long)i);
-                return p;
-            }
+            if (pinned_free_[i].first >= bytes &&
+                (best == pinned_free_.size() || pinned_free_[i].first < pinned_free_[best].first))
+                best = i;
+        if (best < pinned_free_.size()) {
+            void* p = pinned_free_[best].second;
+            pinned_free_.erase(pinned_free_.begin() + (long)best);
+            return p;
+        }
     }
     void* p = nullptr;
     if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> g(pin_mu_);
+    pinned_cap_[p] = bytes;
     return p;
 }
 
 void Context::put_pinned(void* p, size_t bytes) {
     if (!p) return;
     std::lock_guard<std::mutex> g(pin_mu_);
-    pinned_free_.emplace_back(bytes, p);
+    // back into the pool at the size it was allocated with (a reused buffer may be
+    // larger than the request that returns it)
+    const auto it = pinned_cap_.find(p);
+    pinned_free_.emplace_back(it != pinned_cap_.end() ? it->second : bytes, p);
 }
 
 Context::~Context() {

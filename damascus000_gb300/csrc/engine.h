@@ -158,7 +158,8 @@ class Context {
 
    private:
     std::mutex pin_mu_;
-    std::vector<std::pair<size_t, void*>> pinned_free_;
+    std::vector<std::pair<size_t, void*>> pinned_free_;  // idle buffers: (allocated size, address)
+    std::map<void*, size_t> pinned_cap_;                   // every buffer allocated: its size
 
 };
 
