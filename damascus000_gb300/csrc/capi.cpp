@@ -878,7 +878,10 @@ int damascus_engine_scheduler_profile(damascus_engine* e, double* admit_ms, doub
 int damascus_verify_service_create(damascus_ctx* ctx, int workers, uint64_t cache_bytes,
                                    damascus_verify_service** out) {
     if (!ctx || !out) return DAMASCUS_EINVAL;
-    *out = new damascus_verify_service{ctx, new VerifyService(ctx->ctx, workers, cache_bytes)};
+    *out = nullptr;
+    std::unique_ptr<VerifyService> svc(new VerifyService(ctx->ctx, workers, cache_bytes));
+    if (!svc->init_error().empty()) return set_err(ctx, DAMASCUS_ECUDA, svc->init_error());
+    *out = new damascus_verify_service{ctx, svc.release()};
     return DAMASCUS_OK;
 }
 

@@ -12,9 +12,15 @@ VerifyService::VerifyService(Context* ctx, int workers, uint64_t cache_bytes) : 
         workers = hc ? (int)(hc < 16 ? hc : 16) : 4;
     }
     if (cache_bytes) cache_.reset(new GenCache(ctx, cache_bytes));
-    cudaSetDevice(ctx->device());
+    cudaError_t e = cudaSetDevice(ctx->device());
     streams_.resize(workers, nullptr);
-    for (int w = 0; w < workers; ++w) cudaStreamCreateWithFlags(&streams_[w], cudaStreamNonBlocking);
+    for (int w = 0; w < workers && e == cudaSuccess; ++w) e = cudaStreamCreateWithFlags(&streams_[w], cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        // reported by init_error(); no workers: the destructor frees what was created
+        init_error_ = std::string("verifier service setup: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return;
+    }
     for (int w = 0; w < workers; ++w) threads_.emplace_back([this, w] { worker(w); });
 }
 
@@ -59,10 +65,15 @@ void VerifyService::worker(int w) {
     cudaSetDevice(ctx_->device());
     HostSerialScope serial;  // one proof per worker already fills the cores
     std::unique_lock<std::mutex> lk(mu_);
+    uint64_t trimmed_for = 0;  // the queue head this worker trimmed the cache for since it last waited
+    auto wait = [&] {
+        trimmed_for = 0;
+        work_cv_.wait(lk);
+    };
     for (;;) {
         if (queue_.empty()) {
             if (stop_) return;
-            work_cv_.wait(lk);
+            wait();
             continue;
         }
         const uint64_t ticket = queue_.front();
@@ -72,20 +83,27 @@ void VerifyService::worker(int w) {
         // made yet): conservative by at most their footprint.  A job that cannot
         // fit even alone runs alone and fails or succeeds as the one-shot
         // verifier would.
-        uint64_t want = ctx_->reserved() + admitted_bytes_ + job->footprint;
-        if (want > ctx_->budget() && cache_) {
-            // jobs come before cached families: drop the ones nobody holds
-            cache_->trim(admitted_bytes_ + job->footprint);
-            want = ctx_->reserved() + admitted_bytes_ + job->footprint;
+        const uint64_t want = ctx_->reserved() + admitted_bytes_ + job->footprint;
+        if (want > ctx_->budget() && cache_ && trimmed_for != ticket) {
+            // jobs come before cached families: drop the ones nobody holds.  The
+            // trim's cudaFree waits for the device: not under the service's lock,
+            // which the other workers need to finish their jobs.
+            trimmed_for = ticket;
+            const uint64_t need = admitted_bytes_ + job->footprint;
+            lk.unlock();
+            cache_->trim(need);
+            lk.lock();
+            continue;  // the queue may have changed meanwhile
         }
         if ((want > ctx_->budget() || job->alone) && running_ > 0) {
-            work_cv_.wait(lk);
+            wait();
             continue;
         }
         if (want > ctx_->budget() && job->footprint <= ctx_->budget()) {
             // nothing of ours runs and memory held by other users of the context
             // is in the way: their releases do not signal this service, so look
             // again shortly
+            trimmed_for = 0;
             work_cv_.wait_for(lk, std::chrono::milliseconds(2));
             continue;
         }

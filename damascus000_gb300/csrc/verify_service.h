@@ -39,6 +39,9 @@ class VerifyService {
     // the generator cache.
     VerifyService(Context* ctx, int workers, uint64_t cache_bytes);
     ~VerifyService();
+    // Empty when the streams were created; otherwise the failed call (the
+    // service then runs nothing and must be destroyed).
+    const std::string& init_error() const { return init_error_; }
 
     // Copies the proof; returns a ticket.  Never blocks on the GPU.
     int submit(const uint8_t* proof, size_t len, const uint8_t epoch[32], uint64_t* ticket);
@@ -78,6 +81,7 @@ class VerifyService {
     int running_ = 0;
     bool stop_ = false;
     VerifyStats st_;
+    std::string init_error_;
 };
 
 }  // namespace dm
