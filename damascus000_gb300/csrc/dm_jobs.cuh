@@ -87,7 +87,6 @@ struct FinishJobX {
     uint4* host_out;
 };
 
-
 // ---- folds and commitment algebra in the coefficient domain ----
 enum FoldMode : uint32_t {
     kFoldVec = 0,       // dst[e] = a[e] + x * b[e]

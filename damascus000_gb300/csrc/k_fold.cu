@@ -24,8 +24,6 @@ unsigned grid_for(uint64_t n, unsigned bx = 256) {
 #define GRID_STRIDE(i, n) \
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (uint64_t)gridDim.x * blockDim.x)
 
-
-
 // acc += a * b over eight limbs (a, b below 2^112; the caller keeps the sum below 2^256).
 __device__ __forceinline__ void acc_mul(uint32_t acc[8], const fq& a, const fq& b) {
 #pragma unroll
@@ -91,9 +89,6 @@ __global__ void fold_gen_round_kernel(const uint4* __restrict__ src, uint4* __re
     }
 }
 
-
-
-
 // Reference FFI fold on split halves (cuda/fold_kernel.cu:189-206); inputs are
 // reduced mod q first so any 128-bit words are accepted.
 __global__ void fold_split_kernel(const uint64_t* __restrict__ l_lo, const uint64_t* __restrict__ l_hi,
@@ -133,8 +128,6 @@ cudaError_t launch_fold_split(const uint64_t* l_lo, const uint64_t* l_hi, const 
     return cudaGetLastError();
 }
 
-
-
 cudaError_t launch_fold_gen_round(const uint4* d_src, uint4* d_dst, uint64_t N, uint32_t L, fq x_inv, fq y_inv,
                                   bool vec_stage, bool poly_stage, cudaStream_t s) {
     const uint64_t total = (vec_stage ? N / 2 : N) * kRank << (poly_stage ? L - 1 : L);
@@ -144,8 +137,5 @@ cudaError_t launch_fold_gen_round(const uint4* d_src, uint4* d_dst, uint64_t N, 
                                                            fq_neg(xy_inv), vec_stage ? 1 : 0, poly_stage ? 1 : 0);
     return cudaGetLastError();
 }
-
-
-
 
 }  // namespace dm

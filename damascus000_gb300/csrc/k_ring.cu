@@ -199,7 +199,6 @@ DM_D void acc96(uint64_t& lo, uint32_t& hi, uint64_t v) {
 }
 DM_D uint64_t mul64(uint32_t a, uint32_t b) { return (uint64_t)a * b; }
 
-
 // grid: per job, nblk * 72 * parts blocks; block -> (part, row, slot block).
 __global__ void __launch_bounds__(kMacThreads) mac_jobs_kernel(JobList<MacJobX> J, PrimeConsts pc) {
     const MacJobX jb = J.j[find_job(J)];
@@ -966,6 +965,5 @@ cudaError_t launch_finish_jobs(const DeviceTables& T, FinishJobX* jobs, int n, u
     crt_jobs_kernel<<<(unsigned)total, kCrtThreads, 0, st>>>(JC, L, T.pc, T.cc);
     return cudaGetLastError();
 }
-
 
 }  // namespace dm

@@ -56,7 +56,6 @@ void Plan::clear() {
     fold.clear();
     for (int L = 0; L <= kLogMaxProverRing; ++L) {
         ntt[L].clear();
-
         finish[L].clear();
     }
     d2h.clear();
