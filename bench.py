@@ -869,6 +869,9 @@ def run_gpu(args, wl):
         ctx.set_profiling(True)
         ctx.reset_stats()
         with D.Engine(ctx, max_waves=1) as eng1:
+            # every request admitted before the first launch, so each wave carries one
+            # stage of all the requests at it (the launches the kernels are rated on)
+            eng1.set_admission_batch(0)
             t_serial = time.perf_counter()
             serial = [eng1.wait(t)[0] for t in
                       [eng1.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]]

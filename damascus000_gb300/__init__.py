@@ -63,6 +63,7 @@ EXPORTED_SYMBOLS = (
     "damascus_engine_poll",
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
     "damascus_engine_wait_timeout", "damascus_engine_cancel", "damascus_engine_set_request_timeout",
+    "damascus_engine_set_admission_batch",
     "damascus_engine_health",
     "damascus_tuning_set", "damascus_tuning_get", "damascus_tuning_measure",
     "damascus_verify_service_create", "damascus_verify_service_destroy", "damascus_verify_service_submit",
@@ -175,6 +176,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_wait_timeout", i32, vp, u64, ctypes.c_double, P(sz), P(ctypes.c_double))
     sig("damascus_engine_cancel", i32, vp, u64)
     sig("damascus_engine_set_request_timeout", i32, vp, ctypes.c_double)
+    sig("damascus_engine_set_admission_batch", i32, vp, i32)
     sig("damascus_engine_health", i32, vp, P(u64), P(ctypes.c_double))
     sig("damascus_engine_drain", i32, vp)
     sig("damascus_engine_stats", i32, vp, P(u64), P(u64), P(u64), P(u64), P(u64))
@@ -738,6 +740,12 @@ class Engine:
         timeout_ms (0: no limit)."""
         self._ctx.check(self._lib.damascus_engine_set_request_timeout(self._h, float(timeout_ms)),
                         "engine set_request_timeout")
+
+    def set_admission_batch(self, requests_per_pass: int) -> None:
+        """Admissions per scheduling pass while an admitted request is ready
+        (default 1; 0 admits every queued request that fits before launching)."""
+        self._ctx.check(self._lib.damascus_engine_set_admission_batch(self._h, int(requests_per_pass)),
+                        "engine set_admission_batch")
 
     def health(self) -> dict:
         """Unfinished requests and milliseconds since any stage finished."""

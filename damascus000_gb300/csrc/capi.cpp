@@ -822,6 +822,12 @@ int damascus_engine_set_request_timeout(damascus_engine* e, double timeout_ms) {
     return DAMASCUS_OK;
 }
 
+int damascus_engine_set_admission_batch(damascus_engine* e, int requests_per_pass) {
+    if (!e || requests_per_pass < 0) return DAMASCUS_EINVAL;
+    e->e->set_admission_batch(requests_per_pass);
+    return DAMASCUS_OK;
+}
+
 int damascus_engine_health(damascus_engine* e, uint64_t* unfinished, double* ms_since_progress) {
     if (!e) return DAMASCUS_EINVAL;
     e->e->health(unfinished, ms_since_progress);

@@ -70,6 +70,7 @@ Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_w
     poll_ = true;
     if (const char* v = std::getenv("DM_ENGINE_POLL")) poll_ = std::atoi(v) != 0;
     if (const char* v = std::getenv("DM_ENGINE_SPIN_US")) spin_us_ = std::atoi(v);
+    if (const char* v = std::getenv("DM_ENGINE_ADMIT_BATCH")) admit_batch_ = std::atoi(v);
     wave_events_.assign(max_waves_, nullptr);
     for (int i = 0; ok && poll_ && i < max_waves_; ++i)
         ok = check(cudaEventCreateWithFlags(&wave_events_[i], cudaEventDisableTiming), "cudaEventCreateWithFlags");
@@ -255,7 +256,10 @@ void Engine::scheduler() {
         sched_cv_.wait(lk, runnable);
         if (stop_) return;
         // Admission in arrival order while the HBM budget holds the request's footprint.
+        int admitted_now = 0;
         while (!queued_.empty()) {
+            if (admit_batch_ > 0 && admitted_now >= admit_batch_ && !ready_.empty()) break;  // launch these first
+            ++admitted_now;
             Request* r = queued_.front();
             if (const int code = abort_code(r, Clock::now())) {  // cancelled or expired while queued
                 queued_.pop_front();
@@ -575,6 +579,14 @@ int Engine::cancel(uint64_t ticket) {
     if (now) finish_request(now);
     sched_cv_.notify_one();
     return kOk;
+}
+
+void Engine::set_admission_batch(int n) {
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        admit_batch_ = n > 0 ? n : 0;
+    }
+    sched_cv_.notify_one();
 }
 
 void Engine::set_request_timeout(double timeout_ms) {

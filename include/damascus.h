@@ -226,6 +226,13 @@ int damascus_engine_cancel(damascus_engine* e, uint64_t ticket);
  * unfinished timeout_ms after their submission (checked at admission and at
  * stage boundaries, as cancel is).  0 removes the limit. */
 int damascus_engine_set_request_timeout(damascus_engine* e, double timeout_ms);
+/* Admissions per scheduling pass while an admitted request is ready to launch
+ * (default 1: the engine launches after each admission, so the GPU starts on the
+ * first requests while later ones are set up and requests submitted together do
+ * not run their stages in lockstep).  0 admits every queued request that fits
+ * the budget before launching, which coalesces their first stages into one
+ * wave. */
+int damascus_engine_set_admission_batch(damascus_engine* e, int requests_per_pass);
 /* Watchdog reading: unfinished requests and the milliseconds since any stage
  * (or request) finished, 0 while nothing is unfinished.  No kernel of the engine
  * waits on a flag, so an age that keeps growing with requests unfinished points

@@ -110,6 +110,7 @@ extern "C" {
     pub fn damascus_engine_wait_timeout(e: *mut Engine, ticket: u64, timeout_ms: f64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
     pub fn damascus_engine_cancel(e: *mut Engine, ticket: u64) -> c_int;
     pub fn damascus_engine_set_request_timeout(e: *mut Engine, timeout_ms: f64) -> c_int;
+    pub fn damascus_engine_set_admission_batch(e: *mut Engine, requests_per_pass: c_int) -> c_int;
     pub fn damascus_engine_health(e: *mut Engine, unfinished: *mut u64, ms_since_progress: *mut f64) -> c_int;
     pub fn damascus_engine_take(e: *mut Engine, ticket: u64, proof_out: *mut u8, cap: usize) -> c_int;
     pub fn damascus_engine_drain(e: *mut Engine) -> c_int;

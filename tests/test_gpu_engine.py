@@ -300,3 +300,18 @@ def test_engine_completion_modes_give_identical_proofs(ctx, monkeypatch, env):
     assert st["completed"] == len(files) and st["failed"] == 0
     for (d, s), p in zip(files, proofs):
         assert p == ctx.prove(d, s, EPOCH), len(d)
+
+
+@pytest.mark.parametrize("batch", [0, 3])
+def test_engine_admission_batch_gives_identical_proofs(ctx, batch):
+    """Admitting every queued request before launching (0) or a few per pass:
+    the waves' composition changes, the proofs do not."""
+    files = _files(97, [30_000, 120_000, 500_000, 1_500_000, 70_000])
+    with D.Engine(ctx, max_waves=4) as eng:
+        eng.set_admission_batch(batch)
+        proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
+    for (d, s), p in zip(files, proofs):
+        assert p == ctx.prove(d, s, EPOCH), len(d)
+    with D.Engine(ctx) as eng:
+        with pytest.raises(D.DamascusError):
+            eng.set_admission_batch(-1)
