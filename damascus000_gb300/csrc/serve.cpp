@@ -274,12 +274,14 @@ void Engine::scheduler() {
             // ones when a request does not fit
             if (ctx_->reserved() + r->footprint > ctx_->budget() && ctx_->prover_cache()) {
                 // The trim's cudaFree waits for the device, and every wave in flight
-                // ends in on_wave_done, which takes mu_: trim without holding it.
-                // Only this thread admits, so the queue head stays r.
+                // ends in a completion that takes mu_: trim without holding it.
+                // Only this thread admits, but a cancel may take r off the queue
+                // meanwhile: look at the queue again.
                 lk.unlock();
                 ctx_->prover_cache()->trim(r->footprint);
                 lk.lock();
                 if (stop_) return;
+                if (queued_.empty() || queued_.front() != r) continue;
             }
             const uint64_t reserved = ctx_->reserved();
             if (reserved + r->footprint > ctx_->budget()) {
