@@ -276,6 +276,7 @@ static void b3_hash_stack(const uint32_t key[8], uint32_t flags, const uint8_t* 
     int depth = 0;
     size_t nchunks = len == 0 ? 1 : (len + B3_CHUNK_LEN - 1) / B3_CHUNK_LEN;
     b3_output last;
+    memset(&last, 0, sizeof last); /* set by the last chunk; nchunks >= 1 */
     for (size_t c = 0; c < nchunks; ++c) {
         size_t off = c * B3_CHUNK_LEN;
         size_t clen = len - off < B3_CHUNK_LEN ? len - off : B3_CHUNK_LEN;
