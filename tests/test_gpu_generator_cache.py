@@ -241,3 +241,58 @@ def test_engine_trims_cached_family_while_waves_in_flight(reference_proofs):
         assert c.generator_cache_stats()["bytes"] == 0
     finally:
         c.close()
+
+
+def test_engine_cancels_during_admission_and_trims(reference_proofs):
+    """Cancels racing the admission of a tight engine: queued requests under a
+    budget that holds about two d = 9 provers, cached families that must give way
+    (the scheduler trims them outside its lock), and a thread cancelling every
+    third request while the engine admits.  Every request ends (no ticket is lost
+    or admitted twice), the others' proofs equal the cache-free path's, and the
+    memory comes back."""
+    import random
+    import threading
+    f9 = D.prover_footprint(900_000)
+    c = D.Context(0, hbm_budget_bytes=2 * f9 + _entry_bytes(9) + (8 << 20), tuning=None)
+    try:
+        c.set_generator_cache(64 << 30)
+        sizes = [900_000, 250_000, 60_000, 700_000, 30_000, 400_000] * 4
+        rng = random.Random(11)
+        files = []
+        for i, n in enumerate(sizes):
+            data = _files(20 + i, [n])[0]
+            files.append((data, SYSTEM_SEED if i % 2 == 0 else bytes([i]) * 32))
+        with D.Engine(c, max_waves=4) as eng:
+            tickets = [eng.submit(d, s, EPOCH) for d, s in files]
+            victims = tickets[1::3]
+
+            def canceller():
+                for t in victims:
+                    for _ in range(rng.randrange(0, 3000)):
+                        pass
+                    try:
+                        eng.cancel(t)
+                    except D.DamascusError as e:  # already finished, or finished and taken
+                        assert e.code in (D.ESTATE, D.EINVAL)
+
+            th = threading.Thread(target=canceller)
+            th.start()
+            outcomes = {}
+            for t in tickets:
+                try:
+                    res = eng.wait(t, timeout_ms=120_000)
+                    assert res is not None, "a request never finished"
+                    outcomes[t] = res[0]
+                except D.DamascusError as e:
+                    assert e.code == D.ECANCELED and t in victims
+                    outcomes[t] = None
+            th.join()
+            assert eng.health()["unfinished"] == 0
+        for t, (d, s) in zip(tickets, files):
+            if outcomes[t] is not None:
+                assert outcomes[t] == reference_proofs(d, s), len(d)
+        assert sum(p is not None for p in outcomes.values()) >= len(tickets) - len(victims)
+        c.set_generator_cache(0)
+        assert c.reserved == 0
+    finally:
+        c.close()
