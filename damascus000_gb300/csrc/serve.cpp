@@ -458,8 +458,8 @@ void Engine::worker() {
             const int d = (int)r->ps->depth();
             const double id = (double)r->ticket;
             ctx_->trace_host("fiat_shamir", d, t0, t1, 1.0, 0);
-            // the stage's path: waiting for a wave, wave launch to completion
-            // callback, callback to the end of the host step (worker pickup included)
+            // the stage's path: waiting for a wave, wave launch until the host saw
+            // it complete, then until the end of the host step (worker pickup included)
             ctx_->trace_host("req_wait", d, r->t_ready, r->t_launch, id, 0);
             ctx_->trace_host("req_gpu", d, r->t_launch, r->t_landed, id, 0);
             ctx_->trace_host("req_host", d, r->t_landed, t1, id, 0);
