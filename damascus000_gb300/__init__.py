@@ -63,7 +63,7 @@ EXPORTED_SYMBOLS = (
     "damascus_engine_poll",
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
     "damascus_engine_wait_timeout", "damascus_engine_cancel", "damascus_engine_set_request_timeout",
-    "damascus_engine_set_admission_batch",
+    "damascus_engine_set_admission_batch", "damascus_engine_create_with_options",
     "damascus_engine_health",
     "damascus_tuning_set", "damascus_tuning_get", "damascus_tuning_measure",
     "damascus_verify_service_create", "damascus_verify_service_destroy", "damascus_verify_service_submit",
@@ -71,6 +71,14 @@ EXPORTED_SYMBOLS = (
     "damascus_verify_service_stats", "damascus_ctx_set_generator_cache", "damascus_ctx_generator_cache_stats",
     "damascus_commit_witness",
 )
+
+
+class EngineOptions(ctypes.Structure):
+    """damascus_engine_options: a negative value keeps the default (which the
+    DM_ENGINE_* environment variable overrides); host_threads and max_waves keep
+    theirs at 0."""
+    _fields_ = [("host_threads", ctypes.c_int), ("max_waves", ctypes.c_int), ("priority_depth", ctypes.c_int),
+                ("polling", ctypes.c_int), ("spin_us", ctypes.c_int), ("admission_batch", ctypes.c_int)]
 
 
 class DamascusError(RuntimeError):
@@ -167,6 +175,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_ctx_synchronize", i32, vp)
     sig("damascus_file_id_noalloc", i32, vp, sz, vp, vp)
     sig("damascus_engine_create", i32, vp, i32, i32, P(vp))
+    sig("damascus_engine_create_with_options", i32, vp, P(EngineOptions), P(vp))
     sig("damascus_engine_destroy", None, vp)
     sig("damascus_engine_submit", i32, vp, cp, sz, cp, cp, P(u64))
     sig("damascus_engine_submit_device", i32, vp, vp, sz, cp, cp, P(u64))
@@ -657,12 +666,19 @@ class DamascusVerifier:
 class Engine:
     """Continuous-batching prover: submit files, collect proofs (identical bytes to Context.prove)."""
 
-    def __init__(self, ctx: Context, host_threads: int = 0, max_waves: int = 0):
+    def __init__(self, ctx: Context, host_threads: int = 0, max_waves: int = 0, *,
+                 priority_depth: Optional[int] = None, polling: Optional[bool] = None,
+                 spin_us: Optional[int] = None, admission_batch: Optional[int] = None):
+        """Settings left at None keep the library's defaults (or the DM_ENGINE_*
+        environment variables): see damascus_engine_options."""
         self._ctx = ctx
         self._lib = ctx._lib
         max_waves = max_waves or getattr(ctx, "engine_waves", 0)
+        opt = lambda v: -1 if v is None else int(v)
+        o = EngineOptions(host_threads, max_waves, opt(priority_depth), opt(polling), opt(spin_us),
+                          opt(admission_batch))
         h = ctypes.c_void_p()
-        ctx.check(self._lib.damascus_engine_create(ctx.handle, host_threads, max_waves, ctypes.byref(h)),
+        ctx.check(self._lib.damascus_engine_create_with_options(ctx.handle, ctypes.byref(o), ctypes.byref(h)),
                   "engine create")
         self._h = h
 

@@ -726,6 +726,25 @@ int damascus_engine_create(damascus_ctx* ctx, int host_threads, int max_waves, d
     return DAMASCUS_OK;
 }
 
+int damascus_engine_create_with_options(damascus_ctx* ctx, const damascus_engine_options* opts,
+                                        damascus_engine** out) {
+    if (!ctx || !out) return DAMASCUS_EINVAL;
+    *out = nullptr;
+    EngineOptions o;
+    if (opts) {
+        o.host_threads = opts->host_threads;
+        o.max_waves = opts->max_waves;
+        o.priority_depth = opts->priority_depth;
+        o.polling = opts->polling;
+        o.spin_us = opts->spin_us;
+        o.admission_batch = opts->admission_batch;
+    }
+    std::unique_ptr<Engine> eng(new Engine(ctx->ctx, o));
+    if (!eng->init_error().empty()) return set_err(ctx, DAMASCUS_ECUDA, eng->init_error());
+    *out = new damascus_engine{ctx, eng.release(), {}, {}, {}};
+    return DAMASCUS_OK;
+}
+
 void damascus_engine_destroy(damascus_engine* e) {
     if (!e) return;
     delete e->e;

@@ -39,7 +39,26 @@ struct Engine::Wave {
     int stream_idx;
 };
 
-Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_waves_(max_waves > 0 ? max_waves : 16) {
+namespace {
+EngineOptions options_of(int host_threads, int max_waves) {
+    EngineOptions o;
+    o.host_threads = host_threads;
+    o.max_waves = max_waves;
+    return o;
+}
+// An explicit setting, else the environment variable, else the default.
+int setting(int given, const char* env, int dflt) {
+    if (given >= 0) return given;
+    if (const char* v = std::getenv(env)) return std::atoi(v);
+    return dflt;
+}
+}  // namespace
+
+Engine::Engine(Context* ctx, int host_threads, int max_waves) : Engine(ctx, options_of(host_threads, max_waves)) {}
+
+Engine::Engine(Context* ctx, const EngineOptions& opt)
+    : ctx_(ctx), max_waves_(opt.max_waves > 0 ? opt.max_waves : 16) {
+    const int host_threads = opt.host_threads;
     auto check = [this](cudaError_t e, const char* what) {
         if (e != cudaSuccess && init_error_.empty())
             init_error_ = std::string("engine setup, ") + what + ": " + cudaGetErrorString(e);
@@ -49,8 +68,7 @@ Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_w
     wave_stream_busy_.assign(max_waves_, false);
     // d = 11 (16 MiB files and up): on the serving stream +1.9 % against no split
     // (five interleaved A/B pairs on GB300s; d >= 10 measured alike and noisier)
-    priority_depth_ = 11;
-    if (const char* v = std::getenv("DM_ENGINE_PRIORITY_DEPTH")) priority_depth_ = (uint32_t)std::atoi(v);
+    priority_depth_ = (uint32_t)setting(opt.priority_depth, "DM_ENGINE_PRIORITY_DEPTH", 11);
     int least = 0, greatest = 0;
     bool ok = check(cudaSetDevice(ctx_->device()), "cudaSetDevice") &&
               check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreateWithFlags") &&
@@ -67,10 +85,9 @@ Engine::Engine(Context* ctx, int host_threads, int max_waves) : ctx_(ctx), max_w
     // 3 % on the serving stream and 10 % on the batched set.  (Polling from the
     // scheduler thread between its launches instead of a thread of its own
     // measured 1-4 % slower.)  DM_ENGINE_POLL=0 restores the callbacks.
-    poll_ = true;
-    if (const char* v = std::getenv("DM_ENGINE_POLL")) poll_ = std::atoi(v) != 0;
-    if (const char* v = std::getenv("DM_ENGINE_SPIN_US")) spin_us_ = std::atoi(v);
-    if (const char* v = std::getenv("DM_ENGINE_ADMIT_BATCH")) admit_batch_ = std::atoi(v);
+    poll_ = setting(opt.polling, "DM_ENGINE_POLL", 1) != 0;
+    spin_us_ = setting(opt.spin_us, "DM_ENGINE_SPIN_US", spin_us_);
+    admit_batch_ = setting(opt.admission_batch, "DM_ENGINE_ADMIT_BATCH", admit_batch_);
     wave_events_.assign(max_waves_, nullptr);
     for (int i = 0; ok && poll_ && i < max_waves_; ++i)
         ok = check(cudaEventCreateWithFlags(&wave_events_[i], cudaEventDisableTiming), "cudaEventCreateWithFlags");

@@ -41,9 +41,21 @@ struct EngineStats {
     uint64_t cancelled = 0, timed_out = 0;
 };
 
+// Engine settings; a negative value (or 0 for the first two) keeps the default,
+// which the DM_ENGINE_* environment variable of the same setting overrides.
+struct EngineOptions {
+    int host_threads = 0;     // Fiat-Shamir workers; 0: one fewer than the host's cores
+    int max_waves = 0;        // stage waves in flight, each on its own stream; 0: 16
+    int priority_depth = -1;  // requests this deep run on high-priority streams; 0: no split; default 11
+    int polling = -1;         // 1: a poller thread queries each wave's event (default); 0: a host callback per wave
+    int spin_us = -1;         // awake wait before blocking, microseconds; 0: block at once; default 200
+    int admission_batch = -1; // admissions per scheduling pass while a request is ready; 0: all; default 1
+};
+
 class Engine {
    public:
     Engine(Context* ctx, int host_threads, int max_waves);
+    Engine(Context* ctx, const EngineOptions& opt);
     ~Engine();
     // Empty when the streams and events were created; otherwise the failed call
     // (the engine then runs nothing and must be destroyed).

@@ -197,6 +197,24 @@ int damascus_verify(damascus_ctx* ctx, const uint8_t* proof, size_t len, const u
  * Proofs are the same bytes damascus_prove returns. */
 typedef struct damascus_engine damascus_engine;
 int damascus_engine_create(damascus_ctx* ctx, int host_threads, int max_waves, damascus_engine** out);
+/* The engine's settings.  A negative value keeps the default, which the
+ * DM_ENGINE_* environment variable named beside it overrides; host_threads and
+ * max_waves keep theirs at 0. */
+typedef struct damascus_engine_options {
+    int host_threads;    /* Fiat-Shamir workers; 0: one fewer than the host's cores */
+    int max_waves;       /* stage waves in flight, each on its own stream; 0: 16 */
+    int priority_depth;  /* requests this deep or deeper run their stages on high-priority
+                            streams; 0: no split; default 11 (DM_ENGINE_PRIORITY_DEPTH) */
+    int polling;         /* 1: a poller thread queries each wave's completion event (default);
+                            0: a host callback per wave (DM_ENGINE_POLL) */
+    int spin_us;         /* awake wait of the scheduler and two workers before they block;
+                            0: block at once; default 200 (DM_ENGINE_SPIN_US) */
+    int admission_batch; /* admissions per scheduling pass while a request is ready; 0: every
+                            queued request that fits first; default 1 (DM_ENGINE_ADMIT_BATCH) */
+} damascus_engine_options;
+/* damascus_engine_create with every setting; opts NULL: the defaults. */
+int damascus_engine_create_with_options(damascus_ctx* ctx, const damascus_engine_options* opts,
+                                        damascus_engine** out);
 void damascus_engine_destroy(damascus_engine* e);
 /* Copies the file and returns at once with a ticket.  The context's
  * max_preprocess_bytes applies at admission: a larger file's request fails with

@@ -332,6 +332,13 @@ impl<'c> Engine<'c> {
         Ok(Engine { ctx, raw })
     }
 
+    /// With every setting (`sys::EngineOptions::default()` keeps the library's).
+    pub fn with_options(ctx: &'c Context, opts: &sys::EngineOptions) -> Result<Self> {
+        let mut raw = std::ptr::null_mut();
+        ctx.check(unsafe { sys::damascus_engine_create_with_options(ctx.raw, opts, &mut raw) })?;
+        Ok(Engine { ctx, raw })
+    }
+
     /// Copies the file and returns a ticket at once.
     pub fn submit(&self, file: &[u8], seed_generators: &[u8; 32], epoch_seed: &[u8; 32]) -> Result<u64> {
         let mut ticket = 0u64;

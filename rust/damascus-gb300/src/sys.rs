@@ -42,6 +42,26 @@ pub struct Prover {
 pub struct Verifier {
     _p: [u8; 0],
 }
+/// `damascus_engine_options`: a negative value keeps the default (which the
+/// DM_ENGINE_* environment variable overrides); host_threads and max_waves keep
+/// theirs at 0.
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct EngineOptions {
+    pub host_threads: c_int,
+    pub max_waves: c_int,
+    pub priority_depth: c_int,
+    pub polling: c_int,
+    pub spin_us: c_int,
+    pub admission_batch: c_int,
+}
+
+impl Default for EngineOptions {
+    fn default() -> Self {
+        EngineOptions { host_threads: 0, max_waves: 0, priority_depth: -1, polling: -1, spin_us: -1, admission_batch: -1 }
+    }
+}
+
 #[repr(C)]
 pub struct Engine {
     _p: [u8; 0],
@@ -102,6 +122,7 @@ extern "C" {
     pub fn damascus_verifier_dimensions(v: *const Verifier, vector_len: *mut u64, ring_len: *mut u64);
     pub fn damascus_verify(ctx: *mut Ctx, proof: *const u8, len: usize, epoch_seed: *const u8) -> c_int;
     pub fn damascus_engine_create(ctx: *mut Ctx, host_threads: c_int, max_waves: c_int, out: *mut *mut Engine) -> c_int;
+    pub fn damascus_engine_create_with_options(ctx: *mut Ctx, opts: *const EngineOptions, out: *mut *mut Engine) -> c_int;
     pub fn damascus_engine_destroy(e: *mut Engine);
     pub fn damascus_engine_submit(e: *mut Engine, file: *const u8, len: usize, seed_generators: *const u8, epoch_seed: *const u8, ticket: *mut u64) -> c_int;
     pub fn damascus_engine_submit_device(e: *mut Engine, d_file: *const c_void, len: usize, seed_generators: *const u8, epoch_seed: *const u8, ticket: *mut u64) -> c_int;

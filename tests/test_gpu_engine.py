@@ -315,3 +315,16 @@ def test_engine_admission_batch_gives_identical_proofs(ctx, batch):
     with D.Engine(ctx) as eng:
         with pytest.raises(D.DamascusError):
             eng.set_admission_batch(-1)
+
+
+def test_engine_options_give_identical_proofs(ctx):
+    """Every engine setting through damascus_engine_create_with_options (callbacks,
+    no awake waits, admitting all first, no priority split, few waves): the
+    proofs are the plain path's."""
+    files = _files(98, [45_000, 180_000, 650_000, 2_500_000])
+    for kw in [dict(polling=False, spin_us=0), dict(admission_batch=0, priority_depth=0),
+               dict(max_waves=2, host_threads=2, spin_us=1000, admission_batch=2)]:
+        with D.Engine(ctx, **kw) as eng:
+            proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
+        for (d, s), p in zip(files, proofs):
+            assert p == ctx.prove(d, s, EPOCH), (kw, len(d))
