@@ -175,17 +175,54 @@ __global__ void __launch_bounds__(kGenThreads) gen_jobs_kernel(JobList<GenJob> J
     }
 }
 
-__global__ void __launch_bounds__(256) unpack_jobs_kernel(JobList<UnpackJob> J) {
+// A block unpacks kUnpackItems x 256 coefficients, i.e. 1024 x 13 = 13,312 bytes
+// of the file (a multiple of 16): when the file is 16-byte aligned and the
+// block's bytes lie inside it, they come in through shared memory in 16-byte
+// loads, and each coefficient's 13 bytes are assembled from four words.  Blocks
+// past the file's end (the square layout's zero padding) only write zeros.
+constexpr int kUnpackThreads = 256;
+constexpr int kUnpackItems = 4;
+constexpr uint32_t kUnpackBlockCoeffs = kUnpackThreads * kUnpackItems;
+constexpr uint32_t kUnpackBlockBytes = kUnpackBlockCoeffs * kBytesPerCoeff;
+static_assert(kUnpackBlockBytes % 16 == 0, "16-byte loads cover a block's bytes");
+
+__global__ void __launch_bounds__(kUnpackThreads) unpack_jobs_kernel(JobList<UnpackJob> J) {
+    __shared__ __align__(16) uint8_t bytes[kUnpackBlockBytes];
     const UnpackJob jb = J.j[find_job(J)];
-    const uint64_t j = (uint64_t)(blockIdx.x - jb.cta0) * 256 + threadIdx.x;
-    if (j >= jb.total) return;
-    uint32_t w[4] = {0, 0, 0, 0};
-    const uint64_t off = j * kBytesPerCoeff;
-    if (off < jb.len) {
-        const uint64_t n = jb.len - off < (uint64_t)kBytesPerCoeff ? jb.len - off : (uint64_t)kBytesPerCoeff;
-        for (uint32_t b = 0; b < n; ++b) w[b >> 2] |= (uint32_t)jb.file[off + b] << (8 * (b & 3));
+    const uint64_t j0 = (uint64_t)(blockIdx.x - jb.cta0) * kUnpackBlockCoeffs;
+    const uint64_t base = j0 * kBytesPerCoeff;
+    const bool staged = base + kUnpackBlockBytes <= jb.len && (reinterpret_cast<uintptr_t>(jb.file) & 15u) == 0;
+    if (staged) {  // uniform per block
+        const uint4* src = reinterpret_cast<const uint4*>(jb.file + base);
+        uint4* dst = reinterpret_cast<uint4*>(bytes);
+        for (uint32_t i = threadIdx.x; i < kUnpackBlockBytes / 16; i += kUnpackThreads) dst[i] = src[i];
+        __syncthreads();
     }
-    jb.dst[j] = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+    for (int it = 0; it < kUnpackItems; ++it) {
+        const uint32_t t = it * kUnpackThreads + threadIdx.x;  // coefficient within the block
+        const uint64_t j = j0 + t;
+        if (j >= jb.total) return;
+        uint32_t w[4] = {0, 0, 0, 0};
+        if (staged) {
+            // the coefficient's 13 bytes lie in the four words from its byte offset
+            // rounded down (the offset is at most 3 bytes into the first word)
+            const uint32_t bo = t * kBytesPerCoeff, sh = (bo & 3u) * 8u;
+            const uint32_t* words = reinterpret_cast<const uint32_t*>(bytes) + (bo >> 2);
+            const uint32_t v0 = words[0], v1 = words[1], v2 = words[2], v3 = words[3];
+            w[0] = __funnelshift_r(v0, v1, sh);
+            w[1] = __funnelshift_r(v1, v2, sh);
+            w[2] = __funnelshift_r(v2, v3, sh);
+            w[3] = (v3 >> sh) & 0xFFu;
+        } else {
+            const uint64_t off = j * kBytesPerCoeff;
+            if (off < jb.len) {
+                const uint64_t n = jb.len - off < (uint64_t)kBytesPerCoeff ? jb.len - off : (uint64_t)kBytesPerCoeff;
+                for (uint32_t b = 0; b < n; ++b) w[b >> 2] |= (uint32_t)jb.file[off + b] << (8 * (b & 3));
+            }
+        }
+        jb.dst[j] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
 }
 
 DM_D void load_block16(const uint8_t* p, uint32_t n, uint32_t m[16]) {
@@ -293,10 +330,11 @@ cudaError_t launch_unpack_jobs(UnpackJob* jobs, int n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (n > kMaxJobs) return cudaErrorInvalidValue;
     JobList<UnpackJob> JL;
-    const uint32_t ctas = assign_ctas<UnpackJob>(jobs, n, JL,
-                                                 [](const UnpackJob& j) -> uint64_t { return (j.total + 255) / 256; });
+    const uint32_t ctas = assign_ctas<UnpackJob>(jobs, n, JL, [](const UnpackJob& j) -> uint64_t {
+        return (j.total + kUnpackBlockCoeffs - 1) / kUnpackBlockCoeffs;
+    });
     if (!ctas) return cudaSuccess;
-    unpack_jobs_kernel<<<ctas, 256, 0, st>>>(JL);
+    unpack_jobs_kernel<<<ctas, kUnpackThreads, 0, st>>>(JL);
     return cudaGetLastError();
 }
 
