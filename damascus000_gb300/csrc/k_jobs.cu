@@ -20,6 +20,43 @@ constexpr int kFoldItems = 4;  // elements per thread
 __global__ void __launch_bounds__(kFoldThreads) fold_jobs_kernel(JobList<FoldJob> J) {
     const FoldJob jb = J.j[find_job(J)];
     const uint64_t base = (uint64_t)(blockIdx.x - jb.cta0) * kFoldThreads * kFoldItems + threadIdx.x;
+    if (jb.mode == kFoldVec || jb.mode == kFoldPoly || jb.mode == kFoldPolyX) {
+        // The folds the bytes go through (witness and generators): every item's two
+        // inputs loaded before the first multiply, so a thread has all its loads
+        // in flight at once.
+        uint4 va[kFoldItems], vb[kFoldItems];
+        bool neg[kFoldItems];
+#pragma unroll
+        for (int it = 0; it < kFoldItems; ++it) {
+            const uint64_t e = base + (uint64_t)it * kFoldThreads;
+            neg[it] = false;
+            if (e >= jb.n) continue;
+            if (jb.mode == kFoldVec) {
+                va[it] = jb.a[e];
+                vb[it] = jb.b[e];
+            } else {
+                const uint32_t h = 1u << jb.Lout;
+                const uint64_t b2 = (e >> jb.Lout) << (jb.Lout + 1);
+                const uint32_t j = (uint32_t)(e & (h - 1));
+                va[it] = jb.a[b2 + 2 * j];
+                if (jb.mode == kFoldPolyX) {
+                    neg[it] = j == 0;  // X * odd wraps its top coefficient around with a sign
+                    vb[it] = jb.a[j == 0 ? b2 + 2 * h - 1 : b2 + 2 * j - 1];
+                } else {
+                    vb[it] = jb.a[b2 + 2 * j + 1];
+                }
+            }
+        }
+#pragma unroll
+        for (int it = 0; it < kFoldItems; ++it) {
+            const uint64_t e = base + (uint64_t)it * kFoldThreads;
+            if (e >= jb.n) return;
+            fq b{{vb[it].x, vb[it].y, vb[it].z, vb[it].w}};
+            if (neg[it]) b = fq_neg(b);
+            stq(jb.dst, e, fq_fma(fq{{va[it].x, va[it].y, va[it].z, va[it].w}}, jb.x, b));
+        }
+        return;
+    }
 #pragma unroll
     for (int it = 0; it < kFoldItems; ++it) {
         const uint64_t e = base + (uint64_t)it * kFoldThreads;
