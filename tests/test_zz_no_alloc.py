@@ -5,7 +5,8 @@ whose device allocator belongs to another framework.
 Checks damascus_file_id_noalloc through the C ABI against the allocating
 damascus_file_id, bit-exact, on two calls in a row per input (the static
 scratch keeps the previous call's contents), that a call leaves the device's
-free memory unchanged, and the size limit.  Collected last on purpose."""
+free memory unchanged, that it captures into a CUDA graph and replays there,
+and the size limit.  Collected last on purpose."""
 import ctypes
 
 import pytest
@@ -55,6 +56,31 @@ def test_file_id_noalloc_leaves_free_memory_unchanged(ctx):
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
     assert bytes(out.cpu().tolist()) == ctx.file_id(data)
+
+
+def test_file_id_noalloc_replays_from_a_cuda_graph(ctx):
+    """The call captured into a CUDA graph once (after a first call outside
+    capture resolved the array's address), then replayed over new contents of
+    the same input buffer: each replay gives that content's file id."""
+    torch = pytest.importorskip("torch")
+    lib = D.load()
+    n = (2 << 20) + 77
+    first, _ = synth.random_file(79, n, 0)
+    second, _ = synth.random_file(80, n, 0)
+    dev = torch.frombuffer(bytearray(first), dtype=torch.uint8).cuda()
+    out = torch.zeros(32, dtype=torch.uint8, device="cuda")
+    assert _call(lib, dev, n, out, torch.cuda.current_stream()) == D.OK
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, capture_error_mode="thread_local"):
+        rc = _call(lib, dev, n, out, torch.cuda.current_stream())
+    assert rc == D.OK
+    for data in (second, first, second):
+        dev.copy_(torch.frombuffer(bytearray(data), dtype=torch.uint8))
+        out.fill_(0xEE)
+        graph.replay()
+        torch.cuda.synchronize()
+        assert bytes(out.cpu().tolist()) == ctx.file_id(data)
 
 
 def test_file_id_noalloc_rejects_oversized_input():
