@@ -64,7 +64,7 @@ EXPORTED_SYMBOLS = (
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
     "damascus_engine_wait_timeout", "damascus_engine_cancel", "damascus_engine_set_request_timeout",
     "damascus_engine_set_admission_batch", "damascus_engine_create_with_options",
-    "damascus_engine_health",
+    "damascus_engine_health", "damascus_engine_result", "damascus_engine_release",
     "damascus_tuning_set", "damascus_tuning_get", "damascus_tuning_measure",
     "damascus_verify_service_create", "damascus_verify_service_destroy", "damascus_verify_service_submit",
     "damascus_verify_service_poll", "damascus_verify_service_wait", "damascus_verify_service_drain",
@@ -182,6 +182,8 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_poll", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_wait", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_take", i32, vp, u64, vp, sz)
+    sig("damascus_engine_result", i32, vp, u64, P(vp), P(sz))
+    sig("damascus_engine_release", i32, vp, u64)
     sig("damascus_engine_wait_timeout", i32, vp, u64, ctypes.c_double, P(sz), P(ctypes.c_double))
     sig("damascus_engine_cancel", i32, vp, u64)
     sig("damascus_engine_set_request_timeout", i32, vp, ctypes.c_double)
@@ -490,7 +492,7 @@ class Context:
         n = ctypes.c_size_t()
         self.check(self._lib.damascus_commit(self._h, data, len(data), seed_generators, out, cap, ctypes.byref(n)),
                    "commit")
-        return out.raw[:n.value]
+        return ctypes.string_at(out, n.value)
 
     def ring_mul_batch(self, a: bytes, b: bytes, n: int, count: int) -> bytes:
         out = ctypes.create_string_buffer(count * n * 16)
@@ -510,7 +512,7 @@ class Context:
         n = ctypes.c_size_t()
         self.check(self._lib.damascus_prove(self._h, data, len(data), seed_generators, epoch_seed, out, cap,
                                             ctypes.byref(n)), "prove")
-        return out.raw[:n.value]
+        return ctypes.string_at(out, n.value)
 
     def prove_device(self, d_file: int, length: int, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
                      epoch_seed: bytes = DEFAULT_EPOCH_SEED, out=None) -> bytes:
@@ -520,7 +522,7 @@ class Context:
         n = ctypes.c_size_t()
         self.check(self._lib.damascus_prove_device(self._h, ctypes.c_void_p(d_file), length, seed_generators,
                                                    epoch_seed, out, cap, ctypes.byref(n)), "prove_device")
-        return out.raw[:n.value]
+        return ctypes.string_at(out, n.value)
 
     def prove_device_timed(self, d_file: int, length: int, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
                            epoch_seed: bytes = DEFAULT_EPOCH_SEED, out=None):
@@ -533,7 +535,7 @@ class Context:
         self.check(self._lib.damascus_prove_device_timed(self._h, ctypes.c_void_p(d_file), length, seed_generators,
                                                          epoch_seed, out, cap, ctypes.byref(n), ctypes.byref(ms)),
                    "prove_device_timed")
-        return out.raw[:n.value], ms.value
+        return ctypes.string_at(out, n.value), ms.value
 
     def flush_l2(self) -> None:
         self.check(self._lib.damascus_ctx_flush_l2(self._h), "flush_l2")
@@ -602,7 +604,7 @@ class DamascusProver:
         ln = ctypes.c_size_t()
         self._ctx.check(self._lib.damascus_prover_fold_round(self._h, rnd, buf, cap, ctypes.byref(ln)),
                         f"fold_round({rnd})")
-        return buf.raw[:ln.value]
+        return ctypes.string_at(buf, ln.value)
 
     def fold_round_timed(self, rnd: int):
         """fold_round plus the reference's RoundOutput timings
@@ -615,8 +617,8 @@ class DamascusProver:
         t = [ctypes.c_double() for _ in range(3)]
         self._ctx.check(self._lib.damascus_prover_fold_round_timed(
             self._h, rnd, buf, cap, ctypes.byref(ln), *(ctypes.byref(x) for x in t)), f"fold_round({rnd})")
-        return buf.raw[:ln.value], {"vector_fold_ms": t[0].value, "poly_fold_ms": t[1].value,
-                                    "total_round_ms": t[2].value}
+        return ctypes.string_at(buf, ln.value), {"vector_fold_ms": t[0].value, "poly_fold_ms": t[1].value,
+                                                 "total_round_ms": t[2].value}
 
     def final_opening(self) -> Optional[bytes]:
         out = ctypes.create_string_buffer(16)
@@ -737,9 +739,13 @@ class Engine:
             return None
         if rc < 0:
             raise DamascusError(rc, f"engine request {ticket}: {self._ctx.last_error()}")
-        buf = ctypes.create_string_buffer(n.value)
-        self._ctx.check(self._lib.damascus_engine_take(self._h, ticket, buf, n.value), "engine take")
-        return buf.raw, lat.value
+        # one copy, straight from the engine's buffer into the returned bytes
+        ptr, size = ctypes.c_void_p(), ctypes.c_size_t()
+        self._ctx.check(self._lib.damascus_engine_result(self._h, ticket, ctypes.byref(ptr), ctypes.byref(size)),
+                        "engine result")
+        proof = ctypes.string_at(ptr.value, size.value) if size.value else b""
+        self._ctx.check(self._lib.damascus_engine_release(self._h, ticket), "engine release")
+        return proof, lat.value
 
     def wait(self, ticket: int, timeout_ms: Optional[float] = None):
         """(proof bytes, latency ms) once the request finished; with timeout_ms,

@@ -865,6 +865,26 @@ int damascus_engine_take(damascus_engine* e, uint64_t ticket, uint8_t* proof_out
     return DAMASCUS_OK;
 }
 
+int damascus_engine_result(damascus_engine* e, uint64_t ticket, const uint8_t** data, size_t* len) {
+    if (!e || !data || !len) return DAMASCUS_EINVAL;
+    std::lock_guard<std::mutex> g(e->mu);
+    auto it = e->results.find(ticket);
+    if (it == e->results.end()) return DAMASCUS_ESTATE;
+    *data = it->second.data();
+    *len = it->second.size();
+    return DAMASCUS_OK;
+}
+
+int damascus_engine_release(damascus_engine* e, uint64_t ticket) {
+    if (!e) return DAMASCUS_EINVAL;
+    std::lock_guard<std::mutex> g(e->mu);
+    auto it = e->results.find(ticket);
+    if (it == e->results.end()) return DAMASCUS_ESTATE;
+    e->results.erase(it);
+    e->status.erase(ticket);
+    return DAMASCUS_OK;
+}
+
 int damascus_engine_drain(damascus_engine* e) {
     if (!e) return DAMASCUS_EINVAL;
     e->e->drain();

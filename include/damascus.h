@@ -258,6 +258,14 @@ int damascus_engine_set_admission_batch(damascus_engine* e, int requests_per_pas
 int damascus_engine_health(damascus_engine* e, uint64_t* unfinished, double* ms_since_progress);
 /* Copies a finished proof out and forgets it (DAMASCUS_ESIZE keeps it). */
 int damascus_engine_take(damascus_engine* e, uint64_t ticket, uint8_t* proof_out, size_t cap);
+/* Points *data at a finished proof of *len bytes that the engine still holds
+ * (no copy): valid until damascus_engine_take or damascus_engine_release of the
+ * ticket, or the engine's destruction.  A binding that builds its own byte
+ * object from it copies the proof once.  DAMASCUS_ESTATE when the ticket has no
+ * finished proof waiting. */
+int damascus_engine_result(damascus_engine* e, uint64_t ticket, const uint8_t** data, size_t* len);
+/* Forgets a finished proof without copying it out. */
+int damascus_engine_release(damascus_engine* e, uint64_t ticket);
 int damascus_engine_drain(damascus_engine* e);
 int damascus_engine_stats(damascus_engine* e, uint64_t* completed, uint64_t* failed, uint64_t* waves,
                           uint64_t* launches, uint64_t* peak_reserved_bytes);

@@ -356,8 +356,11 @@ impl<'c> Engine<'c> {
         if rc < 0 {
             return self.ctx.check(rc).map(|_| (Vec::new(), 0.0));
         }
-        let mut out = vec![0u8; len];
-        self.ctx.check(unsafe { sys::damascus_engine_take(self.raw, ticket, out.as_mut_ptr(), len) })?;
+        // one copy, from the engine's buffer into the returned vector
+        let mut data: *const u8 = std::ptr::null();
+        self.ctx.check(unsafe { sys::damascus_engine_result(self.raw, ticket, &mut data, &mut len) })?;
+        let out = if len == 0 { Vec::new() } else { unsafe { std::slice::from_raw_parts(data, len) }.to_vec() };
+        self.ctx.check(unsafe { sys::damascus_engine_release(self.raw, ticket) })?;
         Ok((out, ms))
     }
 }

@@ -134,6 +134,8 @@ extern "C" {
     pub fn damascus_engine_set_admission_batch(e: *mut Engine, requests_per_pass: c_int) -> c_int;
     pub fn damascus_engine_health(e: *mut Engine, unfinished: *mut u64, ms_since_progress: *mut f64) -> c_int;
     pub fn damascus_engine_take(e: *mut Engine, ticket: u64, proof_out: *mut u8, cap: usize) -> c_int;
+    pub fn damascus_engine_result(e: *mut Engine, ticket: u64, data: *mut *const u8, len: *mut usize) -> c_int;
+    pub fn damascus_engine_release(e: *mut Engine, ticket: u64) -> c_int;
     pub fn damascus_engine_drain(e: *mut Engine) -> c_int;
     pub fn damascus_engine_stats(e: *mut Engine, completed: *mut u64, failed: *mut u64, waves: *mut u64, launches: *mut u64, peak_reserved_bytes: *mut u64) -> c_int;
     pub fn damascus_ctx_trace_start(ctx: *mut Ctx) -> c_int;

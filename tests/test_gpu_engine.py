@@ -328,3 +328,32 @@ def test_engine_options_give_identical_proofs(ctx):
             proofs = eng.prove_batch([(d, s, EPOCH) for d, s in files])
         for (d, s), p in zip(files, proofs):
             assert p == ctx.prove(d, s, EPOCH), (kw, len(d))
+
+
+def test_engine_result_view_and_release(ctx):
+    """damascus_engine_result points at the finished proof without copying it
+    (the same bytes the copying take gives), release forgets it, and a released
+    or already taken ticket answers ESTATE."""
+    lib = D.load()
+    files = _files(91, [60_000, 300_000, 1 << 20])
+    with D.Engine(ctx) as eng:
+        tickets = [eng.submit(d, s, EPOCH) for d, s in files]
+        n, lat = ctypes.c_size_t(), ctypes.c_double()
+        ptr, size = ctypes.c_void_p(), ctypes.c_size_t()
+        for t, (d, s) in zip(tickets, files):
+            assert lib.damascus_engine_wait(eng._h, t, ctypes.byref(n), ctypes.byref(lat)) == 1
+            assert lib.damascus_engine_result(eng._h, t, ctypes.byref(ptr), ctypes.byref(size)) == D.OK
+            assert size.value == n.value == D.proof_size(len(d))
+            viewed = ctypes.string_at(ptr.value, size.value)
+            assert viewed == ctx.prove(d, s, EPOCH)
+            if t == tickets[0]:
+                buf = ctypes.create_string_buffer(n.value)
+                assert lib.damascus_engine_take(eng._h, t, buf, n.value) == D.OK
+                assert buf.raw == viewed
+            else:
+                assert lib.damascus_engine_release(eng._h, t) == D.OK
+            assert lib.damascus_engine_result(eng._h, t, ctypes.byref(ptr), ctypes.byref(size)) == D.ESTATE
+            assert lib.damascus_engine_release(eng._h, t) == D.ESTATE
+        # the binding's wait copies once from the same view
+        t = eng.submit(*files[1], EPOCH)
+        assert eng.wait(t)[0] == ctx.prove(*files[1], EPOCH)
