@@ -60,6 +60,7 @@ EXPORTED_SYMBOLS = (
     "damascus_ctx_set_profiling", "damascus_ctx_reset_stats", "damascus_ctx_kernel_stat",
     "damascus_ctx_synchronize", "damascus_file_id_noalloc",
     "damascus_engine_create", "damascus_engine_destroy", "damascus_engine_submit", "damascus_engine_submit_device",
+    "damascus_engine_submit_borrowed",
     "damascus_engine_poll",
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
     "damascus_engine_wait_timeout", "damascus_engine_cancel", "damascus_engine_set_request_timeout",
@@ -179,6 +180,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_destroy", None, vp)
     sig("damascus_engine_submit", i32, vp, cp, sz, cp, cp, P(u64))
     sig("damascus_engine_submit_device", i32, vp, vp, sz, cp, cp, P(u64))
+    sig("damascus_engine_submit_borrowed", i32, vp, vp, sz, cp, cp, P(u64))
     sig("damascus_engine_poll", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_wait", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_take", i32, vp, u64, vp, sz)
@@ -717,8 +719,19 @@ class Engine:
                         "engine submit_device")
         return t.value
 
+    def submit_borrowed(self, ptr: int, length: int, seed_generators: bytes = DEFAULT_GENERATOR_SEED,
+                        epoch_seed: bytes = DEFAULT_EPOCH_SEED) -> int:
+        """Submit from a raw host address that stays valid and unchanged until the
+        request finishes (pinned memory: an asynchronous copy): the engine's
+        host-to-device copy reads it directly, with no staging copy."""
+        t = ctypes.c_uint64()
+        self._ctx.check(self._lib.damascus_engine_submit_borrowed(self._h, ctypes.c_void_p(ptr), length,
+                                                                  seed_generators, epoch_seed, ctypes.byref(t)),
+                        "engine submit_borrowed")
+        return t.value
+
     def submit_ptr(self, ptr: int, length: int, seed_generators: bytes, epoch_seed: bytes) -> int:
-        """Submit from a raw host address (e.g. pinned memory)."""
+        """Submit from a raw host address (e.g. pinned memory), copied before return."""
         t = ctypes.c_uint64()
         self._ctx.check(self._lib.damascus_engine_submit(self._h, ctypes.c_char_p(ptr), length, seed_generators,
                                                          epoch_seed, ctypes.byref(t)), "engine submit")

@@ -760,7 +760,14 @@ int damascus_engine_submit(damascus_engine* e, const uint8_t* file, size_t len, 
 int damascus_engine_submit_device(damascus_engine* e, const void* d_file, size_t len,
                                   const uint8_t seed_generators[32], const uint8_t epoch_seed[32], uint64_t* ticket) {
     if (!e) return DAMASCUS_EINVAL;
-    return e->e->submit(static_cast<const uint8_t*>(d_file), len, seed_generators, epoch_seed, ticket, true);
+    return e->e->submit(static_cast<const uint8_t*>(d_file), len, seed_generators, epoch_seed, ticket,
+                        Engine::FileSource::kDevice);
+}
+
+int damascus_engine_submit_borrowed(damascus_engine* e, const uint8_t* file, size_t len,
+                                    const uint8_t seed_generators[32], const uint8_t epoch_seed[32], uint64_t* ticket) {
+    if (!e) return DAMASCUS_EINVAL;
+    return e->e->submit(file, len, seed_generators, epoch_seed, ticket, Engine::FileSource::kHostBorrowed);
 }
 
 static int engine_result(damascus_engine* e, uint64_t ticket, bool block, size_t* proof_len, double* latency_ms) {

@@ -16,7 +16,8 @@ struct Engine::Request {
     uint64_t ticket = 0;
     uint8_t* pinned_file = nullptr;  // staged copy of the file (pinned host memory)
     size_t pinned_bytes = 0;
-    const uint8_t* device_file = nullptr;  // caller-owned device copy instead
+    const uint8_t* caller_file = nullptr;  // the caller's device or host buffer instead (no staging)
+    bool on_device = false;
     uint64_t len = 0;
     uint8_t seed[32], epoch[32];
     std::unique_ptr<ProofState> ps;
@@ -150,15 +151,16 @@ int Engine::take_wave_stream(bool high) {
 }
 
 int Engine::submit(const uint8_t* file, uint64_t len, const uint8_t seed[32], const uint8_t epoch[32],
-                   uint64_t* ticket, bool on_device) {
+                   uint64_t* ticket, FileSource source) {
     if ((!file && len) || !seed || !epoch || !ticket) return kEInval;
     std::unique_ptr<Request> r(new Request());
     r->len = len;
     std::memcpy(r->seed, seed, 32);
     std::memcpy(r->epoch, epoch, 32);
     r->footprint = ProofState::footprint(len);
-    if (on_device) {
-        r->device_file = file;
+    if (source != FileSource::kHostCopy) {
+        r->caller_file = file;
+        r->on_device = source == FileSource::kDevice;
     } else {
         r->pinned_bytes = len ? len : 1;
         r->pinned_file = static_cast<uint8_t*>(ctx_->get_pinned(r->pinned_bytes));
@@ -310,9 +312,9 @@ void Engine::scheduler() {
             }
             queued_.pop_front();
             lk.unlock();
-            const bool dev = r->device_file != nullptr;
+            const bool dev = r->on_device;
             const Clock::time_point t_admit = Clock::now();
-            const int rc = r->ps->setup(dev ? r->device_file : r->pinned_file, r->len, dev, r->seed, r->epoch,
+            const int rc = r->ps->setup(r->caller_file ? r->caller_file : r->pinned_file, r->len, dev, r->seed, r->epoch,
                                         ctx_->max_preprocess(), stream_);
             const double admit_ms = std::chrono::duration<double, std::milli>(Clock::now() - t_admit).count();
             lk.lock();

@@ -61,11 +61,16 @@ class Engine {
     // (the engine then runs nothing and must be destroyed).
     const std::string& init_error() const { return init_error_; }
 
-    // Copies the file; returns a ticket.  Never blocks on the GPU.  With
-    // on_device the file is a device pointer that must stay valid until the
-    // request finishes (no copy is made).
+    // Where a submitted file lives.  kHostCopy: host memory the engine copies
+    // into its own pinned staging before submit returns, so the caller may reuse
+    // it at once.  kDevice: device memory.  kHostBorrowed: host memory that the
+    // request's host-to-device copy reads directly, with no staging copy (page-
+    // locked memory makes that copy asynchronous).  The last two must stay valid
+    // and unchanged until the request finishes.
+    enum class FileSource { kHostCopy, kDevice, kHostBorrowed };
+    // Returns a ticket.  Never blocks on the GPU.
     int submit(const uint8_t* file, uint64_t len, const uint8_t seed[32], const uint8_t epoch[32], uint64_t* ticket,
-               bool on_device = false);
+               FileSource source = FileSource::kHostCopy);
     // 1 = finished (proof moved out), 0 = still running, < 0 = the request failed.
     int poll(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err);
     // Blocks until the ticket finishes; same results as poll.

@@ -225,6 +225,12 @@ int damascus_engine_submit(damascus_engine* e, const uint8_t* file, size_t len, 
  * request finishes. */
 int damascus_engine_submit_device(damascus_engine* e, const void* d_file, size_t len,
                                   const uint8_t seed_generators[32], const uint8_t epoch_seed[32], uint64_t* ticket);
+/* Same with the file in host memory that the caller keeps valid and unchanged
+ * until the request finishes: the engine's host-to-device copy reads it
+ * directly, with no copy into the engine's staging buffer.  Page-locked memory
+ * (cudaHostAlloc, cudaHostRegister) keeps that copy asynchronous. */
+int damascus_engine_submit_borrowed(damascus_engine* e, const uint8_t* file, size_t len,
+                                    const uint8_t seed_generators[32], const uint8_t epoch_seed[32], uint64_t* ticket);
 /* 1 = finished (proof kept for damascus_engine_take), 0 = running, < 0 = failed. */
 int damascus_engine_poll(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms);
 /* Blocks until the ticket finishes; same results as poll. */

@@ -126,6 +126,7 @@ extern "C" {
     pub fn damascus_engine_destroy(e: *mut Engine);
     pub fn damascus_engine_submit(e: *mut Engine, file: *const u8, len: usize, seed_generators: *const u8, epoch_seed: *const u8, ticket: *mut u64) -> c_int;
     pub fn damascus_engine_submit_device(e: *mut Engine, d_file: *const c_void, len: usize, seed_generators: *const u8, epoch_seed: *const u8, ticket: *mut u64) -> c_int;
+    pub fn damascus_engine_submit_borrowed(e: *mut Engine, file: *const u8, len: usize, seed_generators: *const u8, epoch_seed: *const u8, ticket: *mut u64) -> c_int;
     pub fn damascus_engine_poll(e: *mut Engine, ticket: u64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
     pub fn damascus_engine_wait(e: *mut Engine, ticket: u64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
     pub fn damascus_engine_wait_timeout(e: *mut Engine, ticket: u64, timeout_ms: f64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;

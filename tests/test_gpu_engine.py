@@ -357,3 +357,20 @@ def test_engine_result_view_and_release(ctx):
         # the binding's wait copies once from the same view
         t = eng.submit(*files[1], EPOCH)
         assert eng.wait(t)[0] == ctx.prove(*files[1], EPOCH)
+
+
+def test_engine_borrowed_host_submission(ctx):
+    """Files submitted from the caller's own host memory (pinned, and pageable)
+    without a staging copy give the proofs of the copying submission."""
+    torch = pytest.importorskip("torch")
+    files = _files(93, [0, 1, 60_000, 700_000, 3 << 20])
+    pinned = [torch.frombuffer(bytearray(d or b"\0"), dtype=torch.uint8).pin_memory() for d, _ in files]
+    pageable = [ctypes.create_string_buffer(d, len(d) or 1) for d, _ in files]
+    with D.Engine(ctx) as eng:
+        want = [eng.wait(eng.submit(d, s, EPOCH))[0] for d, s in files]
+        got_pinned = [eng.wait(t)[0] for t in [eng.submit_borrowed(p.data_ptr(), len(d), s, EPOCH)
+                                              for p, (d, s) in zip(pinned, files)]]
+        got_pageable = [eng.wait(t)[0] for t in [eng.submit_borrowed(ctypes.addressof(b), len(d), s, EPOCH)
+                                                for b, (d, s) in zip(pageable, files)]]
+    assert got_pinned == want and got_pageable == want
+    assert want[-1] == ctx.prove(*files[-1], EPOCH)
