@@ -518,6 +518,13 @@ def host_hash_rate(D, nbytes: int = 64 << 20, reps: int = 5):
     return reps * len(data) / (time.perf_counter() - t0) / 1e9
 
 
+def collect(eng, tickets):
+    """[(proof, latency ms)] in ticket order, each proof taken as soon as its
+    request finishes (Engine.as_completed), not in submission order."""
+    got = {t: (p, lat) for t, p, lat in eng.as_completed(tickets)}
+    return [got[t] for t in tickets]
+
+
 def measure_batched(ctx, D, torch, args, rank, world, ranks):
     """The 64-file batched set (log-uniform 50 KB - 4 MiB, d 6-10): one engine batch
     per step against the plain one-at-a-time path, every proof checked against the
@@ -529,8 +536,8 @@ def measure_batched(ctx, D, torch, args, rank, world, ranks):
     torch.cuda.synchronize()
     with D.Engine(ctx) as eng:
         def batch():
-            return [eng.wait(t)[0] for t in
-                    [eng.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]]
+            ts = [eng.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]
+            return [r[0] for r in collect(eng, ts)]
         for _ in range(args.warmup):
             batch()
         ranks.barrier()
@@ -833,7 +840,7 @@ def run_gpu(args, wl):
 
         def replay_device():
             ts = [eng.submit_device(t.data_ptr(), len(d), s, EPOCH) for t, (d, s, _) in zip(dev, files)]
-            return [eng.wait(t) for t in ts]
+            return collect(eng, ts)
 
         # warm-up (also checks the engine against the plain path on a few files)
         for _ in range(args.warmup):
@@ -891,7 +898,7 @@ def run_gpu(args, wl):
         d2h = 0
         for _ in range(args.steps):
             ts = [eng.submit_borrowed(p.data_ptr(), len(d), s, EPOCH) for p, (d, s, _) in zip(pinned, files)]
-            outs = [eng.wait(t) for t in ts]
+            outs = collect(eng, ts)
             d2h = sum(len(o[0]) for o in outs)
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(time.perf_counter() - t0) / args.steps
@@ -903,7 +910,7 @@ def run_gpu(args, wl):
         t0 = time.perf_counter()
         for _ in range(staged_steps):
             ts = [eng.submit_ptr(p.data_ptr(), len(d), s, EPOCH) for p, (d, s, _) in zip(pinned, files)]
-            staged = [eng.wait(t) for t in ts]
+            staged = collect(eng, ts)
         torch.cuda.synchronize()
         staged_s = max_over_ranks(time.perf_counter() - t0) / staged_steps
         staged_same = sum(a[0] == b[0] for a, b in zip(staged, outs))

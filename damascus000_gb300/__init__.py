@@ -60,7 +60,7 @@ EXPORTED_SYMBOLS = (
     "damascus_ctx_set_profiling", "damascus_ctx_reset_stats", "damascus_ctx_kernel_stat",
     "damascus_ctx_synchronize", "damascus_file_id_noalloc",
     "damascus_engine_create", "damascus_engine_destroy", "damascus_engine_submit", "damascus_engine_submit_device",
-    "damascus_engine_submit_borrowed",
+    "damascus_engine_submit_borrowed", "damascus_engine_wait_any",
     "damascus_engine_poll",
     "damascus_engine_wait", "damascus_engine_take", "damascus_engine_drain", "damascus_engine_stats",
     "damascus_engine_wait_timeout", "damascus_engine_cancel", "damascus_engine_set_request_timeout",
@@ -181,6 +181,7 @@ def _declare(L: ctypes.CDLL) -> None:
     sig("damascus_engine_submit", i32, vp, cp, sz, cp, cp, P(u64))
     sig("damascus_engine_submit_device", i32, vp, vp, sz, cp, cp, P(u64))
     sig("damascus_engine_submit_borrowed", i32, vp, vp, sz, cp, cp, P(u64))
+    sig("damascus_engine_wait_any", i32, vp, P(u64), sz, P(sz))
     sig("damascus_engine_poll", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_wait", i32, vp, u64, P(sz), P(ctypes.c_double))
     sig("damascus_engine_take", i32, vp, u64, vp, sz)
@@ -764,6 +765,19 @@ class Engine:
         """(proof bytes, latency ms) once the request finished; with timeout_ms,
         None when it has not finished by then (it keeps running)."""
         return self._result(ticket, True, timeout_ms)
+
+    def as_completed(self, tickets):
+        """Yields (ticket, proof bytes, latency ms) for every ticket, in the order
+        the requests finish; a failed request raises when its turn comes."""
+        pending = list(tickets)
+        which = ctypes.c_size_t()
+        while pending:
+            arr = (ctypes.c_uint64 * len(pending))(*pending)
+            self._ctx.check(self._lib.damascus_engine_wait_any(self._h, arr, len(pending), ctypes.byref(which)),
+                            "engine wait_any")
+            t = pending.pop(which.value)
+            proof, lat = self._result(t, True)
+            yield t, proof, lat
 
     def cancel(self, ticket: int) -> None:
         """Ends the request early (queued: at once; admitted: at its next stage

@@ -805,6 +805,19 @@ int damascus_engine_wait(damascus_engine* e, uint64_t ticket, size_t* proof_len,
     return engine_result(e, ticket, true, proof_len, latency_ms);
 }
 
+int damascus_engine_wait_any(damascus_engine* e, const uint64_t* tickets, size_t n, size_t* which) {
+    if (!e || !tickets || !which || n == 0) return DAMASCUS_EINVAL;
+    {
+        std::lock_guard<std::mutex> g(e->mu);  // one collected earlier (by poll or wait) counts as finished
+        for (size_t i = 0; i < n; ++i)
+            if (e->status.count(tickets[i])) {
+                *which = i;
+                return DAMASCUS_OK;
+            }
+    }
+    return e->e->wait_any(tickets, n, which);
+}
+
 int damascus_engine_wait_timeout(damascus_engine* e, uint64_t ticket, double timeout_ms, size_t* proof_len,
                                  double* latency_ms) {
     if (!e) return DAMASCUS_EINVAL;

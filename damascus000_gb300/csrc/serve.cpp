@@ -557,6 +557,27 @@ int Engine::wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_m
     return poll(ticket, proof, latency_ms, err);
 }
 
+int Engine::wait_any(const uint64_t* tickets, size_t n, size_t* which) {
+    if (!tickets || !which) return kEInval;
+    std::unique_lock<std::mutex> lk(mu_);
+    std::vector<std::pair<size_t, const Request*>> known;
+    known.reserve(n);
+    for (size_t i = 0; i < n; ++i) {
+        auto it = all_.find(tickets[i]);
+        if (it != all_.end()) known.emplace_back(i, it->second.get());
+    }
+    if (known.empty()) return kEInval;
+    done_cv_.wait(lk, [&] {
+        for (const auto& k : known)
+            if (k.second->state == Request::Done || k.second->state == Request::Failed) {
+                *which = k.first;
+                return true;
+            }
+        return false;
+    });
+    return kOk;
+}
+
 int Engine::wait_for(uint64_t ticket, double timeout_ms, std::vector<uint8_t>* proof, double* latency_ms,
                      std::string* err) {
     {

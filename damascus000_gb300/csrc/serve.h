@@ -75,6 +75,10 @@ class Engine {
     int poll(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err);
     // Blocks until the ticket finishes; same results as poll.
     int wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err);
+    // Blocks until one of the n tickets has finished (proof ready or failed) and
+    // sets *which to its index; poll then returns its result at once.  Tickets
+    // the engine does not know are skipped (kEInval when it knows none of them).
+    int wait_any(const uint64_t* tickets, size_t n, size_t* which);
     // wait with a limit: kETimeout when the request has not finished within
     // timeout_ms (it keeps running; the ticket stays valid).
     int wait_for(uint64_t ticket, double timeout_ms, std::vector<uint8_t>* proof, double* latency_ms,

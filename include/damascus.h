@@ -235,6 +235,12 @@ int damascus_engine_submit_borrowed(damascus_engine* e, const uint8_t* file, siz
 int damascus_engine_poll(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms);
 /* Blocks until the ticket finishes; same results as poll. */
 int damascus_engine_wait(damascus_engine* e, uint64_t ticket, size_t* proof_len, double* latency_ms);
+/* Blocks until one of the n tickets has finished (its proof is ready or it
+ * failed) and sets *which to that ticket's index in tickets; poll or wait then
+ * returns its result at once.  A client collecting many requests takes each
+ * proof as soon as it is ready this way, not in submission order.  Tickets the
+ * engine does not know are skipped; DAMASCUS_EINVAL when it knows none. */
+int damascus_engine_wait_any(damascus_engine* e, const uint64_t* tickets, size_t n, size_t* which);
 /* wait with a limit: DAMASCUS_ETIMEOUT when the request has not finished within
  * timeout_ms; it keeps running and the ticket stays valid. */
 int damascus_engine_wait_timeout(damascus_engine* e, uint64_t ticket, double timeout_ms, size_t* proof_len,

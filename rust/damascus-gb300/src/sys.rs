@@ -129,6 +129,7 @@ extern "C" {
     pub fn damascus_engine_submit_borrowed(e: *mut Engine, file: *const u8, len: usize, seed_generators: *const u8, epoch_seed: *const u8, ticket: *mut u64) -> c_int;
     pub fn damascus_engine_poll(e: *mut Engine, ticket: u64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
     pub fn damascus_engine_wait(e: *mut Engine, ticket: u64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
+    pub fn damascus_engine_wait_any(e: *mut Engine, tickets: *const u64, n: usize, which: *mut usize) -> c_int;
     pub fn damascus_engine_wait_timeout(e: *mut Engine, ticket: u64, timeout_ms: f64, proof_len: *mut usize, latency_ms: *mut f64) -> c_int;
     pub fn damascus_engine_cancel(e: *mut Engine, ticket: u64) -> c_int;
     pub fn damascus_engine_set_request_timeout(e: *mut Engine, timeout_ms: f64) -> c_int;

@@ -374,3 +374,21 @@ def test_engine_borrowed_host_submission(ctx):
                                                 for b, (d, s) in zip(pageable, files)]]
     assert got_pinned == want and got_pageable == want
     assert want[-1] == ctx.prove(*files[-1], EPOCH)
+
+
+def test_engine_as_completed_yields_every_request_once(ctx):
+    """wait_any / as_completed hand back every ticket once, each with the proof
+    the ticket-order wait gives, the small requests ahead of the large one."""
+    files = _files(95, [3 << 20, 2_000, 60_000, 8_000, 300_000])
+    with D.Engine(ctx) as eng:
+        tickets = [eng.submit(d, s, EPOCH) for d, s in files]
+        got = list(eng.as_completed(tickets))
+        assert sorted(t for t, _, _ in got) == sorted(tickets)
+        by_ticket = {t: p for t, p, _ in got}
+        for t, (d, s) in zip(tickets, files):
+            assert by_ticket[t] == ctx.prove(d, s, EPOCH)
+        assert got[-1][0] == tickets[0]  # the 3 MiB file (depth 10) finishes last
+        lib = D.load()
+        arr = (ctypes.c_uint64 * 2)(987654321, 987654322)
+        which = ctypes.c_size_t()
+        assert lib.damascus_engine_wait_any(eng._h, arr, 2, ctypes.byref(which)) == D.EINVAL
