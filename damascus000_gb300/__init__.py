@@ -752,7 +752,9 @@ class Engine:
         if rc == 0:
             return None
         if rc < 0:
-            raise DamascusError(rc, f"engine request {ticket}: {self._ctx.last_error()}")
+            msg = self._ctx.last_error()
+            self._lib.damascus_engine_release(self._h, ticket)  # the failure is reported once, here
+            raise DamascusError(rc, f"engine request {ticket}: {msg}")
         # one copy, straight from the engine's buffer into the returned bytes
         ptr, size = ctypes.c_void_p(), ctypes.c_size_t()
         self._ctx.check(self._lib.damascus_engine_result(self._h, ticket, ctypes.byref(ptr), ctypes.byref(size)),
