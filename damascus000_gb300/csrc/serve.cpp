@@ -546,13 +546,19 @@ int Engine::poll(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_m
     return rc;
 }
 
+bool Engine::finished_or_gone(uint64_t ticket) const {
+    // a ticket another thread has collected meanwhile is gone (its request freed)
+    auto it = all_.find(ticket);
+    if (it == all_.end()) return true;
+    const Request* r = it->second.get();
+    return r->state == Request::Done || r->state == Request::Failed;
+}
+
 int Engine::wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_ms, std::string* err) {
     {
         std::unique_lock<std::mutex> lk(mu_);
-        auto it = all_.find(ticket);
-        if (it == all_.end()) return kEInval;
-        Request* r = it->second.get();
-        done_cv_.wait(lk, [&] { return r->state == Request::Done || r->state == Request::Failed; });
+        if (!all_.count(ticket)) return kEInval;
+        done_cv_.wait(lk, [&] { return finished_or_gone(ticket); });
     }
     return poll(ticket, proof, latency_ms, err);
 }
@@ -560,17 +566,15 @@ int Engine::wait(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_m
 int Engine::wait_any(const uint64_t* tickets, size_t n, size_t* which) {
     if (!tickets || !which) return kEInval;
     std::unique_lock<std::mutex> lk(mu_);
-    std::vector<std::pair<size_t, const Request*>> known;
+    std::vector<size_t> known;
     known.reserve(n);
-    for (size_t i = 0; i < n; ++i) {
-        auto it = all_.find(tickets[i]);
-        if (it != all_.end()) known.emplace_back(i, it->second.get());
-    }
+    for (size_t i = 0; i < n; ++i)
+        if (all_.count(tickets[i])) known.push_back(i);
     if (known.empty()) return kEInval;
     done_cv_.wait(lk, [&] {
-        for (const auto& k : known)
-            if (k.second->state == Request::Done || k.second->state == Request::Failed) {
-                *which = k.first;
+        for (size_t i : known)
+            if (finished_or_gone(tickets[i])) {
+                *which = i;
                 return true;
             }
         return false;
@@ -582,12 +586,10 @@ int Engine::wait_for(uint64_t ticket, double timeout_ms, std::vector<uint8_t>* p
                      std::string* err) {
     {
         std::unique_lock<std::mutex> lk(mu_);
-        auto it = all_.find(ticket);
-        if (it == all_.end()) return kEInval;
-        Request* r = it->second.get();
+        if (!all_.count(ticket)) return kEInval;
         const bool done = done_cv_.wait_for(
             lk, std::chrono::microseconds((int64_t)(timeout_ms > 0 ? timeout_ms * 1000.0 : 0)),
-            [&] { return r->state == Request::Done || r->state == Request::Failed; });
+            [&] { return finished_or_gone(ticket); });
         if (!done) return kETimeout;
     }
     return poll(ticket, proof, latency_ms, err);

@@ -123,6 +123,10 @@ class Engine {
     void scheduler();
     void worker();
     void finish_request(Request* r);
+    // The ticket's request has finished, or another thread has already collected
+    // it (mu_ held): waits look the ticket up again on every wake-up instead of
+    // holding a pointer to a request that a collector may free.
+    bool finished_or_gone(uint64_t ticket) const;
     // kECanceled / kETimeout when r must end at this boundary, else 0 (mu_ held).
     int abort_code(const Request* r, std::chrono::steady_clock::time_point now) const;
 

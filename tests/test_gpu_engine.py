@@ -392,3 +392,49 @@ def test_engine_as_completed_yields_every_request_once(ctx):
         arr = (ctypes.c_uint64 * 2)(987654321, 987654322)
         which = ctypes.c_size_t()
         assert lib.damascus_engine_wait_any(eng._h, arr, 2, ctypes.byref(which)) == D.EINVAL
+
+
+def test_engine_concurrent_collectors(ctx):
+    """Several threads wait on the same tickets while others take them: every
+    ticket is collected, and a waiter whose ticket another thread took gets an
+    answer (its result, kept by the C layer, or EINVAL) instead of waiting on a
+    freed request."""
+    import threading
+    lib = D.load()
+    files = _files(99, [2_000, 60_000, 200_000, 8_000, 700_000, 30_000])
+    with D.Engine(ctx) as eng:
+        tickets = [eng.submit(d, s, EPOCH) for d, s in files]
+        answers, errors = [], []
+
+        def waiter():
+            try:
+                n, lat = ctypes.c_size_t(), ctypes.c_double()
+                for t in tickets:
+                    answers.append((t, lib.damascus_engine_wait(eng._h, t, ctypes.byref(n), ctypes.byref(lat))))
+            except Exception as e:  # pragma: no cover - reported below
+                errors.append(e)
+
+        def any_waiter():
+            try:
+                arr = (ctypes.c_uint64 * len(tickets))(*tickets)
+                which = ctypes.c_size_t()
+                for _ in range(len(tickets)):
+                    rc = lib.damascus_engine_wait_any(eng._h, arr, len(tickets), ctypes.byref(which))
+                    answers.append(("any", rc))
+            except Exception as e:  # pragma: no cover
+                errors.append(e)
+
+        threads = [threading.Thread(target=f) for f in (waiter, waiter, any_waiter, any_waiter)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join(timeout=120)
+        assert not any(th.is_alive() for th in threads) and not errors
+        assert all(rc in (1, D.EINVAL) for t, rc in answers if t != "any")
+        assert all(rc in (D.OK, D.EINVAL) for t, rc in answers if t == "any")
+        for t, (d, s) in zip(tickets, files):
+            n, lat = ctypes.c_size_t(), ctypes.c_double()
+            assert lib.damascus_engine_poll(eng._h, t, ctypes.byref(n), ctypes.byref(lat)) == 1
+            buf = ctypes.create_string_buffer(n.value)
+            assert lib.damascus_engine_take(eng._h, t, buf, n.value) == D.OK
+            assert buf.raw == ctx.prove(d, s, EPOCH)
