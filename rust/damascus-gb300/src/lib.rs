@@ -349,6 +349,26 @@ impl<'c> Engine<'c> {
         Ok(ticket)
     }
 
+    /// Submits a file the engine reads in place (no staging copy).
+    ///
+    /// # Safety
+    /// `file` must stay valid and unchanged until the request finishes (its
+    /// `wait` returned); page-locked memory keeps the device copy asynchronous.
+    pub unsafe fn submit_borrowed(&self, file: &[u8], seed_generators: &[u8; 32], epoch_seed: &[u8; 32]) -> Result<u64> {
+        let mut ticket = 0u64;
+        self.ctx.check(sys::damascus_engine_submit_borrowed(self.raw, file.as_ptr(), file.len(), seed_generators.as_ptr(),
+                                                            epoch_seed.as_ptr(), &mut ticket))?;
+        Ok(ticket)
+    }
+
+    /// Blocks until one of `tickets` has finished; returns its index (its `wait`
+    /// then returns at once), so proofs are taken in the order they finish.
+    pub fn wait_any(&self, tickets: &[u64]) -> Result<usize> {
+        let mut which = 0usize;
+        self.ctx.check(unsafe { sys::damascus_engine_wait_any(self.raw, tickets.as_ptr(), tickets.len(), &mut which) })?;
+        Ok(which)
+    }
+
     /// Blocks until the ticket finishes: (proof, latency in ms).
     pub fn wait(&self, ticket: u64) -> Result<(Vec<u8>, f64)> {
         let (mut len, mut ms) = (0usize, 0f64);
