@@ -32,6 +32,10 @@ struct Engine::Request {
     Clock::time_point deadline{};
     // current stage, for the launch trace: ready, its wave launched, landed
     Clock::time_point t_ready{}, t_launch{}, t_landed{};
+    // Recorded on the admission stream after the request's setup (allocations,
+    // file upload): its first wave waits on it, and no other wave does.
+    cudaEvent_t admitted = nullptr;
+    bool first_wave = true;
 };
 
 struct Engine::Wave {
@@ -129,6 +133,7 @@ Engine::~Engine() {
         cudaStreamDestroy(s);
     }
     if (admit_ev_) cudaEventDestroy(admit_ev_);
+    for (cudaEvent_t ev : free_admit_events_) cudaEventDestroy(ev);
     for (cudaEvent_t ev : wave_events_)
         if (ev) cudaEventDestroy(ev);
     if (stream_) {
@@ -327,6 +332,12 @@ void Engine::scheduler() {
                 lk.lock();
                 continue;
             }
+            r->admitted = take_admit_event();
+            if (r->admitted && cudaEventRecord(r->admitted, stream_) != cudaSuccess) {
+                cudaGetLastError();
+                free_admit_events_.push_back(r->admitted);
+                r->admitted = nullptr;  // its first wave waits for the whole admission stream instead
+            }
             r->state = Request::Active;
             if (active_++ == 0) active_since_ = Clock::now();
             r->t_ready = Clock::now();
@@ -391,9 +402,20 @@ void Engine::launch_wave(std::vector<Request*> reqs, bool high, std::unique_lock
     for (Request* r : w->reqs) r->t_launch = t_launch;
     NvtxRange range(high ? "wave (deep)" : "wave");
     cudaStream_t ws = wave_streams_[si];
-    // admissions (allocations, file copies) on stream_ precede the wave's kernels
-    cudaEventRecord(admit_ev_, stream_);
-    cudaStreamWaitEvent(ws, admit_ev_, 0);
+    // a request's admission (allocations, file upload on stream_) precedes its first
+    // wave's kernels; later waves have nothing to wait for there, in particular not
+    // the uploads of requests admitted since
+    bool wait_all = false;
+    for (Request* r : w->reqs) {
+        if (!r->first_wave) continue;
+        r->first_wave = false;
+        if (r->admitted) cudaStreamWaitEvent(ws, r->admitted, 0);
+        else wait_all = true;
+    }
+    if (wait_all) {
+        cudaEventRecord(admit_ev_, stream_);
+        cudaStreamWaitEvent(ws, admit_ev_, 0);
+    }
     Plan plan;
     for (Request* r : w->reqs) r->ps->plan_stage(plan);
     std::string err;
@@ -514,6 +536,8 @@ void Engine::finish_request(Request* r) {
         std::lock_guard<std::mutex> g(mu_);
         if (r->pinned_file) ctx_->put_pinned(r->pinned_file, r->pinned_bytes);
         r->pinned_file = nullptr;
+        if (r->admitted) free_admit_events_.push_back(r->admitted);
+        r->admitted = nullptr;
         if (r->state == Request::Active) --active_;
         r->state = ok ? Request::Done : Request::Failed;
         admit_blocked_ = false;
@@ -544,6 +568,20 @@ int Engine::poll(uint64_t ticket, std::vector<uint8_t>* proof, double* latency_m
     if (err) *err = r->err;
     all_.erase(it);
     return rc;
+}
+
+cudaEvent_t Engine::take_admit_event() {
+    if (!free_admit_events_.empty()) {
+        cudaEvent_t ev = free_admit_events_.back();
+        free_admit_events_.pop_back();
+        return ev;
+    }
+    cudaEvent_t ev = nullptr;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return ev;
 }
 
 bool Engine::finished_or_gone(uint64_t ticket) const {

@@ -142,7 +142,10 @@ class Engine {
     // DM_ENGINE_PRIORITY_DEPTH overrides it; 0: one wave of everything.
     int high_streams_ = 0;
     uint32_t priority_depth_ = 0;
-    cudaEvent_t admit_ev_ = nullptr;
+    cudaEvent_t admit_ev_ = nullptr;  // the whole admission stream, for a request without an event of its own
+    // Admission events of finished requests, for reuse (mu_ held).
+    std::vector<cudaEvent_t> free_admit_events_;
+    cudaEvent_t take_admit_event();
     std::mutex mu_;
     std::condition_variable sched_cv_, done_cv_, work_cv_;
     std::deque<Request*> queued_;  // submitted, not admitted
